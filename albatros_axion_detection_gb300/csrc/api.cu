@@ -1,0 +1,161 @@
+// api.cu -- context, status strings, twiddle tables, FFT plans, scratch.
+#include <math.h>
+#include <stdarg.h>
+#include <string.h>
+
+#include "common.cuh"
+
+namespace ab {
+
+static thread_local char g_err[512] = "";
+
+void set_error(const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+}
+
+bool make_plan(int n, FftPlan* p) {
+  if (n < 1) return false;
+  p->n = n;
+  p->npass = 0;
+  int m = n;
+  const int order[] = {8, 4, 2, 7, 5, 3};
+  // Prefer radix 8; a single leftover factor 2 or 4 is taken as radix 2/4.
+  for (int r : order) {
+    while (m % r == 0) {
+      if (p->npass >= kMaxPasses) return false;
+      p->radix[p->npass++] = r;
+      m /= r;
+    }
+  }
+  if (m != 1) return false;
+  int prod = 1;
+  for (int q = 0; q < p->npass; q++) {
+    prod *= p->radix[q];
+    p->span[q] = n / prod;
+  }
+  return true;
+}
+
+int get_twiddles(ab_ctx* ctx, int64_t T, const float2** out) {
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  auto it = ctx->twiddles.find(T);
+  if (it != ctx->twiddles.end()) {
+    *out = it->second;
+    return AB_OK;
+  }
+  std::vector<float2> h((size_t)T);
+  // exp(-2 pi i e / T) evaluated in double precision and rounded once to
+  // float; the exponent is first folded into [0, T/8] by the symmetries of
+  // sin/cos so the double argument stays small.
+  const double twopi = 6.283185307179586476925286766559;
+  for (int64_t e = 0; e < T; e++) {
+    // reduce e/T to an angle in [0, pi/4] and rebuild (c, s) by symmetry
+    int64_t e8 = e * 8;  // octant = floor(8 e / T)
+    int oct = (int)(e8 / T);
+    int64_t rem = e8 - (int64_t)oct * T;  // in [0, T)
+    double c, s;
+    if (oct % 2 == 0) {
+      double a = twopi * (double)rem / (8.0 * (double)T);
+      c = cos(a); s = sin(a);
+    } else {
+      double a = twopi * (double)(T - rem) / (8.0 * (double)T);
+      c = sin(a); s = cos(a);  // angle = (oct+1)*pi/4 - a
+    }
+    // (c, s) is (cos, sin) of the angle within the octant pair; rotate by
+    // the octant's multiple of pi/2
+    double cc, ss;
+    switch (oct / 2) {
+      case 0: cc = c; ss = s; break;
+      case 1: cc = -s; ss = c; break;
+      case 2: cc = -c; ss = -s; break;
+      default: cc = s; ss = -c; break;
+    }
+    h[(size_t)e] = make_float2((float)cc, (float)(-ss));
+  }
+  float2* d = nullptr;
+  if (cudaMalloc(&d, sizeof(float2) * (size_t)T) != cudaSuccess) {
+    set_error("cudaMalloc of %lld twiddles failed", (long long)T);
+    return AB_ERR_NOMEM;
+  }
+  AB_CUDA(cudaMemcpy(d, h.data(), sizeof(float2) * (size_t)T, cudaMemcpyHostToDevice));
+  ctx->twiddles[T] = d;
+  *out = d;
+  return AB_OK;
+}
+
+int get_scratch(ab_ctx* ctx, int slot, size_t bytes, void** out) {
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  auto& e = ctx->scratch[slot];
+  if (e.second < bytes) {
+    if (e.first) cudaFree(e.first);
+    e.first = nullptr;
+    e.second = 0;
+    if (cudaMalloc(&e.first, bytes) != cudaSuccess) {
+      set_error("cudaMalloc of %zu scratch bytes failed", bytes);
+      return AB_ERR_NOMEM;
+    }
+    e.second = bytes;
+  }
+  *out = e.first;
+  return AB_OK;
+}
+
+}  // namespace ab
+
+extern "C" {
+
+int ab_version(void) { return 10000; }
+
+const char* ab_strerror(int code) {
+  switch (code) {
+    case AB_OK: return "ok";
+    case AB_ERR_ARG: return "invalid argument";
+    case AB_ERR_CUDA: return "CUDA error";
+    case AB_ERR_UNSUPPORTED: return "unsupported size";
+    case AB_ERR_NOMEM: return "device allocation failed";
+    case AB_ERR_STATE: return "invalid state";
+    default: return "unknown status";
+  }
+}
+
+const char* ab_last_error(void) { return ab::g_err; }
+
+int ab_ctx_create(int device, ab_ctx** out) {
+  AB_CHECK_ARG(out != nullptr, "ab_ctx_create: out is NULL");
+  AB_CUDA(cudaSetDevice(device));
+  ab_ctx* c = new ab_ctx();
+  c->device = device;
+  cudaDeviceProp prop;
+  cudaError_t e = cudaGetDeviceProperties(&prop, device);
+  if (e != cudaSuccess) {
+    delete c;
+    ab::set_error("cudaGetDeviceProperties: %s", cudaGetErrorString(e));
+    return AB_ERR_CUDA;
+  }
+  c->num_sms = prop.multiProcessorCount;
+  c->smem_optin = prop.sharedMemPerBlockOptin;
+  const float2* t64 = nullptr;
+  int rc = ab::get_twiddles(c, 64, &t64);
+  if (rc != AB_OK) {
+    delete c;
+    return rc;
+  }
+  c->tw64 = const_cast<float2*>(t64);
+  *out = c;
+  return AB_OK;
+}
+
+int ab_ctx_destroy(ab_ctx* ctx) {
+  if (!ctx) return AB_OK;
+  cudaSetDevice(ctx->device);
+  for (auto& kv : ctx->twiddles) cudaFree(kv.second);
+  for (auto& kv : ctx->scratch)
+    if (kv.second.first) cudaFree(kv.second.first);
+  delete ctx;
+  return AB_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,250 @@
+// chain.cu -- streaming unpack -> IPFB -> PFB(osamp) -> fine xcorr, the
+// GB300 form of repfb_xcorr_avg
+// (albatros_analysis/scripts/xcorr/helper_gpu_stream_clean.py:295-456).
+//
+// Per pushed chunk of acclen new spectra (all M = 2*nant inputs at once):
+//   1. row stage   : decode the 4-bit packets of local rows [0, nslice)
+//                    (global spectra chunk*acclen - 2cut ...), place the
+//                    selected channels, P-point inverse FFT, write the
+//                    [n][t] intermediate (ping-pong buffer chunk % 2);
+//   2. time stage  : per column, rfft -> Wiener filter (evaluated on the
+//                    fly from the ntap window taps) -> irfft, in place;
+//   3. PFB stage A : tap fold + osamp-point DFT for every fine block whose
+//                    ntap*osamp rows are now available (rows before this
+//                    chunk come from the other ping-pong buffer);
+//   4. PFB stage B : osamp fine offsets x P-point DFT, keeping only the
+//                    fine band [q0, q1);
+//   5. correlate   : accumulate Y_i conj(Y_j) / nblock into each block's job.
+//
+// The reference's overlap state (the 2*cut coarse rows carried between IPFB
+// chunks and the ntap-1 fine blocks carried between PFB jobs) is realised by
+// re-decoding the previous 2*cut packets in step 1 and by reading the previous
+// chunk's IPFB output in step 3; nothing is copied between chunks.
+#include <algorithm>
+
+#include "ipfb.cuh"
+#include "pfb.cuh"
+
+namespace ab {
+int launch_xcorr_accum(const float2* Y, int M, int64_t nb, int64_t F, int64_t b_lo, int64_t b_hi, float2* vis,
+                       float scale, cudaStream_t s);
+}
+
+using namespace ab;
+
+struct ab_stream {
+  ab_ctx* ctx = nullptr;
+  int nant = 0, M = 0, P = 4096, O = 1, ntap = 4;
+  int64_t nchan_raw = 0, nsel = 0, acclen = 0, cut = 0, nslice = 0;
+  int64_t nblock = 0, njobs = 0, q0 = 0, q1 = 0, nq = 0;
+  float thresh = 0.f;
+  FftPlan planP{}, planM{};
+  const float2 *twP = nullptr, *twN = nullptr, *twL = nullptr;
+  int32_t *d_cols = nullptr, *d_abs = nullptr;
+  float* d_wtaps = nullptr;  // IPFB filter window taps (ntap, P)
+  float* d_win = nullptr;    // PFB window (ntap * L)
+  float* interm[2] = {nullptr, nullptr};
+  float* W = nullptr;
+  float2* Y = nullptr;
+  float2* vis = nullptr;
+  int64_t nb_max = 0;
+  int64_t chunks_done = 0;  // next chunk expected
+  int64_t blocks_done = 0;  // fine blocks already correlated
+  int64_t launches = 0;
+};
+
+static void stream_free(ab_stream* st) {
+  cudaFree(st->d_cols);
+  cudaFree(st->d_abs);
+  cudaFree(st->d_wtaps);
+  cudaFree(st->d_win);
+  cudaFree(st->interm[0]);
+  cudaFree(st->interm[1]);
+  cudaFree(st->W);
+  cudaFree(st->Y);
+  cudaFree(st->vis);
+}
+
+#define AB_ALLOC(ptr, bytes)                                              \
+  do {                                                                    \
+    if (cudaMalloc((void**)&(ptr), (bytes)) != cudaSuccess) {             \
+      set_error("ab_stream_create: cudaMalloc of %zu bytes failed", (size_t)(bytes)); \
+      stream_free(st);                                                    \
+      delete st;                                                          \
+      return AB_ERR_NOMEM;                                                \
+    }                                                                     \
+  } while (0)
+
+extern "C" int ab_stream_create(ab_ctx* ctx, int64_t nant, int64_t nchan_raw, const int64_t* chan_cols,
+                                const int64_t* chan_abs, int64_t nsel, int64_t acclen, int64_t cut, int64_t osamp,
+                                int64_t ntap, double thresh, int64_t nblock, int64_t njobs, int64_t q0, int64_t q1,
+                                ab_stream** out) {
+  AB_CHECK_ARG(ctx && chan_cols && chan_abs && out, "ab_stream_create: NULL pointer");
+  AB_CHECK_ARG(nant >= 1 && nchan_raw >= 1 && nsel >= 1 && acclen >= 1 && cut >= 1 && ntap >= 1 && ntap <= 8,
+               "ab_stream_create: bad sizes (cut >= 1, 1 <= ntap <= 8)");
+  AB_CHECK_ARG(acclen >= 2 * cut, "ab_stream_create: acclen must be >= 2*cut");
+  AB_CHECK_ARG(acclen >= ntap * osamp, "ab_stream_create: acclen must be >= ntap*osamp");
+  AB_CHECK_ARG(osamp >= 1 && osamp <= 64 && (osamp & (osamp - 1)) == 0, "ab_stream_create: osamp must be 1..64, power of two");
+  AB_CHECK_ARG(nblock >= 1 && njobs >= 0, "ab_stream_create: bad nblock/njobs");
+  const int P = 4096;
+  AB_CHECK_ARG(q0 % osamp == 0 && q1 % osamp == 0 && q0 >= 0 && q1 > q0 && q1 / osamp <= P / 2,
+               "ab_stream_create: band [%lld, %lld) must be multiples of osamp inside [0, 2048*osamp]", (long long)q0,
+               (long long)q1);
+  for (int64_t k = 0; k < nsel; k++) {
+    AB_CHECK_ARG(chan_cols[k] >= 0 && chan_cols[k] < nchan_raw, "ab_stream_create: channel column out of range");
+    AB_CHECK_ARG(chan_abs[k] >= 0 && chan_abs[k] <= P / 2, "ab_stream_create: absolute channel out of range");
+  }
+  ab_stream* st = new ab_stream();
+  st->ctx = ctx;
+  st->nant = (int)nant;
+  st->M = (int)(2 * nant);
+  st->P = P;
+  st->O = (int)osamp;
+  st->ntap = (int)ntap;
+  st->nchan_raw = nchan_raw;
+  st->nsel = nsel;
+  st->acclen = acclen;
+  st->cut = cut;
+  st->nslice = acclen + 2 * cut;
+  st->nblock = nblock;
+  st->njobs = njobs;
+  st->q0 = q0;
+  st->q1 = q1;
+  st->nq = q1 - q0;
+  st->thresh = (float)thresh;
+  if (st->nslice % 2 || !make_plan((int)(st->nslice / 2), &st->planM) || !make_plan(P, &st->planP)) {
+    set_error("ab_stream_create: nslice = acclen + 2*cut = %lld must be even with nslice/2 factoring into 2,3,5,7",
+              (long long)st->nslice);
+    delete st;
+    return AB_ERR_UNSUPPORTED;
+  }
+  if ((size_t)(st->nslice / 2) * sizeof(float2) > ctx->smem_optin) {
+    set_error("ab_stream_create: nslice %lld exceeds the shared-memory column limit", (long long)st->nslice);
+    delete st;
+    return AB_ERR_UNSUPPORTED;
+  }
+  int rc;
+  if ((rc = get_twiddles(ctx, P, &st->twP)) != AB_OK || (rc = get_twiddles(ctx, st->nslice, &st->twN)) != AB_OK ||
+      (rc = get_twiddles(ctx, (int64_t)P * osamp, &st->twL)) != AB_OK) {
+    delete st;
+    return rc;
+  }
+  const int64_t L = (int64_t)P * osamp;
+  const int M = st->M;
+  st->nb_max = acclen / osamp + ntap + 1;
+  AB_ALLOC(st->d_cols, sizeof(int32_t) * nsel);
+  AB_ALLOC(st->d_abs, sizeof(int32_t) * nsel);
+  AB_ALLOC(st->d_wtaps, sizeof(float) * ntap * P);
+  AB_ALLOC(st->d_win, sizeof(float) * ntap * L);
+  for (int i = 0; i < 2; i++) AB_ALLOC(st->interm[i], sizeof(float) * (size_t)M * P * st->nslice);
+  AB_ALLOC(st->W, sizeof(float) * (size_t)M * st->nb_max * L);
+  AB_ALLOC(st->Y, sizeof(float2) * (size_t)M * st->nb_max * st->nq);
+  AB_ALLOC(st->vis, sizeof(float2) * (size_t)std::max<int64_t>(njobs, 1) * M * M * st->nq);
+  std::vector<int32_t> hc(nsel), ha(nsel);
+  for (int64_t k = 0; k < nsel; k++) {
+    hc[k] = (int32_t)chan_cols[k];
+    ha[k] = (int32_t)chan_abs[k];
+  }
+  std::vector<double> w;
+  sinc_hamming_host((int)ntap, P, w);  // IPFB: window of the coarse PFB (lblock 4096)
+  std::vector<float> wf(w.begin(), w.end());
+  sinc_hamming_host((int)ntap, L, w);  // PFB: window of the fine PFB
+  std::vector<float> wl(w.begin(), w.end());
+  bool ok = cudaMemcpy(st->d_cols, hc.data(), sizeof(int32_t) * nsel, cudaMemcpyHostToDevice) == cudaSuccess &&
+            cudaMemcpy(st->d_abs, ha.data(), sizeof(int32_t) * nsel, cudaMemcpyHostToDevice) == cudaSuccess &&
+            cudaMemcpy(st->d_wtaps, wf.data(), sizeof(float) * wf.size(), cudaMemcpyHostToDevice) == cudaSuccess &&
+            cudaMemcpy(st->d_win, wl.data(), sizeof(float) * wl.size(), cudaMemcpyHostToDevice) == cudaSuccess &&
+            cudaMemset(st->vis, 0, sizeof(float2) * (size_t)std::max<int64_t>(njobs, 1) * M * M * st->nq) == cudaSuccess;
+  if (!ok) {
+    set_error("ab_stream_create: upload failed");
+    stream_free(st);
+    delete st;
+    return AB_ERR_CUDA;
+  }
+  *out = st;
+  return AB_OK;
+}
+
+extern "C" int ab_stream_destroy(ab_stream* st) {
+  if (!st) return AB_OK;
+  stream_free(st);
+  delete st;
+  return AB_OK;
+}
+
+extern "C" int ab_stream_reset(ab_stream* st, void* stream) {
+  AB_CHECK_ARG(st, "ab_stream_reset: NULL stream object");
+  st->chunks_done = 0;
+  st->blocks_done = 0;
+  st->launches = 0;
+  AB_CUDA(cudaMemsetAsync(st->vis, 0, sizeof(float2) * (size_t)std::max<int64_t>(st->njobs, 1) * st->M * st->M * st->nq,
+                          as_stream(stream)));
+  return AB_OK;
+}
+
+extern "C" const float* ab_stream_vis(const ab_stream* st) { return st ? (const float*)st->vis : nullptr; }
+extern "C" int64_t ab_stream_kernel_launches(const ab_stream* st) { return st ? st->launches : -1; }
+
+// Push chunk `chunk`.  final != 0 marks the last chunk of the stream: every
+// remaining block of the planned jobs is then produced with zeros past the end
+// (the reference's zero-padded last job, helper_gpu_stream_clean.py:163-167).
+static int stream_push(ab_stream* st, const uint8_t* raw, int64_t ant_stride, const int32_t* spec_map,
+                       int64_t map_stride, int64_t chunk, bool final, cudaStream_t s) {
+  AB_CHECK_ARG(raw, "ab_stream_push: NULL raw pointer");
+  AB_CHECK_ARG(chunk == st->chunks_done, "ab_stream_push: expected chunk %lld, got %lld", (long long)st->chunks_done,
+               (long long)chunk);
+  const int P = st->P, O = st->O, M = st->M;
+  const int64_t acclen = st->acclen, cut = st->cut, nslice = st->nslice;
+  float* cur = st->interm[chunk & 1];
+  float* prev = chunk > 0 ? st->interm[(chunk - 1) & 1] : nullptr;
+  // 1. row stage
+  Packed4Src src{raw, ant_stride, 2 * st->nchan_raw, spec_map, map_stride, chunk * acclen - 2 * cut,
+                 st->d_cols, st->d_abs, (int)st->nsel};
+  AB_TRY(launch_row_stage_packed4(src, st->nant, (int)nslice, P, st->planP, st->twP, cur, nslice, s));
+  // 2. time stage
+  AB_TRY(launch_time_stage(cur, nslice, M, P, (int)nslice, st->planM, st->twN, nullptr, st->d_wtaps, st->ntap,
+                           st->thresh, st->ctx->smem_optin, s));
+  st->launches += 2;
+  // 3-5. fine blocks now complete: block B needs timestream rows
+  // [B*O, (B+ntap)*O); rows [0, (chunk+1)*acclen) exist.
+  const int64_t total_blocks = st->njobs * st->nblock;
+  const int64_t rows_avail = (chunk + 1) * acclen;
+  int64_t b_end = rows_avail / O - st->ntap + 1;  // exclusive
+  if (final) b_end = total_blocks;
+  if (b_end > total_blocks) b_end = total_blocks;
+  st->chunks_done++;
+  while (st->blocks_done < b_end) {
+    int64_t nb = std::min(b_end - st->blocks_done, st->nb_max);
+    int64_t row0 = st->blocks_done * O - chunk * acclen;  // local row of the first block
+    AB_CHECK_ARG(row0 >= -acclen || chunk == 0, "ab_stream_push: internal block bookkeeping error");
+    TsSrc ts{cur, prev, nslice, cut, cut + acclen, acclen, 0};
+    AB_TRY(launch_pfb_stage_a(ts, M, P, O, st->ntap, row0, nb, st->d_win, st->W, st->ctx->tw64, s));
+    AB_TRY(launch_pfb_stage_b(st->W, M, P, O, nb, st->planP, st->twL, (int)(st->q0 / O), (int)(st->q1 / O), st->Y, s));
+    st->launches += 2;
+    // correlate, split at job boundaries
+    int64_t b = st->blocks_done, bend = st->blocks_done + nb;
+    while (b < bend) {
+      int64_t job = b / st->nblock;
+      int64_t jend = std::min(bend, (job + 1) * st->nblock);
+      AB_TRY(launch_xcorr_accum(st->Y, M, nb, st->nq, b - st->blocks_done, jend - st->blocks_done,
+                                st->vis + job * (int64_t)M * M * st->nq, 1.0f / (float)st->nblock, s));
+      st->launches++;
+      b = jend;
+    }
+    st->blocks_done = bend;
+  }
+  return AB_OK;
+}
+
+extern "C" int ab_stream_push(ab_stream* st, const uint8_t* raw, int64_t ant_stride, const int32_t* spec_map,
+                              int64_t map_stride, int64_t chunk, void* stream) {
+  AB_CHECK_ARG(st, "ab_stream_push: NULL stream object");
+  return stream_push(st, raw, ant_stride, spec_map, map_stride, chunk, false, as_stream(stream));
+}
+
+// Last chunk of a stream: also produces the zero-padded tail blocks.
+extern "C" int ab_stream_push_final(ab_stream* st, const uint8_t* raw, int64_t ant_stride, const int32_t* spec_map,
+                                    int64_t map_stride, int64_t chunk, void* stream) {
+  AB_CHECK_ARG(st, "ab_stream_push_final: NULL stream object");
+  return stream_push(st, raw, ant_stride, spec_map, map_stride, chunk, true, as_stream(stream));
+}

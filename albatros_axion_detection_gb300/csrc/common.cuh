@@ -1,0 +1,84 @@
+// common.cuh -- status codes, error capture, the library context (twiddle
+// tables, FFT plans, grow-only scratch) shared by all translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/albatros_gb300.h"
+#include "fft.cuh"
+
+namespace ab {
+
+// thread-local detail message for the last failing call
+void set_error(const char* fmt, ...);
+
+#define AB_CHECK_ARG(cond, ...)        \
+  do {                                 \
+    if (!(cond)) {                     \
+      ::ab::set_error(__VA_ARGS__);    \
+      return AB_ERR_ARG;               \
+    }                                  \
+  } while (0)
+
+#define AB_CUDA(call)                                                                  \
+  do {                                                                                 \
+    cudaError_t e_ = (call);                                                           \
+    if (e_ != cudaSuccess) {                                                           \
+      ::ab::set_error("%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, \
+                      __LINE__);                                                       \
+      return AB_ERR_CUDA;                                                              \
+    }                                                                                  \
+  } while (0)
+
+#define AB_LAUNCH_CHECK()                                                                 \
+  do {                                                                                    \
+    cudaError_t e_ = cudaGetLastError();                                                  \
+    if (e_ != cudaSuccess) {                                                              \
+      ::ab::set_error("kernel launch failed: %s (%s:%d)", cudaGetErrorString(e_), __FILE__, \
+                      __LINE__);                                                          \
+      return AB_ERR_CUDA;                                                                 \
+    }                                                                                     \
+  } while (0)
+
+#define AB_TRY(expr)          \
+  do {                        \
+    int rc_ = (expr);         \
+    if (rc_ != AB_OK) return rc_; \
+  } while (0)
+
+inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+// Factorise n into supported radices (8, 4, 2, 7, 5, 3). Returns false if n
+// has another prime factor.
+bool make_plan(int n, FftPlan* p);
+
+}  // namespace ab
+
+// The opaque context of the C-ABI.
+struct ab_ctx {
+  int device = 0;
+  int num_sms = 0;
+  size_t smem_optin = 0;
+  std::mutex mu;
+  // twiddle tables exp(-2 pi i e / T), e in [0, T), keyed by T
+  std::map<int64_t, float2*> twiddles;
+  // grow-only scratch buffers keyed by slot
+  std::map<int, std::pair<void*, size_t>> scratch;
+  float2* tw64 = nullptr;  // exp(-2 pi i e / 64)
+};
+
+namespace ab {
+// Device twiddle table of length T (cached in ctx; uploaded synchronously on
+// first use, so call outside stream capture).
+int get_twiddles(ab_ctx* ctx, int64_t T, const float2** out);
+// Grow-only device scratch; the pointer stays valid until a larger request
+// for the same slot.
+int get_scratch(ab_ctx* ctx, int slot, size_t bytes, void** out);
+enum ScratchSlot { kScratchPfbW = 1, kScratchXcorrG = 2, kScratchChain = 3, kScratchYband = 4 };
+}  // namespace ab

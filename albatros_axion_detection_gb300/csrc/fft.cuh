@@ -1,0 +1,276 @@
+// fft.cuh -- in-place mixed-radix FFT passes on shared memory, and small
+// register FFTs, for the IPFB / PFB kernels.
+//
+// Shared-memory transforms (one CTA owns one sequence of length n):
+//   * dif_forward: natural-order input -> spectrum in digit-reversed order
+//     (Sande-Tukey decimation in frequency, radices R_1..R_m applied in order);
+//   * dit_inverse: the adjoint sequence of passes, digit-reversed input ->
+//     natural-order output of the unnormalised inverse DFT.
+// Running dif_forward, a pointwise operation addressed through
+// fft_pos(), then dit_inverse needs no permutation pass at all.
+//
+// Position of frequency f after dif_forward: write f in mixed radix with R_1
+// as the least significant digit, f = f_1 + R_1 f_2 + R_1 R_2 f_3 + ...; then
+// pos(f) = sum_p f_p * S_p with S_p = n / (R_1 ... R_p).
+//
+// Twiddles come from a table tw[e] = exp(-2 pi i e / T) for e in [0, T)
+// (T a multiple of n), computed on the host in double precision and rounded
+// to float once.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace ab {
+
+constexpr int kMaxPasses = 12;
+
+struct FftPlan {
+  int n;                  // transform length (complex points)
+  int npass;
+  int radix[kMaxPasses];  // R_p
+  int span[kMaxPasses];   // S_p = n / (R_1 .. R_p)
+};
+
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+__device__ __forceinline__ float2 cmulc(float2 a, float2 b) {  // a * conj(b)
+  return make_float2(fmaf(a.x, b.x, a.y * b.y), fmaf(a.y, b.x, -a.x * b.y));
+}
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
+__device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+// multiply by -i (forward) or +i (inverse)
+template <bool INV>
+__device__ __forceinline__ float2 mul_mi(float2 a) {
+  return INV ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
+}
+
+// ---- small DFTs in registers, forward uses exp(-2 pi i rk / R) ----------
+template <bool INV>
+__device__ __forceinline__ void dft2(float2* x) {
+  float2 a = x[0], b = x[1];
+  x[0] = cadd(a, b);
+  x[1] = csub(a, b);
+}
+
+template <bool INV>
+__device__ __forceinline__ void dft4(float2* x) {
+  float2 s02 = cadd(x[0], x[2]), d02 = csub(x[0], x[2]);
+  float2 s13 = cadd(x[1], x[3]), d13 = mul_mi<INV>(csub(x[1], x[3]));
+  x[0] = cadd(s02, s13);
+  x[2] = csub(s02, s13);
+  x[1] = cadd(d02, d13);
+  x[3] = csub(d02, d13);
+}
+
+template <bool INV>
+__device__ __forceinline__ void dft8(float2* x) {
+  const float h = 0.7071067811865476f;
+  float2 a[4] = {x[0], x[2], x[4], x[6]}, b[4] = {x[1], x[3], x[5], x[7]};
+  dft4<INV>(a);
+  dft4<INV>(b);
+  // twiddles w8^k, k = 0..3 (forward w8 = exp(-i pi/4))
+  float2 b1 = INV ? make_float2(h * (b[1].x - b[1].y), h * (b[1].x + b[1].y))
+                  : make_float2(h * (b[1].x + b[1].y), h * (b[1].y - b[1].x));
+  float2 b2 = mul_mi<INV>(b[2]);
+  float2 b3 = INV ? make_float2(-h * (b[3].x + b[3].y), h * (b[3].x - b[3].y))
+                  : make_float2(h * (b[3].y - b[3].x), -h * (b[3].x + b[3].y));
+  x[0] = cadd(a[0], b[0]);
+  x[4] = csub(a[0], b[0]);
+  x[1] = cadd(a[1], b1);
+  x[5] = csub(a[1], b1);
+  x[2] = cadd(a[2], b2);
+  x[6] = csub(a[2], b2);
+  x[3] = cadd(a[3], b3);
+  x[7] = csub(a[3], b3);
+}
+
+// odd prime R: y_k = x0 + sum_r a_r cos(2pi rk/R) -/+ i sum_r b_r sin(2pi rk/R)
+template <int R, bool INV>
+__device__ __forceinline__ void dft_odd(float2* x, const float* cs, const float* sn) {
+  constexpr int H = (R - 1) / 2;
+  float2 a[H], b[H];
+  float2 y0 = x[0];
+#pragma unroll
+  for (int r = 1; r <= H; r++) {
+    a[r - 1] = cadd(x[r], x[R - r]);
+    b[r - 1] = csub(x[r], x[R - r]);
+    y0 = cadd(y0, a[r - 1]);
+  }
+  float2 out[R];
+  out[0] = y0;
+#pragma unroll
+  for (int k = 1; k <= H; k++) {
+    float2 t1 = x[0], t2 = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int r = 1; r <= H; r++) {
+      int idx = (r * k) % R;  // cos(2pi rk/R) = cos(2pi idx/R)
+      float c = idx <= H ? cs[idx] : cs[R - idx];
+      float s = idx <= H ? sn[idx] : -sn[R - idx];
+      t1.x = fmaf(a[r - 1].x, c, t1.x);
+      t1.y = fmaf(a[r - 1].y, c, t1.y);
+      t2.x = fmaf(b[r - 1].x, s, t2.x);
+      t2.y = fmaf(b[r - 1].y, s, t2.y);
+    }
+    float2 it2 = mul_mi<INV>(t2);  // -i t2 (forward)
+    out[k] = cadd(t1, it2);
+    out[R - k] = csub(t1, it2);
+  }
+#pragma unroll
+  for (int k = 0; k < R; k++) x[k] = out[k];
+}
+
+template <bool INV>
+__device__ __forceinline__ void dft3(float2* x) {
+  const float cs[2] = {1.f, -0.5f}, sn[2] = {0.f, 0.8660254037844387f};
+  dft_odd<3, INV>(x, cs, sn);
+}
+template <bool INV>
+__device__ __forceinline__ void dft5(float2* x) {
+  const float cs[3] = {1.f, 0.30901699437494745f, -0.8090169943749473f};
+  const float sn[3] = {0.f, 0.9510565162951535f, 0.5877852522924732f};
+  dft_odd<5, INV>(x, cs, sn);
+}
+template <bool INV>
+__device__ __forceinline__ void dft7(float2* x) {
+  const float cs[4] = {1.f, 0.6234898018587336f, -0.22252093395631434f, -0.900968867902419f};
+  const float sn[4] = {0.f, 0.7818314824680298f, 0.9749279121818236f, 0.43388373911755823f};
+  dft_odd<7, INV>(x, cs, sn);
+}
+
+template <int R, bool INV>
+__device__ __forceinline__ void dft_small(float2* x) {
+  if constexpr (R == 2) dft2<INV>(x);
+  else if constexpr (R == 3) dft3<INV>(x);
+  else if constexpr (R == 4) dft4<INV>(x);
+  else if constexpr (R == 5) dft5<INV>(x);
+  else if constexpr (R == 7) dft7<INV>(x);
+  else if constexpr (R == 8) dft8<INV>(x);
+}
+
+// One DIF pass of radix R over buf[0..n): butterfly, then twiddle.
+// tw has length T; twiddle exponent j*k*(T/(R*S)).
+template <int R>
+__device__ __forceinline__ void dif_pass(float2* buf, int n, int S, const float2* __restrict__ tw, int T,
+                                         int tid, int nthr) {
+  const int nbf = n / R;
+  const int tstep = T / (R * S);
+  for (int bf = tid; bf < nbf; bf += nthr) {
+    int blk = bf / S, j = bf - blk * S;
+    int base = blk * R * S + j;
+    float2 x[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) x[r] = buf[base + r * S];
+    dft_small<R, false>(x);
+    if (j) {
+#pragma unroll
+      for (int k = 1; k < R; k++) x[k] = cmul(x[k], __ldg(&tw[j * k * tstep]));
+    }
+#pragma unroll
+    for (int k = 0; k < R; k++) buf[base + k * S] = x[k];
+  }
+}
+
+// One DIT (adjoint) pass: conjugate twiddle, then inverse butterfly.
+template <int R>
+__device__ __forceinline__ void dit_pass(float2* buf, int n, int S, const float2* __restrict__ tw, int T,
+                                         int tid, int nthr) {
+  const int nbf = n / R;
+  const int tstep = T / (R * S);
+  for (int bf = tid; bf < nbf; bf += nthr) {
+    int blk = bf / S, j = bf - blk * S;
+    int base = blk * R * S + j;
+    float2 x[R];
+#pragma unroll
+    for (int r = 0; r < R; r++) x[r] = buf[base + r * S];
+    if (j) {
+#pragma unroll
+      for (int k = 1; k < R; k++) x[k] = cmulc(x[k], __ldg(&tw[j * k * tstep]));
+    }
+    dft_small<R, true>(x);
+#pragma unroll
+    for (int k = 0; k < R; k++) buf[base + k * S] = x[k];
+  }
+}
+
+template <bool INV>
+__device__ __forceinline__ void run_pass(int R, float2* buf, int n, int S, const float2* tw, int T, int tid,
+                                         int nthr) {
+  switch (R) {
+    case 2: INV ? dit_pass<2>(buf, n, S, tw, T, tid, nthr) : dif_pass<2>(buf, n, S, tw, T, tid, nthr); break;
+    case 3: INV ? dit_pass<3>(buf, n, S, tw, T, tid, nthr) : dif_pass<3>(buf, n, S, tw, T, tid, nthr); break;
+    case 4: INV ? dit_pass<4>(buf, n, S, tw, T, tid, nthr) : dif_pass<4>(buf, n, S, tw, T, tid, nthr); break;
+    case 5: INV ? dit_pass<5>(buf, n, S, tw, T, tid, nthr) : dif_pass<5>(buf, n, S, tw, T, tid, nthr); break;
+    case 7: INV ? dit_pass<7>(buf, n, S, tw, T, tid, nthr) : dif_pass<7>(buf, n, S, tw, T, tid, nthr); break;
+    case 8: INV ? dit_pass<8>(buf, n, S, tw, T, tid, nthr) : dif_pass<8>(buf, n, S, tw, T, tid, nthr); break;
+    default: break;
+  }
+}
+
+// Forward transform, whole CTA, natural -> digit-reversed. Caller syncs before.
+__device__ __forceinline__ void dif_forward(float2* buf, const FftPlan& p, const float2* tw, int T) {
+  for (int q = 0; q < p.npass; q++) {
+    run_pass<false>(p.radix[q], buf, p.n, p.span[q], tw, T, threadIdx.x, blockDim.x);
+    __syncthreads();
+  }
+}
+
+// Inverse (unnormalised) transform, digit-reversed -> natural. Caller syncs before.
+__device__ __forceinline__ void dit_inverse(float2* buf, const FftPlan& p, const float2* tw, int T) {
+  for (int q = p.npass - 1; q >= 0; q--) {
+    run_pass<true>(p.radix[q], buf, p.n, p.span[q], tw, T, threadIdx.x, blockDim.x);
+    __syncthreads();
+  }
+}
+
+// Storage position of frequency f after dif_forward.
+__device__ __forceinline__ int fft_pos(const FftPlan& p, int f) {
+  int pos = 0;
+  for (int q = 0; q < p.npass; q++) {
+    int R = p.radix[q];
+    int d = f % R;
+    f /= R;
+    pos += d * p.span[q];
+  }
+  return pos;
+}
+
+// ---- register FFT of compile-time power-of-two length N <= 64 ------------
+// Forward, natural order in and out; twiddles from a constant table of
+// exp(-2 pi i e / 64), e in [0, 64).
+template <int N>
+__device__ __forceinline__ void reg_fft_pow2(float2 (&x)[N], const float2* __restrict__ tw64) {
+  static_assert(N >= 1 && N <= 64 && (N & (N - 1)) == 0, "N must be a power of two <= 64");
+  if constexpr (N == 1) return;
+  else {
+    // bit reversal
+#pragma unroll
+    for (int i = 0; i < N; i++) {
+      int j = 0;
+#pragma unroll
+      for (int b = 1, t = i; b < N; b <<= 1, t >>= 1) j = (j << 1) | (t & 1);
+      if (i < j) {
+        float2 t = x[i];
+        x[i] = x[j];
+        x[j] = t;
+      }
+    }
+#pragma unroll
+    for (int len = 2; len <= N; len <<= 1) {
+#pragma unroll
+      for (int i = 0; i < N; i += len) {
+#pragma unroll
+        for (int k = 0; k < len / 2; k++) {
+          float2 w = tw64[k * (64 / len)];
+          float2 u = x[i + k], v = cmul(x[i + k + len / 2], w);
+          x[i + k] = cadd(u, v);
+          x[i + k + len / 2] = csub(u, v);
+        }
+      }
+    }
+  }
+}
+
+}  // namespace ab

@@ -1,0 +1,264 @@
+// pfb.cu -- forward PFB (cupy_pfb, albatros_analysis/src/utils/pfb_gpu_utils.py:105-121):
+//   y[b, k] = sum_{i<ntap} ts[(b+i) L + k] win[i L + k];  out[b] = rfft(y[b])
+// computed as stage A (tap fold + O-point real DFT over t', k = n + P t')
+// and stage B (twiddle + P-point DFT over n), see pfb.cuh.
+#include "pfb.cuh"
+
+namespace ab {
+
+constexpr int kFoldCols = 32;   // sample phases per CTA (one warp lane each)
+constexpr int kFoldBlocks = 8;  // output blocks per CTA (one warp each)
+
+template <int O>
+__global__ void __launch_bounds__(kFoldCols* kFoldBlocks)
+    pfb_stage_a_kernel(TsSrc src, int P, int ntap, int64_t row0, int64_t nb, const float* __restrict__ win,
+                       float* __restrict__ W, const float2* __restrict__ tw64) {
+  extern __shared__ float tile[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int n0 = blockIdx.y * kFoldCols;
+  const int64_t b0 = (int64_t)blockIdx.x * kFoldBlocks;
+  const int in = blockIdx.z;
+  const int RW = (kFoldBlocks + ntap - 1) * O;  // rows in the tile
+  const int pitch = RW + 1;                     // odd pitch: conflict-free columns
+  const int64_t rbase = row0 + b0 * O;          // first tile row (timestream row)
+  // ---- load tile[n][r] = ts(rbase + r, n0 + n) ----
+  if (src.natural) {
+    for (int r = warp; r < RW; r += kFoldBlocks) {
+      int64_t rr = rbase + r;
+      float v = 0.f;
+      if (rr >= 0 && rr < src.nrows_valid) v = __ldg(&src.cur[rr * P + n0 + lane]);
+      tile[lane * pitch + r] = v;
+    }
+  } else {
+    for (int c = warp; c < kFoldCols; c += kFoldBlocks) {
+      const int64_t colbase = ((int64_t)in * P + n0 + c) * src.ld;
+      for (int r = lane; r < RW; r += 32) {
+        int64_t rr = rbase + r;
+        float v = 0.f;
+        if (rr < src.nrows_valid) {
+          if (rr >= 0) v = __ldg(&src.cur[colbase + src.off + rr]);
+          else if (src.prev) v = __ldg(&src.prev[colbase + src.prev_off + rr]);
+        }
+        tile[c * pitch + r] = v;
+      }
+    }
+  }
+  __syncthreads();
+  const int64_t b = b0 + warp;
+  if (b >= nb) return;
+  const int n = n0 + lane;
+  const float* col = tile + lane * pitch + warp * O;
+  // tap fold: y[t'] = sum_i ts((b+i) O + t') win[(i O + t') P + n]
+  constexpr int H = O > 1 ? O / 2 : 1;
+  float2 z[H];
+#pragma unroll
+  for (int m = 0; m < H; m++) z[m] = make_float2(0.f, 0.f);
+  for (int i = 0; i < ntap; i++) {
+    const float* wrow = win + (int64_t)i * O * P + n;
+#pragma unroll
+    for (int tp = 0; tp < O; tp++) {
+      float v = col[i * O + tp] * __ldg(&wrow[(int64_t)tp * P]);
+      if (O == 1) z[0].x += v;
+      else if (tp & 1) z[tp >> 1].y += v;
+      else z[tp >> 1].x += v;
+    }
+  }
+  const int GW = O < 8 ? O : 8;
+  const int NG = O / GW;
+  float* Wb = W + (((int64_t)in * nb + b) * NG * P) * GW;
+  if constexpr (O == 1) {
+    Wb[n] = z[0].x;
+  } else {
+    reg_fft_pow2<H>(z, tw64);
+    float out[O];
+    out[0] = z[0].x + z[0].y;  // W_0
+    out[1] = z[0].x - z[0].y;  // W_{O/2}
+#pragma unroll
+    for (int k = 1; k < H; k++) {
+      float2 zk = z[k], zc = cconj(z[H - k]);
+      float2 E = cscale(cadd(zk, zc), 0.5f);
+      float2 Dd = csub(zk, zc);                        // 2 i O_k
+      float2 Od = make_float2(0.5f * Dd.y, -0.5f * Dd.x);  // O_k
+      float2 w = tw64[k * (64 / O)];                   // exp(-2 pi i k / O)
+      float2 Wk = cadd(E, cmul(w, Od));
+      out[2 * k] = Wk.x;
+      out[2 * k + 1] = Wk.y;
+    }
+#pragma unroll
+    for (int g = 0; g < NG; g++) {
+      float* dst = Wb + ((int64_t)g * P + n) * GW;
+      if constexpr (O >= 4) {
+#pragma unroll
+        for (int e = 0; e < GW; e += 4)
+          *reinterpret_cast<float4*>(dst + e) =
+              make_float4(out[g * GW + e], out[g * GW + e + 1], out[g * GW + e + 2], out[g * GW + e + 3]);
+      } else {
+#pragma unroll
+        for (int e = 0; e < GW; e++) dst[e] = out[g * GW + e];
+      }
+    }
+  }
+}
+
+// Stage B: one CTA per (group g, block b, input).  Loads the group's P x GW
+// floats, then for each fine offset s carried by the group forms
+// V_s[n] = W_s[n] exp(-2 pi i s n / L) and its P-point DFT.
+constexpr int kStageBThreads = 512;
+
+__global__ void __launch_bounds__(kStageBThreads)
+    pfb_stage_b_kernel(const float* __restrict__ W, int P, int O, int64_t nb, FftPlan plan,
+                       const float2* __restrict__ twL, int u0, int u1, float2* __restrict__ out) {
+  extern __shared__ float4 smem4[];
+  const int GW = O < 8 ? O : 8, NG = O / GW;
+  const int g = blockIdx.y;
+  const int64_t b = blockIdx.x;
+  const int in = blockIdx.z;
+  float* wt = reinterpret_cast<float*>(smem4);          // P * GW floats
+  float2* buf = reinterpret_cast<float2*>(wt + (size_t)P * GW);  // P complex
+  const float* src = W + ((((int64_t)in * nb + b) * NG + g) * P) * GW;
+  if (GW >= 4) {
+    const float4* s4 = reinterpret_cast<const float4*>(src);
+    for (int i = threadIdx.x; i < P * GW / 4; i += blockDim.x) smem4[i] = __ldg(&s4[i]);
+  } else {
+    for (int i = threadIdx.x; i < P * GW; i += blockDim.x) wt[i] = __ldg(&src[i]);
+  }
+  __syncthreads();
+  const int64_t L = (int64_t)P * O;
+  const bool full = u1 < 0;
+  const int64_t nq = full ? L / 2 + 1 : (int64_t)(u1 - u0) * O;
+  float2* ob = out + ((int64_t)in * nb + b) * nq;
+  // slots of this group: pairs of floats (e, e+1), e even
+  for (int e = 0; e < GW; e += (GW == 1 ? 1 : 2)) {
+    const int c = (g * GW + e) / 2;  // complex slot index (0 holds W_0 / W_{O/2})
+    const int nv = (GW == 1) ? 1 : 2;
+    for (int v = 0; v < nv; v++) {
+      int s;
+      if (c == 0) s = (v == 0) ? 0 : O / 2;
+      else s = (v == 0) ? c : O - c;
+      // build V
+      for (int n = threadIdx.x; n < P; n += blockDim.x) {
+        float2 x;
+        if (GW == 1) x = make_float2(wt[n], 0.f);
+        else if (c == 0) x = make_float2(wt[n * GW + e + v], 0.f);
+        else {
+          x = make_float2(wt[n * GW + e], wt[n * GW + e + 1]);
+          if (v) x.y = -x.y;
+        }
+        if (s) x = cmul(x, __ldg(&twL[(int64_t)s * n]));
+        buf[n] = x;
+      }
+      __syncthreads();
+      dif_forward(buf, plan, twL, (int)L);
+      // extract
+      if (full) {
+        int umax = (s == 0) ? P / 2 : P / 2 - 1;
+        for (int u = threadIdx.x; u <= umax; u += blockDim.x) ob[(int64_t)u * O + s] = buf[fft_pos(plan, u)];
+      } else {
+        for (int u = u0 + threadIdx.x; u < u1; u += blockDim.x)
+          ob[(int64_t)(u - u0) * O + s] = buf[fft_pos(plan, u)];
+      }
+      __syncthreads();
+    }
+  }
+}
+
+int launch_pfb_stage_a(const TsSrc& src, int ninputs, int P, int O, int ntap, int64_t row0, int64_t nb,
+                       const float* win, float* W, const float2* tw64, cudaStream_t s) {
+  AB_CHECK_ARG(P % kFoldCols == 0, "pfb: lblock/osamp %d must be a multiple of %d", P, kFoldCols);
+  AB_CHECK_ARG(ntap >= 1 && ntap <= 16, "pfb: ntap %d out of range", ntap);
+  if (nb <= 0) return AB_OK;
+  size_t smem = sizeof(float) * (size_t)kFoldCols * ((kFoldBlocks + ntap - 1) * O + 1);
+  AB_CHECK_ARG(smem <= 200 * 1024, "pfb: tile of %zu bytes too large (osamp %d, ntap %d)", smem, O, ntap);
+  dim3 grid((unsigned)((nb + kFoldBlocks - 1) / kFoldBlocks), (unsigned)(P / kFoldCols), (unsigned)ninputs);
+  dim3 block(kFoldCols * kFoldBlocks);
+#define AB_STAGE_A(OO)                                                                                        \
+  case OO:                                                                                                   \
+    AB_CUDA(cudaFuncSetAttribute(pfb_stage_a_kernel<OO>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024)); \
+    pfb_stage_a_kernel<OO><<<grid, block, smem, s>>>(src, P, ntap, row0, nb, win, W, tw64);                   \
+    break;
+  switch (O) {
+    AB_STAGE_A(1)
+    AB_STAGE_A(2)
+    AB_STAGE_A(4)
+    AB_STAGE_A(8)
+    AB_STAGE_A(16)
+    AB_STAGE_A(32)
+    AB_STAGE_A(64)
+    default:
+      set_error("pfb: osamp %d not supported (1..64, power of two)", O);
+      return AB_ERR_UNSUPPORTED;
+  }
+#undef AB_STAGE_A
+  AB_LAUNCH_CHECK();
+  return AB_OK;
+}
+
+int launch_pfb_stage_b(const float* W, int ninputs, int P, int O, int64_t nb, const FftPlan& planP,
+                       const float2* twL, int u0, int u1, float2* out, cudaStream_t s) {
+  if (nb <= 0) return AB_OK;
+  const int GW = O < 8 ? O : 8;
+  size_t smem = sizeof(float) * (size_t)P * GW + sizeof(float2) * (size_t)P;
+  AB_CHECK_ARG(smem <= 220 * 1024, "pfb: stage B needs %zu bytes of shared memory", smem);
+  AB_CUDA(cudaFuncSetAttribute(pfb_stage_b_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
+  dim3 grid((unsigned)nb, (unsigned)(O / GW), (unsigned)ninputs);
+  pfb_stage_b_kernel<<<grid, kStageBThreads, smem, s>>>(W, P, O, nb, planP, twL, u0, u1, out);
+  AB_LAUNCH_CHECK();
+  return AB_OK;
+}
+
+// split lblock into P (<= 4096) and O = lblock / P
+static bool split_lblock(int64_t L, int* P, int* O) {
+  if (L < 64 || (L & (L - 1))) return false;
+  *P = (int)(L < 4096 ? L : 4096);
+  *O = (int)(L / *P);
+  return *O <= 64;
+}
+
+static int pfb_common(ab_ctx* ctx, const float* ts, int64_t nsamp, const float* win, int64_t nchan, int64_t ntap,
+                      int64_t q0, int64_t q1, bool band, float* out, void* stream) {
+  AB_CHECK_ARG(ctx && ts && win && out, "ab_pfb: NULL pointer");
+  AB_CHECK_ARG(nchan >= 2 && ntap >= 1, "ab_pfb: bad nchan/ntap");
+  const int64_t L = 2 * (nchan - 1);
+  int P, O;
+  if (!split_lblock(L, &P, &O)) {
+    set_error("ab_pfb: lblock %lld must be a power of two in [64, 262144]", (long long)L);
+    return AB_ERR_UNSUPPORTED;
+  }
+  int64_t nblock = nsamp / L - (ntap - 1);
+  AB_CHECK_ARG(nblock >= 0, "ab_pfb: timestream shorter than ntap blocks");
+  if (nblock == 0) return AB_OK;
+  int u0 = -1, u1 = -1;
+  if (band) {
+    AB_CHECK_ARG(q0 % O == 0 && q1 % O == 0 && q0 >= 0 && q1 > q0 && q1 <= (int64_t)P * O / 2 + 1,
+                 "ab_pfb_band: band [%lld, %lld) must be multiples of osamp %d inside the spectrum", (long long)q0,
+                 (long long)q1, O);
+    u0 = (int)(q0 / O);
+    u1 = (int)(q1 / O);
+    AB_CHECK_ARG(u1 <= P / 2 || (u1 == P / 2 + 1 && O == 1), "ab_pfb_band: band beyond Nyquist");
+  }
+  FftPlan planP;
+  if (!make_plan(P, &planP)) return AB_ERR_UNSUPPORTED;
+  const float2* twL;
+  AB_TRY(get_twiddles(ctx, L, &twL));
+  void* Wv = nullptr;
+  AB_TRY(get_scratch(ctx, kScratchPfbW, sizeof(float) * (size_t)(nblock * L), &Wv));
+  TsSrc src{ts, nullptr, 0, 0, 0, nsamp / P, 1};
+  cudaStream_t s = as_stream(stream);
+  AB_TRY(launch_pfb_stage_a(src, 1, P, O, (int)ntap, 0, nblock, win, (float*)Wv, ctx->tw64, s));
+  AB_TRY(launch_pfb_stage_b((const float*)Wv, 1, P, O, nblock, planP, twL, u0, u1, (float2*)out, s));
+  return AB_OK;
+}
+
+}  // namespace ab
+
+using namespace ab;
+
+extern "C" int ab_pfb(ab_ctx* ctx, const float* timestream, int64_t nsamp, const float* win, int64_t nchan,
+                      int64_t ntap, float* out, void* stream) {
+  return pfb_common(ctx, timestream, nsamp, win, nchan, ntap, 0, 0, false, out, stream);
+}
+
+extern "C" int ab_pfb_band(ab_ctx* ctx, const float* timestream, int64_t nsamp, const float* win, int64_t nchan,
+                           int64_t ntap, int64_t q0, int64_t q1, float* out, void* stream) {
+  return pfb_common(ctx, timestream, nsamp, win, nchan, ntap, q0, q1, true, out, stream);
+}

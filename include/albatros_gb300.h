@@ -1,0 +1,207 @@
+/*
+ * albatros_gb300.h -- C-ABI of the GB300 (sm_103a) ALBATROS baseband library.
+ *
+ * Every compute entry point takes DEVICE pointers (plain pointers and sizes,
+ * no framework types), a CUDA stream passed as `void*` (NULL = legacy default
+ * stream), launches asynchronously, and returns an int status: AB_OK (0) or a
+ * negative AB_ERR_* code.  Nothing ever calls exit() or prints.
+ * ab_last_error() gives a human-readable detail for the calling thread.
+ *
+ * Complex arrays are interleaved float32 (re, im) pairs ("c64").
+ *
+ * Each declaration names the reference interface it replaces, as
+ * path:line inside the PhilJ0ly/albatros_axion_detection project
+ * (albatros_analysis/...).
+ */
+#ifndef ALBATROS_GB300_H
+#define ALBATROS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define AB_OK 0
+#define AB_ERR_ARG (-1)         /* invalid argument (shape, size, alignment) */
+#define AB_ERR_CUDA (-2)        /* a CUDA runtime call or launch failed */
+#define AB_ERR_UNSUPPORTED (-3) /* valid but unsupported size (e.g. FFT length) */
+#define AB_ERR_NOMEM (-4)       /* device allocation failed */
+#define AB_ERR_STATE (-5)       /* object used in the wrong state */
+
+typedef struct ab_ctx ab_ctx;       /* per-device tables, plans and scratch */
+typedef struct ab_stream ab_stream; /* streaming unpack->IPFB->PFB->xcorr state */
+
+/* ---- library / context ------------------------------------------------ */
+int ab_version(void);
+const char *ab_strerror(int code);
+const char *ab_last_error(void);
+/* Create a context on `device` (makes it current for the calling thread).
+   Replaces the reference's per-call cuBLAS handle and cuFFT plan cache
+   (albatros_analysis/src/correlations/cgemm_batch.cu:26-31,
+    albatros_analysis/src/utils/pycufft.py:27-90). */
+int ab_ctx_create(int device, ab_ctx **out);
+int ab_ctx_destroy(ab_ctx *ctx);
+
+/* ---- unpacking ----------------------------------------------------------
+ * ab_unpack_4bit: replaces unpack_4bit / _unpack_4bit_float_gpu
+ * (albatros_analysis/src/correlations/unpacking.py:140-155,193-245; CPU
+ * albatros_analysis/src/correlations/unpacking.c:155-205).
+ * data: (nspec, 2*nchan) bytes; rows [rowstart,rowend); channels: device
+ * int64 column indices (ncols); pol0/pol1: c64 (rowend-rowstart, ncols).
+ * Nibble decode v>8 -> v-16 (0x8 -> +8). */
+int ab_unpack_4bit(const uint8_t *data, float *pol0, float *pol1, int64_t rowstart, int64_t rowend,
+                   const int64_t *channels, int64_t ncols, int64_t nchan, void *stream);
+/* Same as ab_unpack_4bit for the contiguous channels [c0, c0+ncols) with
+ * c0, ncols, nchan multiples of 4 (one 8-byte load per 4 channels). */
+int ab_unpack_4bit_range(const uint8_t *data, float *pol0, float *pol1, int64_t rowstart, int64_t rowend,
+                         int64_t c0, int64_t ncols, int64_t nchan, void *stream);
+
+/* ab_unpack_1bit: replaces unpack_1bit / _unpack_1bit_float_gpu
+ * (albatros_analysis/src/correlations/unpacking.py:165-191,248-302; CPU
+ * albatros_analysis/src/correlations/unpacking.c:207-246).
+ * data: (nspec, nchan/2) bytes; cols: device int64 byte columns (the
+ * reference's channels[::2]//2), ncols_bytes of them; pol0/pol1: c64
+ * (rows, 2*ncols_bytes) with even output channels from the high half-byte. */
+int ab_unpack_1bit(const uint8_t *data, float *pol0, float *pol1, int64_t rowstart, int64_t rowend,
+                   const int64_t *cols, int64_t ncols_bytes, int64_t nchan, void *stream);
+
+/* ab_sortpols: replaces sortpols (albatros_analysis/src/correlations/unpacking.c:248-368,
+ * albatros_analysis/src/correlations/unpacking.py:305-377), on the device.
+ * pol0/pol1: (rowend-rowstart, ncols) bytes. bit_depth 4 or 1. */
+int ab_sortpols(const uint8_t *data, uint8_t *pol0, uint8_t *pol1, int64_t rowstart, int64_t rowend,
+                int64_t ncols, int64_t nchan, int bit_depth, int64_t chanstart, int64_t chanend,
+                void *stream);
+
+/* ab_make_continuous: replaces make_continuous_gpu
+ * (albatros_analysis/src/correlations/baseband_data_classes.py:48-73).
+ * spec: c64 (nrows, ncols); specnum: device int64 (nrows); channels: device
+ * int64 absolute channel numbers (ncols); out: c64 (nspec, nchans), fully
+ * written (zeros where nothing is placed). Rows go to (specnum-start) mod nspec. */
+int ab_make_continuous(const float *spec, int64_t nrows, int64_t ncols, const int64_t *specnum,
+                       int64_t start_specnum, const int64_t *channels, int64_t nspec, int64_t nchans,
+                       float *out, void *stream);
+
+/* ---- IPFB / PFB ---------------------------------------------------------
+ * ab_get_matft: replaces get_matft (albatros_analysis/src/utils/pfb_gpu_utils.py:123-137),
+ * computed directly in FP64 as a 4-term DFT per (k, f) and rounded to c64.
+ * matft: c64 (lblock, nslice/2+1), lblock = 2*(nchan-1). */
+int ab_get_matft(ab_ctx *ctx, float *matft, int64_t nslice, int64_t nchan, int64_t ntap, void *stream);
+
+/* ab_calculate_filter: replaces calculate_filter
+ * (albatros_analysis/src/utils/pfb_gpu_utils.py:29-36), evaluated in FP64. */
+int ab_calculate_filter(const float *matft, float *filt, int64_t n, double thresh, void *stream);
+
+/* ab_build_filter: calculate_filter(get_matft(nslice, nchan, ntap), thresh)
+ * (albatros_analysis/scripts/xcorr/helper_gpu_stream_clean.py:281-292) in one
+ * FP64 pass, rounded to c64 (lblock, nslice/2+1). */
+int ab_build_filter(ab_ctx *ctx, float *filt, int64_t nslice, int64_t nchan, int64_t ntap, double thresh,
+                    void *stream);
+
+/* ab_ipfb: replaces cupy_ipfb(dat, filt) (albatros_analysis/src/utils/pfb_gpu_utils.py:56-91).
+ * dat: c64 (nslice, nchan); filt: c64 (lblock, nslice/2+1);
+ * out: float32 (lblock, nslice) row-major, i.e. the reference's returned
+ * F-ordered (nslice, lblock) transposed view.  nslice must be even, nslice/2
+ * and lblock must factor into 2, 3, 5, 7. */
+int ab_ipfb(ab_ctx *ctx, const float *dat, const float *filt, float *out, int64_t nslice, int64_t nchan,
+            void *stream);
+
+/* ab_pfb: replaces cupy_pfb(timestream, win, out=None, nchan, ntap)
+ * (albatros_analysis/src/utils/pfb_gpu_utils.py:105-121).
+ * timestream: float32, nsamp samples; win: float32 (ntap*lblock);
+ * out: c64 (nblock, nchan) with nblock = nsamp/lblock - (ntap-1),
+ * lblock = 2*(nchan-1) a power of two >= 64. */
+int ab_pfb(ab_ctx *ctx, const float *timestream, int64_t nsamp, const float *win, int64_t nchan,
+           int64_t ntap, float *out, void *stream);
+
+/* ab_pfb_band: cupy_pfb followed by the fine-band slice [q0, q1) of
+ * scripts/xcorr/helper_gpu_stream_clean.py:375-380, without forming the
+ * other bins. q0, q1 multiples of osamp = lblock/4096 (lblock >= 4096).
+ * out: c64 (nblock, q1-q0). */
+int ab_pfb_band(ab_ctx *ctx, const float *timestream, int64_t nsamp, const float *win, int64_t nchan,
+                int64_t ntap, int64_t q0, int64_t q1, float *out, void *stream);
+
+/* ---- correlators --------------------------------------------------------
+ * ab_avg_xcorr_all_ant: replaces avg_xcorr_all_ant_gpu
+ * (albatros_analysis/src/correlations/correlations_gpu.py:95-121) and its
+ * cublasCgemmStridedBatched call (albatros_analysis/src/correlations/cgemm_batch.cu:8-53).
+ * x: c64 F-ordered (M, ntime, nfreq), M = nant*npol; out: c64 F-ordered
+ * (M, M, nfreq) = sum_t x_i conj(x_j) / ntime. */
+int ab_avg_xcorr_all_ant(const float *x, int64_t nant, int64_t npol, int64_t ntime, int64_t nfreq,
+                         float *out, void *stream);
+
+/* ab_xcorr_coarse_4bit: exact all-baseline coarse correlator on raw 4-bit
+ * packets; the integer form of avg_xcorr_all_ant_gpu for unpacked 4-bit data
+ * (albatros_analysis/src/correlations/correlations_gpu.py:95-121) and of the
+ * CPU avg_xcorr_4bit family (albatros_analysis/src/correlations/correlations_cpu.c:128-271).
+ * raw: nant arrays of (nspec, 2*nchan) bytes, antenna a at raw + a*ant_stride;
+ * rows: optional device int32 (nant, nrows) row indices per antenna (NULL =
+ * rows rowstart..rowstart+nrows-1 for every antenna); channels: device int64
+ * (ncols).  Rows are split into chunks of chunk_rows (0 = one chunk).
+ * out_re/out_im: int64 (nchunks, M, M, ncols), M = 2*nant, unnormalised sums
+ * of Re/Im x_i conj(x_j).  Tensor cores (mma.sync s8, int32 partials flushed
+ * into int64): bit-exact. */
+int ab_xcorr_coarse_4bit(ab_ctx *ctx, const uint8_t *raw, int64_t ant_stride, int64_t nant, int64_t nspec,
+                         int64_t nchan, int64_t rowstart, int64_t nrows, const int32_t *rows,
+                         const int64_t *channels, int64_t ncols, int64_t chunk_rows, int64_t *out_re,
+                         int64_t *out_im, void *stream);
+
+/* ab_avg_xcorr_4bit_pairs: device form of avg_xcorr_4bit / avg_xcorr_4bit_2ant
+ * (albatros_analysis/src/correlations/correlations_cpu.c:128-271) on sortpols'd
+ * 4-bit data (rows, ncol). rows0/rows1: device int32 matched row indices
+ * (nmatch) or NULL for rows 0..nmatch-1. Exact int64 sums re/im (ncol). */
+int ab_avg_xcorr_4bit_pairs(const uint8_t *data0, const uint8_t *data1, const int32_t *rows0,
+                            const int32_t *rows1, int64_t nmatch, int64_t ncol, int64_t *re, int64_t *im,
+                            void *stream);
+
+/* ab_avg_xcorr_1bit_pairs: device form of avg_xcorr_1bit
+ * (albatros_analysis/src/correlations/correlations_cpu.c:273-433) and of the
+ * Van Vleck partial sums (albatros_analysis/src/correlations/correlations_cpu.c:435-638).
+ * data: (rows, ncol) sortpols'd 1-bit bytes; nchan channels.
+ * sums: int64 (6, nchan) = Re, Im, R0, R1, IM0, IM1 (unnormalised). */
+int ab_avg_xcorr_1bit_pairs(const uint8_t *data0, const uint8_t *data1, const int32_t *rows0,
+                            const int32_t *rows1, int64_t nmatch, int64_t ncol, int64_t nchan, int64_t *sums,
+                            void *stream);
+
+/* ---- streaming chain ----------------------------------------------------
+ * The streaming unpack -> IPFB -> PFB(osamp) -> fine xcorr of
+ * repfb_xcorr_avg (albatros_analysis/scripts/xcorr/helper_gpu_stream_clean.py:295-456),
+ * with the IPFB overlap rows and the ntap-1 PFB overlap blocks kept on the
+ * device between chunks.  Inputs are 4-bit packets of nant antennas,
+ * 2 pols each (M = 2*nant inputs).
+ *
+ * ab_stream_create: acclen new spectra per chunk, nslice = acclen + 2*cut;
+ * chan_cols / chan_abs: HOST int64 arrays (nsel) of raw column index and
+ * absolute channel number (0..2048) of the selected coarse channels;
+ * fine band [q0, q1) (multiples of osamp); nblock fine rows per job, njobs
+ * jobs (from the reference's job planner). Allocates all device state. */
+int ab_stream_create(ab_ctx *ctx, int64_t nant, int64_t nchan_raw, const int64_t *chan_cols,
+                     const int64_t *chan_abs, int64_t nsel, int64_t acclen, int64_t cut, int64_t osamp,
+                     int64_t ntap, double thresh, int64_t nblock, int64_t njobs, int64_t q0, int64_t q1,
+                     ab_stream **out);
+int ab_stream_destroy(ab_stream *st);
+/* Reset to the state before the first chunk (zero overlap, zero vis). */
+int ab_stream_reset(ab_stream *st, void *stream);
+/* Push chunk `chunk` (0,1,2,... in order): raw is the device base of packets
+ * (nant arrays of ant_stride bytes, rows of 2*nchan_raw bytes); spectrum
+ * g (global, 0-based) of antenna a is row spec_map[a*map_stride + g] when
+ * spec_map != NULL (negative = missing, zero-filled), else row g. Rows for
+ * g in [chunk*acclen - 2*cut, (chunk+1)*acclen) are read. */
+int ab_stream_push(ab_stream *st, const uint8_t *raw, int64_t ant_stride, const int32_t *spec_map,
+                   int64_t map_stride, int64_t chunk, void *stream);
+/* The last chunk: as ab_stream_push, then every remaining fine block of the
+ * njobs planned jobs is produced with zero samples past the end of the stream,
+ * like the reference's zero-padded final job
+ * (albatros_analysis/scripts/xcorr/helper_gpu_stream_clean.py:163-167). */
+int ab_stream_push_final(ab_stream *st, const uint8_t *raw, int64_t ant_stride, const int32_t *spec_map,
+                         int64_t map_stride, int64_t chunk, void *stream);
+/* Visibilities accumulated so far: device c64 (njobs, M, M, q1-q0), each
+ * job divided by nblock once complete (the reference's /K). */
+const float *ab_stream_vis(const ab_stream *st);
+int64_t ab_stream_kernel_launches(const ab_stream *st);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ALBATROS_GB300_H */

@@ -1,0 +1,57 @@
+"""C-ABI shape checks that need no GPU: the library loads, exports every
+symbol declared in include/*.h, and rejects bad arguments with AB_ERR_ARG
+before touching the device."""
+import ctypes
+import glob
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        src = open(h).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        for m in re.finditer(r"^\s*(?:const\s+)?[A-Za-z_][\w\s\*]*?\b(ab_\w+)\s*\(", src, flags=re.M):
+            names.add(m.group(1))
+    return sorted(names)
+
+
+def test_header_declares_entry_points():
+    names = declared_symbols()
+    for must in ("ab_unpack_4bit", "ab_unpack_1bit", "ab_ipfb", "ab_pfb", "ab_avg_xcorr_all_ant",
+                 "ab_xcorr_coarse_4bit", "ab_stream_create", "ab_stream_push"):
+        assert must in names
+
+
+def test_library_exports_every_declared_symbol():
+    from albatros_axion_detection_gb300 import _lib
+    lib = _lib.load()
+    missing = [n for n in declared_symbols() if not hasattr(lib, n)]
+    assert not missing, f"not exported: {missing}"
+    # every binding the Python layer uses is declared in the header
+    assert set(_lib.SIGNATURES) <= set(declared_symbols())
+
+
+def test_bad_arguments_are_rejected_on_host():
+    from albatros_axion_detection_gb300 import _lib
+    lib = _lib.load()
+    assert lib.ab_unpack_4bit(None, None, None, 0, 10, None, 4, 8, None) == -1
+    assert b"NULL" in lib.ab_last_error()
+    assert lib.ab_sortpols(1, 1, 1, 0, 1, 1, 8, 3, 0, 8, None) == -1
+    assert lib.ab_strerror(-3) == b"unsupported size"
+    assert lib.ab_version() >= 10000
+
+
+def test_ops_fail_loudly_without_gpu():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("GPU present")
+    import numpy as np
+    from albatros_axion_detection_gb300 import unpacking
+    with pytest.raises((RuntimeError, TypeError)):
+        unpacking.unpack_4bit(np.zeros((4, 8), np.uint8), 0, 4, np.arange(4), 4)

@@ -1,0 +1,131 @@
+"""GPU parity: correlators.  Integer paths bit-exact against the C oracle /
+the reference's golden sums; float paths within 1e-5 relative of FP64."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import int_oracle as io
+from oracle import pfb_oracle as po
+from tests.golden import gen
+
+pytestmark = pytest.mark.gpu
+
+
+def cu(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def f_order(x):
+    """numpy (M, T, F) -> torch CUDA tensor with F-ordered strides."""
+    return cu(np.asfortranarray(x).T.copy()).permute(2, 1, 0)
+
+
+def test_all_ant_known_answers():
+    """Constant inputs 3,5,7 / 4,6,8 give exact products
+    (src/correlations/tests/test_gpu_all_ant_complex_xcorr.py:35-68)."""
+    from albatros_axion_detection_gb300.correlations import avg_xcorr_all_ant_gpu
+    x = np.zeros((3, 10000, 2), np.complex64)
+    x[:, :, 0] = np.array([3, 5, 7])[:, None]
+    x[:, :, 1] = np.array([4, 6, 8])[:, None]
+    out = avg_xcorr_all_ant_gpu(f_order(x), 3, 1, 10000, 2)
+    o = out.cpu().numpy()
+    assert o[0, 0, 0] == 9 and o[0, 1, 0] == 15 and o[0, 2, 0] == 21 and o[1, 2, 0] == 35
+    assert o[0, 0, 1] == 16 and o[0, 1, 1] == 24 and o[0, 2, 1] == 32 and o[1, 2, 1] == 48
+    assert np.all(o.imag == 0)
+    assert out.permute(2, 1, 0).is_contiguous()
+
+
+@pytest.mark.parametrize("M,T,F", [(2, 10000, 2), (4, 512, 4096), (32, 300, 7), (5, 1, 3)])
+def test_all_ant_random(M, T, F):
+    from albatros_axion_detection_gb300.correlations import avg_xcorr_all_ant_gpu
+    rng = np.random.default_rng(M * T)
+    x = (rng.standard_normal((M, T, F)) + 10j * rng.standard_normal((M, T, F))).astype(np.complex64)
+    got = avg_xcorr_all_ant_gpu(f_order(x), M, 1, T, F).cpu().numpy()
+    exp = po.xcorr_all_ant(x, M, 1, T, F)
+    assert np.linalg.norm(got - exp) / np.linalg.norm(exp) < 1e-5
+
+
+def test_all_ant_errors():
+    from albatros_axion_detection_gb300.correlations import avg_xcorr_all_ant_gpu
+    x = f_order(np.zeros((2, 10, 3), np.complex64))
+    with pytest.raises(ValueError):
+        avg_xcorr_all_ant_gpu(x, 2, 1, 10, 3, split=3)
+    with pytest.raises(NotImplementedError):
+        avg_xcorr_all_ant_gpu(x, 2, 1, 10, 3, split=2)
+    with pytest.raises(ValueError):
+        avg_xcorr_all_ant_gpu(x, 2, 1, 10, 3, out=torch.zeros((2, 2, 3), dtype=torch.complex64, device="cuda"))
+
+
+@pytest.mark.parametrize("nant,nspec,nchan,chunk", [(2, 2 ** 14, 64, 2 ** 12), (16, 2048, 256, None),
+                                                     (1, 333, 5, 100), (3, 1000, 16, 64)])
+def test_coarse_xcorr_bit_exact(nant, nspec, nchan, chunk):
+    from albatros_axion_detection_gb300.correlations import xcorr_coarse_4bit
+    raw = gen.raw_4bit_uniform(seed=nant * nchan, nspec=nspec, nchan=nchan, nant=nant)
+    ch = np.arange(nchan) if nchan < 64 else np.arange(0, nchan, 3)
+    re, im = xcorr_coarse_4bit(cu(raw), 0, nspec, ch, nchan, chunk=chunk, average=False)
+    re, im = re.cpu().numpy(), im.cpu().numpy()
+    c = nspec if chunk is None else chunk
+    for k in range(re.shape[0]):
+        r0, r1 = k * c, min((k + 1) * c, nspec)
+        er, ei = io.xcorr_all_ant_4bit(raw, r0, r1, ch, nchan, nthreads=8)
+        np.testing.assert_array_equal(re[k], er)
+        np.testing.assert_array_equal(im[k], ei)
+
+
+def test_coarse_xcorr_worst_case_magnitudes():
+    """All nibbles 0x8 (+8): the largest products, exact in int32 partials."""
+    from albatros_axion_detection_gb300.correlations import xcorr_coarse_4bit
+    raw = np.full((2, 8192, 8), 0x88, np.uint8)
+    re, im = xcorr_coarse_4bit(cu(raw), 0, 8192, np.arange(4), 4, average=False)
+    assert np.all(re.cpu().numpy() == 8192 * 128) and np.all(im.cpu().numpy() == 0)
+
+
+def test_coarse_xcorr_row_lists():
+    from albatros_axion_detection_gb300.correlations import xcorr_coarse_4bit
+    raw = gen.raw_4bit(seed=3, nspec=700, nchan=32, nant=2)
+    rows = np.stack([np.arange(0, 600), np.arange(100, 700)]).astype(np.int32)
+    re, im = xcorr_coarse_4bit(cu(raw), 0, 0, np.arange(32), 32, rows=rows, average=False)
+    shifted = np.stack([raw[0, 0:600], raw[1, 100:700]])
+    er, ei = io.xcorr_all_ant_4bit(shifted, 0, 600, np.arange(32), 32)
+    np.testing.assert_array_equal(re.cpu().numpy()[0], er)
+    np.testing.assert_array_equal(im.cpu().numpy()[0], ei)
+
+
+def test_pairs_4bit_golden(golden_int):
+    from albatros_axion_detection_gb300 import correlations as cr
+    d0, d1 = gen.sorted_4bit_pair(seed=21, nrows=2000, ncol=33)
+    got = cr.avg_xcorr_4bit(cu(d0), cu(d1), np.arange(2000))
+    np.testing.assert_array_equal(got, golden_int["x4_sum"] / 2000)
+    s0, s1 = gen.specnum_pair(seed=22, n=2000, span=2600)
+    got = cr.avg_xcorr_4bit_2ant(cu(d0), cu(d1), s0, s1, 0, 0)
+    np.testing.assert_array_equal(got, golden_int["x4_2ant_sum"] / int(golden_int["x4_2ant_rows"]))
+    assert np.isnan(cr.avg_xcorr_4bit(d0, d1, []))
+
+
+def test_pairs_1bit_golden(golden_int):
+    from albatros_axion_detection_gb300 import correlations as cr
+    for nch in (32, 29):
+        nb = int(np.ceil(nch / 4))
+        e0, e1 = gen.sorted_1bit_pair(seed=23 + nch, nrows=1500, nbytes=nb)
+        got = cr.avg_xcorr_1bit(cu(e0), cu(e1), np.arange(1500), nch)
+        np.testing.assert_array_equal(got, golden_int[f"x1_{nch}_sum"] / 1500)
+    e0, e1 = gen.sorted_1bit_pair(seed=31, nrows=2000, nbytes=8)
+    s0, s1 = gen.specnum_pair(seed=22, n=2000, span=2600)
+    vv, n = cr.avg_xcorr_1bit_vanvleck_2ant(cu(e0), cu(e1), 32, s0, s1, 0, 0)
+    assert n == int(golden_int["vv_2ant_rows"])
+    np.testing.assert_array_equal(np.stack(vv), golden_int["vv_2ant"])
+    vv1 = cr.avg_xcorr_1bit_vanvleck(cu(e0), cu(e1), np.arange(2000), 32)
+    exp = io.vanvleck_sums(e0, e1, 32, 2000)
+    for a, b in zip(vv1, exp):
+        np.testing.assert_array_equal(a, b.astype(np.float32) / 2000)
+
+
+def test_float_gpu_single_baseline():
+    from albatros_axion_detection_gb300 import correlations as cr
+    rng = np.random.default_rng(4)
+    d0 = (rng.standard_normal((1000, 16)) + 1j * rng.standard_normal((1000, 16))).astype(np.complex64)
+    d1 = (rng.standard_normal((1000, 16)) + 1j * rng.standard_normal((1000, 16))).astype(np.complex64)
+    sn = np.arange(900)
+    got, n = cr.avg_xcorr_4bit_float_gpu(cu(d0), cu(d1), sn, sn)
+    exp = (d0[:900].astype(np.complex128) * np.conj(d1[:900])).mean(0)
+    assert n == 900 and np.linalg.norm(got.cpu().numpy() - exp) / np.linalg.norm(exp) < 1e-5
