@@ -17,8 +17,12 @@ def device_array(a, dtype: torch.dtype | None = None, name: str = "array") -> to
     _lib.require_cuda()
     if isinstance(a, torch.Tensor):
         t = a
-    elif hasattr(a, "__cuda_array_interface__") or hasattr(a, "__dlpack__"):
+    elif isinstance(a, np.ndarray):
+        raise TypeError(f"{name} must be a device array, got a host numpy array")
+    elif hasattr(a, "__cuda_array_interface__"):
         t = torch.as_tensor(a, device="cuda")
+    elif hasattr(a, "__dlpack__") and hasattr(a, "__dlpack_device__") and a.__dlpack_device__()[0] == 2:
+        t = torch.from_dlpack(a)  # kDLCUDA
     else:
         raise TypeError(f"{name} must be a device array (torch CUDA tensor or __cuda_array_interface__), "
                         f"got {type(a).__name__}")

@@ -45,6 +45,8 @@ SIGNATURES = {
     "ab_stream_push": (I32, [P, P, I64, P, I64, I64, P]),
     "ab_stream_push_final": (I32, [P, P, I64, P, I64, I64, P]),
     "ab_stream_vis": (P, [P]),
+    "ab_stream_profile": (I32, [P, I32]),
+    "ab_stream_stage_times": (I32, [P, P, P]),
     "ab_stream_kernel_launches": (I64, [P]),
 }
 

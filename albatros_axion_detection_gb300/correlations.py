@@ -186,7 +186,7 @@ def avg_xcorr_4bit_float_gpu(data0, data1, specnum0, specnum1):
         return np.nan, 0
     nchan = a.shape[1]
     # F-ordered (2, n, nchan): element (i, t, f) at i + 2 (t + n f)
-    x = torch.stack([a, b]).permute(2, 1, 0).contiguous()
+    x = torch.stack([a, b]).permute(2, 1, 0).contiguous().permute(2, 1, 0)
     out = avg_xcorr_all_ant_gpu(x, 2, 1, n, nchan)
     return out[0, 1, :].contiguous(), n
 

@@ -51,9 +51,16 @@ struct ab_stream {
   int64_t chunks_done = 0;  // next chunk expected
   int64_t blocks_done = 0;  // fine blocks already correlated
   int64_t launches = 0;
+  // optional per-stage timing (row, time, PFB A, PFB B, xcorr)
+  bool profile = false;
+  double stage_ms[5] = {0, 0, 0, 0, 0};
+  int64_t stage_launches[5] = {0, 0, 0, 0, 0};
+  cudaEvent_t ev[2] = {nullptr, nullptr};
 };
 
 static void stream_free(ab_stream* st) {
+  for (auto& e : st->ev)
+    if (e) cudaEventDestroy(e);
   cudaFree(st->d_cols);
   cudaFree(st->d_abs);
   cudaFree(st->d_wtaps);
@@ -182,8 +189,52 @@ extern "C" int ab_stream_reset(ab_stream* st, void* stream) {
   return AB_OK;
 }
 
+extern "C" int ab_stream_profile(ab_stream* st, int enable) {
+  AB_CHECK_ARG(st, "ab_stream_profile: NULL stream object");
+  if (enable && !st->ev[0]) {
+    AB_CUDA(cudaEventCreate(&st->ev[0]));
+    AB_CUDA(cudaEventCreate(&st->ev[1]));
+  }
+  st->profile = enable != 0;
+  for (int i = 0; i < 5; i++) {
+    st->stage_ms[i] = 0;
+    st->stage_launches[i] = 0;
+  }
+  return AB_OK;
+}
+
+extern "C" int ab_stream_stage_times(const ab_stream* st, double* ms, int64_t* launches) {
+  AB_CHECK_ARG(st && ms && launches, "ab_stream_stage_times: NULL pointer");
+  for (int i = 0; i < 5; i++) {
+    ms[i] = st->stage_ms[i];
+    launches[i] = st->stage_launches[i];
+  }
+  return AB_OK;
+}
+
 extern "C" const float* ab_stream_vis(const ab_stream* st) { return st ? (const float*)st->vis : nullptr; }
 extern "C" int64_t ab_stream_kernel_launches(const ab_stream* st) { return st ? st->launches : -1; }
+
+// Stage timing (profiling mode only): events around one stage, synchronised
+// immediately, so this mode serialises the host with the device.
+struct StageTimer {
+  ab_stream* st;
+  cudaStream_t s;
+  int stage;
+  StageTimer(ab_stream* st_, cudaStream_t s_, int stage_) : st(st_), s(s_), stage(stage_) {
+    if (st->profile) cudaEventRecord(st->ev[0], s);
+  }
+  void done(int nlaunch) {
+    st->launches += nlaunch;
+    if (!st->profile) return;
+    cudaEventRecord(st->ev[1], s);
+    cudaEventSynchronize(st->ev[1]);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, st->ev[0], st->ev[1]);
+    st->stage_ms[stage] += ms;
+    st->stage_launches[stage] += nlaunch;
+  }
+};
 
 // Push chunk `chunk`.  final != 0 marks the last chunk of the stream: every
 // remaining block of the planned jobs is then produced with zeros past the end
@@ -200,11 +251,18 @@ static int stream_push(ab_stream* st, const uint8_t* raw, int64_t ant_stride, co
   // 1. row stage
   Packed4Src src{raw, ant_stride, 2 * st->nchan_raw, spec_map, map_stride, chunk * acclen - 2 * cut,
                  st->d_cols, st->d_abs, (int)st->nsel};
-  AB_TRY(launch_row_stage_packed4(src, st->nant, (int)nslice, P, st->planP, st->twP, cur, nslice, s));
+  {
+    StageTimer t(st, s, 0);
+    AB_TRY(launch_row_stage_packed4(src, st->nant, (int)nslice, P, st->planP, st->twP, cur, nslice, s));
+    t.done(1);
+  }
   // 2. time stage
-  AB_TRY(launch_time_stage(cur, nslice, M, P, (int)nslice, st->planM, st->twN, nullptr, st->d_wtaps, st->ntap,
-                           st->thresh, st->ctx->smem_optin, s));
-  st->launches += 2;
+  {
+    StageTimer t(st, s, 1);
+    AB_TRY(launch_time_stage(cur, nslice, M, P, (int)nslice, st->planM, st->twN, nullptr, st->d_wtaps, st->ntap,
+                             st->thresh, st->ctx->smem_optin, s));
+    t.done(1);
+  }
   // 3-5. fine blocks now complete: block B needs timestream rows
   // [B*O, (B+ntap)*O); rows [0, (chunk+1)*acclen) exist.
   const int64_t total_blocks = st->njobs * st->nblock;
@@ -218,19 +276,29 @@ static int stream_push(ab_stream* st, const uint8_t* raw, int64_t ant_stride, co
     int64_t row0 = st->blocks_done * O - chunk * acclen;  // local row of the first block
     AB_CHECK_ARG(row0 >= -acclen || chunk == 0, "ab_stream_push: internal block bookkeeping error");
     TsSrc ts{cur, prev, nslice, cut, cut + acclen, acclen, 0};
-    AB_TRY(launch_pfb_stage_a(ts, M, P, O, st->ntap, row0, nb, st->d_win, st->W, st->ctx->tw64, s));
-    AB_TRY(launch_pfb_stage_b(st->W, M, P, O, nb, st->planP, st->twL, (int)(st->q0 / O), (int)(st->q1 / O), st->Y, s));
-    st->launches += 2;
+    {
+      StageTimer t(st, s, 2);
+      AB_TRY(launch_pfb_stage_a(ts, M, P, O, st->ntap, row0, nb, st->d_win, st->W, st->ctx->tw64, s));
+      t.done(1);
+    }
+    {
+      StageTimer t(st, s, 3);
+      AB_TRY(launch_pfb_stage_b(st->W, M, P, O, nb, st->planP, st->twL, (int)(st->q0 / O), (int)(st->q1 / O), st->Y, s));
+      t.done(1);
+    }
     // correlate, split at job boundaries
     int64_t b = st->blocks_done, bend = st->blocks_done + nb;
+    StageTimer tx(st, s, 4);
+    int nx = 0;
     while (b < bend) {
       int64_t job = b / st->nblock;
       int64_t jend = std::min(bend, (job + 1) * st->nblock);
       AB_TRY(launch_xcorr_accum(st->Y, M, nb, st->nq, b - st->blocks_done, jend - st->blocks_done,
                                 st->vis + job * (int64_t)M * M * st->nq, 1.0f / (float)st->nblock, s));
-      st->launches++;
+      nx++;
       b = jend;
     }
+    tx.done(nx);
     st->blocks_done = bend;
   }
   return AB_OK;

@@ -136,6 +136,18 @@ class StreamCorrelator:
     def kernel_launches(self) -> int:
         return int(_lib.load().ab_stream_kernel_launches(self._h))
 
+    STAGES = ("row_ifft", "time_deconv", "pfb_fold", "pfb_dft", "xcorr")
+
+    def profile(self, enable: bool = True):
+        """Time each stage of later pushes with CUDA events (serialising)."""
+        _lib.call("ab_stream_profile", self._h, 1 if enable else 0)
+
+    def stage_times(self) -> dict:
+        ms = np.zeros(5, np.float64)
+        n = np.zeros(5, np.int64)
+        _lib.call("ab_stream_stage_times", self._h, ms.ctypes.data, n.ctypes.data)
+        return {k: (float(ms[i]), int(n[i])) for i, k in enumerate(self.STAGES)}
+
 
 def _device_view(addr: int, n: int) -> torch.Tensor:
     """Wrap n complex64 at device address `addr` (owned by the library)."""

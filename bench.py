@@ -1,0 +1,330 @@
+"""Benchmark: input spectra/s of the streaming unpack -> IPFB -> PFB -> xcorr chain.
+
+Workload (the full-chain streaming configuration): 2 antennas x 2 pols of
+4-bit packets, 64 contiguous coarse channels, 2^20 spectra per antenna fed in
+chunks of 2^15 spectra (IPFB cut 80 -> nslice 32928 = 2^5*3*7^3), PFB osamp 64
+(4096 fine channels), 512 fine blocks per job (31 jobs), fine 4x4 visibilities
+per job.  One step = the whole 2^20-spectrum stream.  Synthetic seeded data
+(Gaussian nibbles, sigma 2.5, clipped to +-7).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line (rank 0).  `value` is device-resident throughput; `e2e`
+is the same through the public API from pinned host packets with the H2D copy
+of the step's packets and the D2H read of the visibilities inside the timed
+region; `roofline` is the dominant kernel's achieved HBM bandwidth against
+MEASURED_PEAKS.json; `cpu_baseline` the CPU chain on this host's cores over a
+bounded sample.  `--impl reference` times the reference's CPU path.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "input spectra/s, unpack→IPFB→PFB→xcorr on 1 GB300 vs plain GPU path; HBM % roofline"
+NANT, NCHAN_RAW, NSPEC, ACCLEN, CUT, OSAMP, NBLOCK, NTAP, THRESH = 2, 64, 2 ** 20, 2 ** 15, 80, 64, 512, 4, 0.45
+CHAN0 = 640  # absolute number of the first recorded coarse channel
+WORKLOAD = ("full-chain streaming: 2 ant x 2 pol 4-bit, 64 coarse ch, 2^20 spectra in 2^15-spectrum chunks, "
+            "cut 80 (nslice 32928), osamp 64 -> 4096 fine ch, 512 fine blocks/job (31 jobs), fine xcorr")
+P = 4096
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def synth_raw(torch, device, seed=1234):
+    """(NANT, NSPEC, 2*NCHAN_RAW) uint8 Gaussian 4-bit packets, made on the device."""
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    shape = (NANT, NSPEC, NCHAN_RAW, 2)
+    def nib():
+        v = torch.randn(shape, generator=g, device=device, dtype=torch.float32) * 2.5
+        return torch.clamp(torch.round(v), -7, 7).to(torch.int16) & 15
+    re, im = nib(), nib()
+    return ((re << 4) | im).to(torch.uint8).reshape(NANT, NSPEC, 2 * NCHAN_RAW).contiguous()
+
+
+def stage_bytes(sc):
+    """Algorithmic DRAM bytes per launch of each stage for one chunk.
+    Unit = one input row (one pol of one spectrum) of 4096 samples."""
+    M, nslice, nq = 2 * NANT, ACCLEN + 2 * CUT, sc.nq
+    nb = ACCLEN // OSAMP
+    L = P * OSAMP
+    return {
+        "row_ifft": NANT * nslice * 2 * NCHAN_RAW + M * P * nslice * 4,      # packets in, f32 rows out
+        "time_deconv": 2 * M * P * nslice * 4,                              # column in + out
+        "pfb_fold": M * P * ACCLEN * 4 + M * nb * L * 4,                     # timestream in, W out
+        "pfb_dft": M * nb * L * 4 + M * nb * nq * 8,                         # W in, band spectra out
+        "xcorr": M * nb * nq * 8,                                           # band spectra in
+    }
+
+
+def run_ours(args):
+    import torch
+    global NSPEC
+    if args.chunks:
+        NSPEC = ACCLEN * args.chunks
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    from albatros_axion_detection_gb300 import stream
+
+    channels = np.arange(CHAN0, CHAN0 + NCHAN_RAW)
+    raw = synth_raw(torch, dev)
+    sc = stream.StreamCorrelator(NANT, channels, 0, NCHAN_RAW, ACCLEN, NSPEC // ACCLEN, NBLOCK, OSAMP, CUT, THRESH,
+                                 NTAP, nchan_raw=NCHAN_RAW)
+    nchunks = NSPEC // ACCLEN
+    s = torch.cuda.current_stream(dev)
+
+    def step(src):
+        sc.reset()
+        for j in range(nchunks):
+            sc.push(src, j, final=(j == nchunks - 1))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        step(raw)
+    torch.cuda.synchronize()
+    step(raw)
+    launches_per_step = sc.kernel_launches()  # counter restarts at reset()
+    barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        e0.record(s)
+        for _ in range(args.steps):
+            step(raw)
+        e1.record(s)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    barrier()
+    if dist is not None:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    spectra_per_step = NANT * NSPEC
+    value = world * spectra_per_step / (ms / 1e3)
+
+    # ---- end to end: pinned host packets -> device, chain, visibilities -> host
+    host = torch.empty(raw.shape, dtype=torch.uint8, pin_memory=True)
+    host.copy_(raw)
+    dev_in = torch.empty_like(raw)
+    vis_host = torch.empty(sc.vis_device().shape, dtype=torch.complex64, pin_memory=True)
+
+    def e2e_step():
+        dev_in.copy_(host, non_blocking=True)
+        step(dev_in)
+        vis_host.copy_(sc.vis_device(), non_blocking=True)
+
+    for _ in range(max(1, args.warmup // 2)):
+        e2e_step()
+    torch.cuda.synchronize()
+    barrier()
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record(s)
+    for _ in range(args.steps):
+        e2e_step()
+    f1.record(s)
+    torch.cuda.synchronize()
+    ms_e2e = f0.elapsed_time(f1) / args.steps
+    if dist is not None:
+        t = torch.tensor([ms_e2e], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_e2e = float(t.item())
+
+    # ---- per-stage timing (serialised, separate pass) for the roofline
+    sc.profile(True)
+    step(raw)
+    torch.cuda.synchronize()
+    st = sc.stage_times()
+    sc.profile(False)
+    algo = stage_bytes(sc)
+    dom = max(st, key=lambda k: st[k][0])
+    tot_ms, nl = st[dom]
+    avg_ms = tot_ms / max(nl, 1)
+    # bytes per launch: stages run once per chunk (PFB/xcorr: per chunk's blocks)
+    per_launch = algo[dom] * nchunks / max(nl, 1)
+    peak, peak_kind = peaks()
+    achieved = per_launch / (avg_ms / 1e3) / 1e9
+    traffic = None
+    tr_path = os.path.join(ROOT, "profiles", "traffic_per_launch.json")
+    if os.path.exists(tr_path):
+        try:
+            traffic = json.load(open(tr_path)).get(dom)
+        except Exception:
+            traffic = None
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_baseline_sample(raw.cpu().numpy(), sc)
+
+    if rank == 0:
+        out = {
+            "metric": METRIC, "value": value, "unit": "spectra/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded Gaussian 4-bit packets)",
+            "config": {"workload": WORKLOAD, "spectra_per_step": spectra_per_step, "chunks_per_step": nchunks,
+                       "parallelism": f"replicas x{world}",
+                       "l2": "inputs larger than L2 (256 MiB packets, 2 x 4.3 GB IPFB intermediates per step)"},
+            "e2e": {"value": world * spectra_per_step / (ms_e2e / 1e3), "unit": "spectra/s",
+                    "ms_per_step": ms_e2e, "h2d_bytes_per_step": int(host.numel()),
+                    "d2h_bytes_per_step": int(vis_host.numel() * 8)},
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
+                         "algorithmic_bytes_per_launch": per_launch, "avg_launch_ms": avg_ms,
+                         "stages_ms_per_step": {k: v[0] for k, v in st.items()},
+                         "chain_algorithmic_GBps": sum(algo.values()) * nchunks / (ms / 1e3) / 1e9},
+            "gpu_launches": int(launches_per_step * args.steps),
+            "clocks": clk.summary(),
+        }
+        if cpu:
+            out["cpu_baseline"] = cpu
+        print(json.dumps(out), flush=True)
+    sc.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def cpu_baseline_sample(raw_np, sc=None, reps=1):
+    """The CPU chain over one 2^15-spectrum chunk of both antennas."""
+    from oracle import cpu_chain
+    channels = np.arange(CHAN0, CHAN0 + NCHAN_RAW)
+    q0, q1 = CHAN0 * OSAMP, (CHAN0 + NCHAN_RAW) * OSAMP
+    sec, kind, workers = cpu_chain.time_sample(raw_np, np.arange(NCHAN_RAW), channels, NCHAN_RAW, ACCLEN, CUT, OSAMP,
+                                               q0, q1, reps=reps)
+    return {"value": NANT * ACCLEN / sec, "unit": "spectra/s", "cores": workers, "kind": kind,
+            "sample": f"one {ACCLEN}-spectrum chunk of both antennas (unpack, IPFB, PFB, xcorr), {sec:.2f} s"}
+
+
+def run_reference(args):
+    """The reference's CPU path on this host's cores (rank 0 only)."""
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if rank != 0:
+        return
+    rng = np.random.default_rng(1234)
+    shape = (NANT, 2 * ACCLEN, NCHAN_RAW, 2)
+    nib = lambda: np.clip(np.rint(rng.normal(0, 2.5, shape).astype(np.float32)), -7, 7).astype(np.int64) & 15
+    raw = ((nib() << 4) | nib()).astype(np.uint8).reshape(NANT, 2 * ACCLEN, 2 * NCHAN_RAW)
+    from oracle import cpu_chain
+    channels = np.arange(CHAN0, CHAN0 + NCHAN_RAW)
+    q0, q1 = CHAN0 * OSAMP, (CHAN0 + NCHAN_RAW) * OSAMP
+    chain = cpu_chain.CpuChain(channels, ACCLEN, CUT, OSAMP, q0, q1, THRESH, NTAP)
+    for _ in range(args.warmup):
+        chain.run_chunk(raw, np.arange(NCHAN_RAW), NCHAN_RAW, 0)
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        chain.run_chunk(raw, np.arange(NCHAN_RAW), NCHAN_RAW, k % 2)
+    sec = (time.perf_counter() - t0) / args.steps
+    value = NANT * ACCLEN / sec
+    out = {"impl": "reference", "metric": METRIC, "value": value, "unit": "spectra/s", "n_gpus": world,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded Gaussian 4-bit packets)",
+           "config": {"workload": WORKLOAD, "step": f"one {ACCLEN}-spectrum chunk of both antennas"},
+           "cpu_baseline": {"value": value, "unit": "spectra/s", "cores": chain.workers, "kind": chain.kind,
+                            "sample": f"one {ACCLEN}-spectrum chunk of both antennas per step"},
+           "e2e": {"value": value, "unit": "spectra/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline sample")
+    ap.add_argument("--chunks", type=int, default=None,
+                    help="stream only this many 2^15-spectrum chunks (smaller case for profiling; "
+                         "every launch keeps its full size)")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

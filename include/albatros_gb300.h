@@ -199,6 +199,14 @@ int ab_stream_push_final(ab_stream *st, const uint8_t *raw, int64_t ant_stride, 
 /* Visibilities accumulated so far: device c64 (njobs, M, M, q1-q0), each
  * job divided by nblock once complete (the reference's /K). */
 const float *ab_stream_vis(const ab_stream *st);
+/* Measurement hooks (no reference counterpart; the reference times whole
+ * jobs with CUDA events, scripts/xcorr/helper_gpu_stream.py:113-142):
+ * ab_stream_profile(st, 1) times every stage of later pushes with CUDA events
+ * (synchronising after each stage), ab_stream_stage_times() returns the
+ * accumulated ms and launch counts of the 5 stages
+ * (row iFFT, time-axis deconvolution, PFB fold, PFB DFT, correlate). */
+int ab_stream_profile(ab_stream *st, int enable);
+int ab_stream_stage_times(const ab_stream *st, double *ms, int64_t *launches);
 int64_t ab_stream_kernel_launches(const ab_stream *st);
 
 #ifdef __cplusplus

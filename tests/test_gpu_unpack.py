@@ -92,7 +92,8 @@ def test_make_continuous():
     from albatros_axion_detection_gb300.baseband_data_classes import make_continuous_gpu
     rng = np.random.default_rng(2)
     spec = (rng.standard_normal((50, 6)) + 1j * rng.standard_normal((50, 6))).astype(np.complex64)
-    specnum = np.sort(rng.choice(np.arange(1000, 1080), 50, replace=False))
+    # distinct rows modulo nspec: colliding rows are a write race in the reference too
+    specnum = np.sort(rng.choice(np.arange(1000, 1064), 50, replace=False)) + 64 * 3
     channels = np.array([3, 10, 11, 12, 400, 2048])
     out = make_continuous_gpu(cu(spec), specnum, 1000, channels, 64, nchans=2049)
     exp = po.make_continuous(spec, specnum, 1000, channels, 64, 2049)
