@@ -86,6 +86,45 @@ int get_twiddles(ab_ctx* ctx, int64_t T, const float2** out) {
   return AB_OK;
 }
 
+int get_twiddle_stream(ab_ctx* ctx, int n, const std::vector<int>& radices, const float2** out) {
+  std::vector<int> key = radices;
+  key.insert(key.begin(), n);
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  auto it = ctx->streams.find(key);
+  if (it != ctx->streams.end()) {
+    *out = it->second;
+    return AB_OK;
+  }
+  std::vector<float2> h;
+  int prod = 1;
+  const double twopi = 6.283185307179586476925286766559;
+  for (int R : radices) {
+    prod *= R;
+    int S = n / prod;
+    int B = R * S;
+    for (int k = 1; k < R; k++)
+      for (int j = 0; j < S; j++) {
+        long long e = ((long long)j * k) % B;
+        double a = twopi * (double)e / (double)B;
+        h.push_back(make_float2((float)cos(a), (float)(-sin(a))));
+      }
+  }
+  if (prod != n) {
+    set_error("twiddle stream: radices do not multiply to %d", n);
+    return AB_ERR_ARG;
+  }
+  float2* d = nullptr;
+  size_t bytes = sizeof(float2) * (h.empty() ? 1 : h.size());
+  if (cudaMalloc(&d, bytes) != cudaSuccess) {
+    set_error("cudaMalloc of a twiddle stream failed");
+    return AB_ERR_NOMEM;
+  }
+  if (!h.empty()) AB_CUDA(cudaMemcpy(d, h.data(), sizeof(float2) * h.size(), cudaMemcpyHostToDevice));
+  ctx->streams[key] = d;
+  *out = d;
+  return AB_OK;
+}
+
 int get_scratch(ab_ctx* ctx, int slot, size_t bytes, void** out) {
   std::lock_guard<std::mutex> lk(ctx->mu);
   auto& e = ctx->scratch[slot];
@@ -152,6 +191,7 @@ int ab_ctx_destroy(ab_ctx* ctx) {
   if (!ctx) return AB_OK;
   cudaSetDevice(ctx->device);
   for (auto& kv : ctx->twiddles) cudaFree(kv.second);
+  for (auto& kv : ctx->streams) cudaFree(kv.second);
   for (auto& kv : ctx->scratch)
     if (kv.second.first) cudaFree(kv.second.first);
   delete ctx;

@@ -44,6 +44,8 @@ struct ab_stream {
   float* d_wtaps = nullptr;  // IPFB filter window taps (ntap, P)
   float* d_win = nullptr;    // PFB window (ntap * L)
   float* interm[2] = {nullptr, nullptr};
+  bool fused = false;        // PFB fold fused into the time stage (osamp >= 4)
+  float* state = nullptr;    // fused: last 4*osamp timestream rows per column
   float* W = nullptr;
   float2* Y = nullptr;
   float2* vis = nullptr;
@@ -67,6 +69,7 @@ static void stream_free(ab_stream* st) {
   cudaFree(st->d_win);
   cudaFree(st->interm[0]);
   cudaFree(st->interm[1]);
+  cudaFree(st->state);
   cudaFree(st->W);
   cudaFree(st->Y);
   cudaFree(st->vis);
@@ -138,12 +141,29 @@ extern "C" int ab_stream_create(ab_ctx* ctx, int64_t nant, int64_t nchan_raw, co
   }
   const int64_t L = (int64_t)P * osamp;
   const int M = st->M;
-  st->nb_max = acclen / osamp + ntap + 1;
+  st->fused = osamp >= 4;
+  // largest number of fine blocks one push produces (the last push also
+  // produces the zero-padded tail of the planned jobs)
+  {
+    int64_t done = 0, mx = 0, total = njobs * nblock;
+    for (int64_t c = 0; done < total; c++) {
+      int64_t be = ((c + 1) * acclen) / osamp - ntap + 1;
+      if (be > total) be = total;
+      if (be < done) be = done;
+      mx = std::max(mx, be - done);
+      done = be;
+      if (c > total + 2) break;
+    }
+    st->nb_max = std::max<int64_t>(mx, acclen / osamp + 1);
+    // the final push may flush up to a whole job plus the taps beyond the data
+    st->nb_max = std::max<int64_t>(st->nb_max, acclen / osamp + nblock + ntap + 1);
+  }
   AB_ALLOC(st->d_cols, sizeof(int32_t) * nsel);
   AB_ALLOC(st->d_abs, sizeof(int32_t) * nsel);
   AB_ALLOC(st->d_wtaps, sizeof(float) * ntap * P);
   AB_ALLOC(st->d_win, sizeof(float) * ntap * L);
-  for (int i = 0; i < 2; i++) AB_ALLOC(st->interm[i], sizeof(float) * (size_t)M * P * st->nslice);
+  for (int i = 0; i < (st->fused ? 1 : 2); i++) AB_ALLOC(st->interm[i], sizeof(float) * (size_t)M * P * st->nslice);
+  if (st->fused) AB_ALLOC(st->state, sizeof(float) * (size_t)M * P * 4 * osamp);
   AB_ALLOC(st->W, sizeof(float) * (size_t)M * st->nb_max * L);
   AB_ALLOC(st->Y, sizeof(float2) * (size_t)M * st->nb_max * st->nq);
   AB_ALLOC(st->vis, sizeof(float2) * (size_t)std::max<int64_t>(njobs, 1) * M * M * st->nq);
@@ -161,7 +181,8 @@ extern "C" int ab_stream_create(ab_ctx* ctx, int64_t nant, int64_t nchan_raw, co
             cudaMemcpy(st->d_abs, ha.data(), sizeof(int32_t) * nsel, cudaMemcpyHostToDevice) == cudaSuccess &&
             cudaMemcpy(st->d_wtaps, wf.data(), sizeof(float) * wf.size(), cudaMemcpyHostToDevice) == cudaSuccess &&
             cudaMemcpy(st->d_win, wl.data(), sizeof(float) * wl.size(), cudaMemcpyHostToDevice) == cudaSuccess &&
-            cudaMemset(st->vis, 0, sizeof(float2) * (size_t)std::max<int64_t>(njobs, 1) * M * M * st->nq) == cudaSuccess;
+            cudaMemset(st->vis, 0, sizeof(float2) * (size_t)std::max<int64_t>(njobs, 1) * M * M * st->nq) == cudaSuccess &&
+            (!st->fused || cudaMemset(st->state, 0, sizeof(float) * (size_t)M * P * 4 * osamp) == cudaSuccess);
   if (!ok) {
     set_error("ab_stream_create: upload failed");
     stream_free(st);
@@ -186,6 +207,8 @@ extern "C" int ab_stream_reset(ab_stream* st, void* stream) {
   st->launches = 0;
   AB_CUDA(cudaMemsetAsync(st->vis, 0, sizeof(float2) * (size_t)std::max<int64_t>(st->njobs, 1) * st->M * st->M * st->nq,
                           as_stream(stream)));
+  if (st->fused)
+    AB_CUDA(cudaMemsetAsync(st->state, 0, sizeof(float) * (size_t)st->M * st->P * 4 * st->O, as_stream(stream)));
   return AB_OK;
 }
 
@@ -246,61 +269,75 @@ static int stream_push(ab_stream* st, const uint8_t* raw, int64_t ant_stride, co
                (long long)chunk);
   const int P = st->P, O = st->O, M = st->M;
   const int64_t acclen = st->acclen, cut = st->cut, nslice = st->nslice;
-  float* cur = st->interm[chunk & 1];
-  float* prev = chunk > 0 ? st->interm[(chunk - 1) & 1] : nullptr;
-  // 1. row stage
-  Packed4Src src{raw, ant_stride, 2 * st->nchan_raw, spec_map, map_stride, chunk * acclen - 2 * cut,
-                 st->d_cols, st->d_abs, (int)st->nsel};
-  {
-    StageTimer t(st, s, 0);
-    AB_TRY(launch_row_stage_packed4(src, st->nant, (int)nslice, P, st->planP, st->twP, cur, nslice, s));
-    t.done(1);
-  }
-  // 2. time stage
-  {
-    StageTimer t(st, s, 1);
-    AB_TRY(launch_time_stage(cur, nslice, M, P, (int)nslice, st->planM, st->twN, nullptr, st->d_wtaps, st->ntap,
-                             st->thresh, st->ctx->smem_optin, s));
-    t.done(1);
-  }
-  // 3-5. fine blocks now complete: block B needs timestream rows
-  // [B*O, (B+ntap)*O); rows [0, (chunk+1)*acclen) exist.
+  float* cur = st->fused ? st->interm[0] : st->interm[chunk & 1];
+  float* prev = (!st->fused && chunk > 0) ? st->interm[(chunk - 1) & 1] : nullptr;
+  // fine blocks completed by this chunk: block B needs timestream rows
+  // [B*O, (B+ntap)*O); rows [0, (chunk+1)*acclen) exist after this chunk.
   const int64_t total_blocks = st->njobs * st->nblock;
   const int64_t rows_avail = (chunk + 1) * acclen;
   int64_t b_end = rows_avail / O - st->ntap + 1;  // exclusive
   if (final) b_end = total_blocks;
   if (b_end > total_blocks) b_end = total_blocks;
+  if (b_end < st->blocks_done) b_end = st->blocks_done;
+  const int64_t nb_all = b_end - st->blocks_done;
+  const int64_t row0_all = st->blocks_done * O - chunk * acclen;  // local row of the first block
+  AB_CHECK_ARG(!st->fused || nb_all <= st->nb_max, "ab_stream_push: %lld blocks exceed the buffer", (long long)nb_all);
+  AB_CHECK_ARG(row0_all >= -4 * (int64_t)O || chunk == 0 || !st->fused, "ab_stream_push: block bookkeeping error");
+  // 1. row stage
+  Packed4Src src{raw, ant_stride, 2 * st->nchan_raw, spec_map, map_stride, chunk * acclen - 2 * cut,
+                 st->d_cols, st->d_abs, (int)st->nsel};
+  {
+    StageTimer t(st, s, 0);
+    AB_TRY(launch_row_stage_packed4(st->ctx, src, st->nant, (int)nslice, P, st->planP, st->twP, cur, nslice, s));
+    t.done(1);
+  }
+  // 2. time stage (with the PFB fold fused in when osamp >= 4)
+  if (st->fused) {
+    StageTimer t(st, s, 1);
+    FoldArgs fa{O, st->ntap, (int)cut, (int)acclen, row0_all, nb_all, st->d_win, st->W, st->state};
+    AB_TRY(launch_time_fold(st->ctx, cur, nslice, M, P, (int)nslice, st->planM, st->twN, st->d_wtaps, st->ntap,
+                            st->thresh, fa, st->ctx->tw64, s));
+    t.done(1);
+  } else {
+    StageTimer t(st, s, 1);
+    AB_TRY(launch_time_stage(st->ctx, cur, nslice, M, P, (int)nslice, st->planM, st->twN, nullptr, st->d_wtaps,
+                             st->ntap, st->thresh, s));
+    t.done(1);
+  }
   st->chunks_done++;
-  while (st->blocks_done < b_end) {
-    int64_t nb = std::min(b_end - st->blocks_done, st->nb_max);
-    int64_t row0 = st->blocks_done * O - chunk * acclen;  // local row of the first block
-    AB_CHECK_ARG(row0 >= -acclen || chunk == 0, "ab_stream_push: internal block bookkeeping error");
-    TsSrc ts{cur, prev, nslice, cut, cut + acclen, acclen, 0};
-    {
+  int64_t done = 0;
+  while (done < nb_all) {
+    const int64_t nb = st->fused ? nb_all : std::min(nb_all - done, st->nb_max);
+    if (!st->fused) {
+      const int64_t row0 = row0_all + done * O;
+      TsSrc ts{cur, prev, nslice, cut, cut + acclen, acclen, 0};
       StageTimer t(st, s, 2);
       AB_TRY(launch_pfb_stage_a(ts, M, P, O, st->ntap, row0, nb, st->d_win, st->W, st->ctx->tw64, s));
       t.done(1);
     }
     {
       StageTimer t(st, s, 3);
-      AB_TRY(launch_pfb_stage_b(st->W, M, P, O, nb, st->planP, st->twL, (int)(st->q0 / O), (int)(st->q1 / O), st->Y, s));
+      AB_TRY(launch_pfb_stage_b(st->ctx, st->W, M, P, O, nb, st->planP, st->twL, (int)(st->q0 / O), (int)(st->q1 / O),
+                                st->Y, s));
       t.done(1);
     }
     // correlate, split at job boundaries
-    int64_t b = st->blocks_done, bend = st->blocks_done + nb;
+    const int64_t bfirst = st->blocks_done + done;
+    int64_t b = bfirst, bend = bfirst + nb;
     StageTimer tx(st, s, 4);
     int nx = 0;
     while (b < bend) {
       int64_t job = b / st->nblock;
       int64_t jend = std::min(bend, (job + 1) * st->nblock);
-      AB_TRY(launch_xcorr_accum(st->Y, M, nb, st->nq, b - st->blocks_done, jend - st->blocks_done,
+      AB_TRY(launch_xcorr_accum(st->Y, M, nb, st->nq, b - bfirst, jend - bfirst,
                                 st->vis + job * (int64_t)M * M * st->nq, 1.0f / (float)st->nblock, s));
       nx++;
       b = jend;
     }
     tx.done(nx);
-    st->blocks_done = bend;
+    done += nb;
   }
+  st->blocks_done = b_end;
   return AB_OK;
 }
 

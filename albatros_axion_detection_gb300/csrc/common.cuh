@@ -68,6 +68,7 @@ struct ab_ctx {
   std::mutex mu;
   // twiddle tables exp(-2 pi i e / T), e in [0, T), keyed by T
   std::map<int64_t, float2*> twiddles;
+  std::map<std::vector<int>, float2*> streams;
   // grow-only scratch buffers keyed by slot
   std::map<int, std::pair<void*, size_t>> scratch;
   float2* tw64 = nullptr;  // exp(-2 pi i e / 64)
@@ -77,6 +78,9 @@ namespace ab {
 // Device twiddle table of length T (cached in ctx; uploaded synchronously on
 // first use, so call outside stream capture).
 int get_twiddles(ab_ctx* ctx, int64_t T, const float2** out);
+// Device twiddle stream of a plan (radices applied in order), cached in ctx:
+// stream_q[(k-1) S_q + j] = exp(-2 pi i j k / (R_q S_q)), q = 0..npass-1.
+int get_twiddle_stream(ab_ctx* ctx, int n, const std::vector<int>& radices, const float2** out);
 // Grow-only device scratch; the pointer stays valid until a larger request
 // for the same slot.
 int get_scratch(ab_ctx* ctx, int slot, size_t bytes, void** out);

@@ -150,11 +150,36 @@ __device__ __forceinline__ void dft_small(float2* x) {
   else if constexpr (R == 8) dft8<INV>(x);
 }
 
-// One DIF pass of radix R over buf[0..n): butterfly, then twiddle.
-// tw has length T; twiddle exponent j*k*(T/(R*S)).
-template <int R>
-__device__ __forceinline__ void dif_pass(float2* buf, int n, int S, const float2* __restrict__ tw, int T,
-                                         int tid, int nthr) {
+// Padded shared-memory index: one float2 of padding after every 16 keeps the
+// stride-R (R = 2, 4, 8) butterfly accesses of the last passes free of bank
+// conflicts.  A buffer of n complex values occupies padded_len(n) float2.
+__device__ __forceinline__ int pidx(int i) { return i + (i >> 4); }
+__host__ __device__ constexpr int padded_len(int n) { return n + (n >> 4) + 1; }
+
+// Twiddle source: exp(-2 pi i e / T) = hi[e >> 6] * lo[e & 63], two small
+// shared-memory tables filled from the FP64-derived global table (exact
+// float entries; the product adds at most ~1 ulp).
+struct SmemTw {
+  const float2* hi;  // ceil(T/64) entries: exp(-2 pi i 64 h / T)
+  const float2* lo;  // 64 entries: exp(-2 pi i l / T)
+  __device__ __forceinline__ float2 operator()(int e) const { return cmul(hi[e >> 6], lo[e & 63]); }
+};
+__host__ __device__ constexpr int smem_tw_len(int T) { return (T + 63) / 64 + 64; }
+
+// Fill hi/lo (contiguous, smem_tw_len(T) float2 at `dst`) from the global
+// table gtw of length T. Caller syncs afterwards.
+__device__ __forceinline__ SmemTw load_smem_tw(float2* dst, const float2* __restrict__ gtw, int T, int tid,
+                                               int nthr) {
+  const int nhi = (T + 63) / 64;
+  for (int i = tid; i < nhi; i += nthr) dst[i] = __ldg(&gtw[(int64_t)i * 64]);
+  for (int i = tid; i < 64; i += nthr) dst[nhi + i] = i < T ? __ldg(&gtw[i]) : make_float2(1.f, 0.f);
+  return SmemTw{dst, dst + nhi};
+}
+
+// One DIF pass of radix R over buf (padded indexing): butterfly, then twiddle
+// exp(-2 pi i j k / (R S)) = tw(j * k * tstep), tstep = T / (R S).
+template <int R, class TW>
+__device__ __forceinline__ void dif_pass(float2* buf, int n, int S, const TW& tw, int T, int tid, int nthr) {
   const int nbf = n / R;
   const int tstep = T / (R * S);
   for (int bf = tid; bf < nbf; bf += nthr) {
@@ -162,21 +187,20 @@ __device__ __forceinline__ void dif_pass(float2* buf, int n, int S, const float2
     int base = blk * R * S + j;
     float2 x[R];
 #pragma unroll
-    for (int r = 0; r < R; r++) x[r] = buf[base + r * S];
+    for (int r = 0; r < R; r++) x[r] = buf[pidx(base + r * S)];
     dft_small<R, false>(x);
     if (j) {
 #pragma unroll
-      for (int k = 1; k < R; k++) x[k] = cmul(x[k], __ldg(&tw[j * k * tstep]));
+      for (int k = 1; k < R; k++) x[k] = cmul(x[k], tw(j * k * tstep));
     }
 #pragma unroll
-    for (int k = 0; k < R; k++) buf[base + k * S] = x[k];
+    for (int k = 0; k < R; k++) buf[pidx(base + k * S)] = x[k];
   }
 }
 
 // One DIT (adjoint) pass: conjugate twiddle, then inverse butterfly.
-template <int R>
-__device__ __forceinline__ void dit_pass(float2* buf, int n, int S, const float2* __restrict__ tw, int T,
-                                         int tid, int nthr) {
+template <int R, class TW>
+__device__ __forceinline__ void dit_pass(float2* buf, int n, int S, const TW& tw, int T, int tid, int nthr) {
   const int nbf = n / R;
   const int tstep = T / (R * S);
   for (int bf = tid; bf < nbf; bf += nthr) {
@@ -184,20 +208,19 @@ __device__ __forceinline__ void dit_pass(float2* buf, int n, int S, const float2
     int base = blk * R * S + j;
     float2 x[R];
 #pragma unroll
-    for (int r = 0; r < R; r++) x[r] = buf[base + r * S];
+    for (int r = 0; r < R; r++) x[r] = buf[pidx(base + r * S)];
     if (j) {
 #pragma unroll
-      for (int k = 1; k < R; k++) x[k] = cmulc(x[k], __ldg(&tw[j * k * tstep]));
+      for (int k = 1; k < R; k++) x[k] = cmulc(x[k], tw(j * k * tstep));
     }
     dft_small<R, true>(x);
 #pragma unroll
-    for (int k = 0; k < R; k++) buf[base + k * S] = x[k];
+    for (int k = 0; k < R; k++) buf[pidx(base + k * S)] = x[k];
   }
 }
 
-template <bool INV>
-__device__ __forceinline__ void run_pass(int R, float2* buf, int n, int S, const float2* tw, int T, int tid,
-                                         int nthr) {
+template <bool INV, class TW>
+__device__ __forceinline__ void run_pass(int R, float2* buf, int n, int S, const TW& tw, int T, int tid, int nthr) {
   switch (R) {
     case 2: INV ? dit_pass<2>(buf, n, S, tw, T, tid, nthr) : dif_pass<2>(buf, n, S, tw, T, tid, nthr); break;
     case 3: INV ? dit_pass<3>(buf, n, S, tw, T, tid, nthr) : dif_pass<3>(buf, n, S, tw, T, tid, nthr); break;
@@ -209,23 +232,26 @@ __device__ __forceinline__ void run_pass(int R, float2* buf, int n, int S, const
   }
 }
 
-// Forward transform, whole CTA, natural -> digit-reversed. Caller syncs before.
-__device__ __forceinline__ void dif_forward(float2* buf, const FftPlan& p, const float2* tw, int T) {
+// Forward transform of the padded buffer, natural -> digit-reversed.
+// The caller syncs before; this syncs after every pass.
+template <class TW>
+__device__ __forceinline__ void dif_forward(float2* buf, const FftPlan& p, const TW& tw, int T, int tid, int nthr) {
   for (int q = 0; q < p.npass; q++) {
-    run_pass<false>(p.radix[q], buf, p.n, p.span[q], tw, T, threadIdx.x, blockDim.x);
+    run_pass<false>(p.radix[q], buf, p.n, p.span[q], tw, T, tid, nthr);
     __syncthreads();
   }
 }
 
-// Inverse (unnormalised) transform, digit-reversed -> natural. Caller syncs before.
-__device__ __forceinline__ void dit_inverse(float2* buf, const FftPlan& p, const float2* tw, int T) {
+// Inverse (unnormalised) transform, digit-reversed -> natural.
+template <class TW>
+__device__ __forceinline__ void dit_inverse(float2* buf, const FftPlan& p, const TW& tw, int T, int tid, int nthr) {
   for (int q = p.npass - 1; q >= 0; q--) {
-    run_pass<true>(p.radix[q], buf, p.n, p.span[q], tw, T, threadIdx.x, blockDim.x);
+    run_pass<true>(p.radix[q], buf, p.n, p.span[q], tw, T, tid, nthr);
     __syncthreads();
   }
 }
 
-// Storage position of frequency f after dif_forward.
+// Storage position (logical, before pidx) of frequency f after dif_forward.
 __device__ __forceinline__ int fft_pos(const FftPlan& p, int f) {
   int pos = 0;
   for (int q = 0; q < p.npass; q++) {

@@ -11,6 +11,9 @@
 // one CTA's shared memory.
 #include <math.h>
 
+#include <type_traits>
+
+#include "fft_static.cuh"
 #include "ipfb.cuh"
 
 namespace ab {
@@ -72,39 +75,69 @@ void sinc_hamming_host(int ntap, int64_t lblock, std::vector<double>& w) {
 // FFT: Z = A + iB with A, B Hermitian-extended, z = IDFT(Z), rows = Re z,
 // Im z.  The nonzero bins are scattered straight into digit-reversed
 // positions so the DIT passes produce natural order.
-constexpr int kRowFftsPerCta = 2;
+constexpr int kRowFftsPerCta = 4;
 constexpr int kRowThreadsPerFft = 256;
 
-// value of bin k of a real spectrum pair into Z (k in [0, P/2])
-__device__ __forceinline__ void put_pair(float2* buf, const FftPlan& p, int P, int k, float2 A, float2 B) {
-  if (k == 0 || 2 * k == P) {
-    buf[fft_pos(p, k)] = make_float2(A.x, B.x);  // imag parts of DC / Nyquist ignored (irfft)
-  } else {
-    buf[fft_pos(p, k)] = make_float2(A.x - B.y, A.y + B.x);          // A + iB
-    buf[fft_pos(p, P - k)] = make_float2(A.x + B.y, B.x - A.y);      // conj(A) + i conj(B)
-  }
-}
-
-__device__ __forceinline__ void row_dit(float2* buf, const FftPlan& p, const float2* tw, int T, int tid, int nthr) {
-  for (int q = p.npass - 1; q >= 0; q--) {
-    run_pass<true>(p.radix[q], buf, p.n, p.span[q], tw, T, tid, nthr);
-    __syncthreads();
-  }
+// shared memory of a row-stage CTA: kRowFftsPerCta padded P-point buffers,
+// then the twiddle tables of T = P
+__host__ __device__ inline size_t row_smem_bytes(int P) {
+  return sizeof(float2) * ((size_t)padded_len(P) * kRowFftsPerCta + smem_tw_len(P));
 }
 
 __device__ __forceinline__ float dec4f(unsigned v) { return (float)((int)((v + 7u) & 15u) - 7); }
 
+struct NoPlan {};
+
+// FFT policy helpers: a compile-time plan (twiddle stream `tws`) or the
+// generic runtime plan (two-level shared-memory table `tw`).
+template <class PL, int NTHR>
+__device__ __forceinline__ void fft_inv(float2* buf, const FftPlan& plan, const SmemTw& tw, int T,
+                                        const float2* tws, int tid) {
+  if constexpr (std::is_same<PL, NoPlan>::value) dit_inverse(buf, plan, tw, T, tid, NTHR);
+  else sdit<PL, NTHR>(buf, tws, tid);
+}
+template <class PL, int NTHR>
+__device__ __forceinline__ void fft_fwd(float2* buf, const FftPlan& plan, const SmemTw& tw, int T,
+                                        const float2* tws, int tid) {
+  if constexpr (std::is_same<PL, NoPlan>::value) dif_forward(buf, plan, tw, T, tid, NTHR);
+  else sdif<PL, NTHR>(buf, tws, tid);
+}
+template <class PL>
+__device__ __forceinline__ int fpos(const FftPlan& plan, int f) {
+  if constexpr (std::is_same<PL, NoPlan>::value) return fft_pos(plan, f);
+  else return spos<PL>(f);
+}
+
+// value of bin k of a real spectrum pair into Z (k in [0, P/2]); padded buffer
+template <class PL>
+__device__ __forceinline__ void put_pair_t(float2* buf, const FftPlan& p, int P, int k, float2 A, float2 B) {
+  if (k == 0 || 2 * k == P) {
+    buf[pidx(fpos<PL>(p, k))] = make_float2(A.x, B.x);  // imag parts of DC / Nyquist ignored (irfft)
+  } else {
+    buf[pidx(fpos<PL>(p, k))] = make_float2(A.x - B.y, A.y + B.x);      // A + iB
+    buf[pidx(fpos<PL>(p, P - k))] = make_float2(A.x + B.y, B.x - A.y);  // conj(A) + i conj(B)
+  }
+}
+
 // grid: (ceil(nrows / kRowFftsPerCta), nant); one FFT per spectrum row, both pols.
+template <class PL>
 __global__ void __launch_bounds__(kRowFftsPerCta* kRowThreadsPerFft)
     row_stage_packed4_kernel(Packed4Src src, int nrows, FftPlan plan, const float2* __restrict__ tw,
-                             float* __restrict__ out, int64_t ld) {
+                             const float2* __restrict__ tws, float* __restrict__ out, int64_t ld) {
   extern __shared__ float2 smem[];
-  const int P = plan.n;
+  const int P = plan.n, PL_ = padded_len(P);
   const int a = blockIdx.y;
   const int sub = threadIdx.x / kRowThreadsPerFft, ltid = threadIdx.x % kRowThreadsPerFft;
   const int t = blockIdx.x * kRowFftsPerCta + sub;
-  float2* buf = smem + (size_t)sub * P;
-  for (int i = ltid; i < P; i += kRowThreadsPerFft) buf[i] = make_float2(0.f, 0.f);
+  float2* buf = smem + (size_t)sub * PL_;
+  SmemTw tws_s{nullptr, nullptr};
+  if constexpr (std::is_same<PL, NoPlan>::value)
+    tws_s = load_smem_tw(smem + (size_t)kRowFftsPerCta * PL_, tw, P, threadIdx.x, blockDim.x);
+  {
+    float4* b4 = reinterpret_cast<float4*>(smem);  // zero all buffers (PL_ * FFTS float2, even count)
+    const int n4 = (kRowFftsPerCta * PL_) / 2;
+    for (int i = threadIdx.x; i < n4; i += blockDim.x) b4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
   __syncthreads();
   int64_t rawrow = -1;
   if (t < nrows) {
@@ -117,36 +150,52 @@ __global__ void __launch_bounds__(kRowFftsPerCta* kRowThreadsPerFft)
       uchar2 b = *reinterpret_cast<const uchar2*>(row + 2 * __ldg(&src.chan_cols[k]));
       float2 A = make_float2(dec4f(b.x >> 4), dec4f(b.x & 15u));
       float2 B = make_float2(dec4f(b.y >> 4), dec4f(b.y & 15u));
-      put_pair(buf, plan, P, __ldg(&src.chan_abs[k]), A, B);
+      put_pair_t<PL>(buf, plan, P, __ldg(&src.chan_abs[k]), A, B);
     }
   }
   __syncthreads();
-  row_dit(smem + (size_t)sub * P, plan, tw, P, ltid, kRowThreadsPerFft);
-  // write: column n of input (2a+p) at row t; threads of a warp take
-  // consecutive rows of the same n where possible
+  fft_inv<PL, kRowThreadsPerFft>(buf, plan, tws_s, P, tws, ltid);
+  // write: column n of input (2a+p) at rows t0..t0+3 (one 16-byte store per
+  // column and pol when the rows are 16-byte aligned)
   const float inv = 1.0f / (float)P;
   const int nthr = kRowFftsPerCta * kRowThreadsPerFft;
   const int64_t t0 = (int64_t)blockIdx.x * kRowFftsPerCta;
-  for (int i = threadIdx.x; i < kRowFftsPerCta * P; i += nthr) {
-    int n = i / kRowFftsPerCta, f = i - n * kRowFftsPerCta;
-    int64_t tt = t0 + f;
-    if (tt >= nrows) continue;
-    float2 z = smem[(size_t)f * P + n];
-    out[((int64_t)(2 * a) * P + n) * ld + tt] = z.x * inv;
-    out[((int64_t)(2 * a + 1) * P + n) * ld + tt] = z.y * inv;
+  if (kRowFftsPerCta == 4 && ld % 4 == 0 && t0 + 4 <= nrows && ((uintptr_t)out & 15) == 0) {
+    for (int n = threadIdx.x; n < P; n += nthr) {
+      float2 z0 = smem[pidx(n)], z1 = smem[(size_t)PL_ + pidx(n)];
+      float2 z2 = smem[(size_t)2 * PL_ + pidx(n)], z3 = smem[(size_t)3 * PL_ + pidx(n)];
+      *reinterpret_cast<float4*>(out + ((int64_t)(2 * a) * P + n) * ld + t0) =
+          make_float4(z0.x * inv, z1.x * inv, z2.x * inv, z3.x * inv);
+      *reinterpret_cast<float4*>(out + ((int64_t)(2 * a + 1) * P + n) * ld + t0) =
+          make_float4(z0.y * inv, z1.y * inv, z2.y * inv, z3.y * inv);
+    }
+  } else {
+    for (int i = threadIdx.x; i < kRowFftsPerCta * P; i += nthr) {
+      int n = i / kRowFftsPerCta, f = i - n * kRowFftsPerCta;
+      int64_t tt = t0 + f;
+      if (tt >= nrows) continue;
+      float2 z = smem[(size_t)f * PL_ + pidx(n)];
+      out[((int64_t)(2 * a) * P + n) * ld + tt] = z.x * inv;
+      out[((int64_t)(2 * a + 1) * P + n) * ld + tt] = z.y * inv;
+    }
   }
 }
 
 // dense c64 rows (nslice, P/2+1): one FFT for rows (2j, 2j+1)
+template <class PL>
 __global__ void __launch_bounds__(kRowFftsPerCta* kRowThreadsPerFft)
     row_stage_c64_kernel(const float2* __restrict__ dat, int64_t nslice, FftPlan plan,
-                         const float2* __restrict__ tw, float* __restrict__ out, int64_t ld) {
+                         const float2* __restrict__ tw, const float2* __restrict__ tws, float* __restrict__ out,
+                         int64_t ld) {
   extern __shared__ float2 smem[];
-  const int P = plan.n, nb = P / 2 + 1;
+  const int P = plan.n, nb = P / 2 + 1, PL_ = padded_len(P);
   const int sub = threadIdx.x / kRowThreadsPerFft, ltid = threadIdx.x % kRowThreadsPerFft;
   const int64_t ta = 2 * ((int64_t)blockIdx.x * kRowFftsPerCta + sub);
-  float2* buf = smem + (size_t)sub * P;
-  for (int i = ltid; i < P; i += kRowThreadsPerFft) buf[i] = make_float2(0.f, 0.f);
+  float2* buf = smem + (size_t)sub * PL_;
+  SmemTw tws_s{nullptr, nullptr};
+  if constexpr (std::is_same<PL, NoPlan>::value)
+    tws_s = load_smem_tw(smem + (size_t)kRowFftsPerCta * PL_, tw, P, threadIdx.x, blockDim.x);
+  for (int i = ltid; i < PL_; i += kRowThreadsPerFft) buf[i] = make_float2(0.f, 0.f);
   __syncthreads();
   if (ta < nslice) {
     const float2* ra = dat + ta * nb;
@@ -154,11 +203,11 @@ __global__ void __launch_bounds__(kRowFftsPerCta* kRowThreadsPerFft)
     for (int k = ltid; k < nb; k += kRowThreadsPerFft) {
       float2 A = ra[k];
       float2 B = rb ? rb[k] : make_float2(0.f, 0.f);
-      put_pair(buf, plan, P, k, A, B);
+      put_pair_t<PL>(buf, plan, P, k, A, B);
     }
   }
   __syncthreads();
-  row_dit(buf, plan, tw, P, ltid, kRowThreadsPerFft);
+  fft_inv<PL, kRowThreadsPerFft>(buf, plan, tws_s, P, tws, ltid);
   const float inv = 1.0f / (float)P;
   const int nthr = kRowFftsPerCta * kRowThreadsPerFft;
   const int64_t tbase = 2 * (int64_t)blockIdx.x * kRowFftsPerCta;
@@ -167,7 +216,7 @@ __global__ void __launch_bounds__(kRowFftsPerCta* kRowThreadsPerFft)
     int f = r >> 1, part = r & 1;
     int64_t tt = tbase + r;
     if (tt >= nslice) continue;
-    float2 z = smem[(size_t)f * P + n];
+    float2 z = smem[(size_t)f * PL_ + pidx(n)];
     out[(int64_t)n * ld + tt] = (part ? z.y : z.x) * inv;
   }
 }
@@ -177,17 +226,138 @@ __global__ void __launch_bounds__(kRowFftsPerCta* kRowThreadsPerFft)
 // multiply by the filter, inverse.  All in shared memory, one CTA per column.
 constexpr int kTimeThreads = 1024;
 
-template <bool TABLE>
-__global__ void __launch_bounds__(kTimeThreads)
+// Warp-level fold + osamp-point real DFT for the fused epilogue.  A group of
+// G = O/2 lanes owns one block: lane m of the group folds rows 2m, 2m+1 of
+// the block (z_m = y[2m] + i y[2m+1]), the group takes a G-point complex DFT
+// by shuffles (decimation in frequency, output in bit-reversed lane order),
+// and untangles the real-input spectrum W_k, k = 0..O/2.
+template <int G>
+__device__ __forceinline__ void fold_blocks(const float2* buf, const float* stail, const FoldArgs& fa, int P, int n,
+                                            int in, const float2* __restrict__ tw64) {
+  constexpr int O = 2 * G;
+  constexpr int LOG = G == 1 ? 0 : G == 2 ? 1 : G == 4 ? 2 : G == 8 ? 3 : G == 16 ? 4 : 5;
+  constexpr int GW = O < 8 ? O : 8;
+  constexpr int NG = O / GW;
+  constexpr int BPW = 32 / G;  // blocks per warp
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const int m = lane % G, grp = lane / G;
+  const int gbase = grp * G;
+  // window taps of rows 2m, 2m+1 for this sample phase
+  float w0[8], w1[8];
+#pragma unroll
+  for (int i = 0; i < 8; i++) {
+    w0[i] = i < fa.ntap ? __ldg(&fa.win[(int64_t)(i * O + 2 * m) * P + n]) : 0.f;
+    w1[i] = i < fa.ntap ? __ldg(&fa.win[(int64_t)(i * O + 2 * m + 1) * P + n]) : 0.f;
+  }
+  // per-stage DIF twiddles exp(-2 pi i (m mod h) / (2h)) and untangle twiddle
+  float2 stw[LOG > 0 ? LOG : 1];
+#pragma unroll
+  for (int st = 0; st < LOG; st++) {
+    int h = G >> (st + 1);
+    stw[st] = tw64[(m % h) * (32 / h)];  // exp(-2 pi i (m mod h)/(2h)) = w64^((m mod h) * 64/(2h))
+  }
+  // bit-reversed frequency held by this lane after the DFT
+  int k = 0;
+#pragma unroll
+  for (int bit = 0; bit < LOG; bit++) k |= ((m >> bit) & 1) << (LOG - 1 - bit);
+  const int kc = (G - k) % G;  // partner frequency G - k
+  int src_lane = 0;
+#pragma unroll
+  for (int bit = 0; bit < LOG; bit++) src_lane |= ((kc >> bit) & 1) << (LOG - 1 - bit);
+  src_lane += gbase;
+  const float2 wk = tw64[(k * (64 / O)) & 63];  // exp(-2 pi i k / O)
+  const int p = 2 * k;                        // packed float position (k >= 1), 0 for k = 0
+  const int g = p / GW, e = p % GW;
+  const int64_t nbw = (fa.nb + BPW - 1) / BPW;
+  const float* fbuf = reinterpret_cast<const float*>(buf);
+  // rows of a block start at an even IPFB row when cut + row0 is even: then
+  // each lane's pair (2m, 2m+1) is one float2 slot of the column buffer
+  const bool even = ((fa.cut + fa.row0) & 1) == 0;
+  const int ntap = fa.ntap;
+  const int cut = fa.cut, acclen = fa.acclen;
+  for (int64_t wb = warp; wb < nbw; wb += nwarps) {
+    const int64_t b = wb * BPW + grp;
+    const bool valid = b < fa.nb;
+    float2 z = make_float2(0.f, 0.f);
+    if (valid) {
+      // first row of this lane's pair (int32: rows of one chunk)
+      const int rb = (int)(fa.row0 + b * O) + 2 * m;
+      const int rfirst = (int)(fa.row0 + b * O), rlast = rfirst + ntap * O;  // block's row span
+      if (even && rfirst >= 0 && rlast <= acclen) {
+        // all rows inside this chunk: one float2 slot per tap
+        const int s0 = (cut + rb) >> 1;
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+          if (i < ntap) {
+            float2 v = buf[pidx(s0 + i * (O / 2))];
+            z.x = fmaf(v.x, w0[i], z.x);
+            z.y = fmaf(v.y, w1[i], z.y);
+          }
+        }
+      } else {
+        auto get = [&](int rr) -> float {
+          if (rr < 0) return stail[rr + 4 * O];
+          if (rr >= acclen) return 0.f;
+          int t = cut + rr;
+          return fbuf[2 * pidx(t >> 1) + (t & 1)];
+        };
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+          if (i < ntap) {
+            z.x = fmaf(get(rb + i * O), w0[i], z.x);
+            z.y = fmaf(get(rb + i * O + 1), w1[i], z.y);
+          }
+        }
+      }
+    }
+    // G-point DIF across the group
+#pragma unroll
+    for (int st = 0; st < LOG; st++) {
+      const int h = G >> (st + 1);
+      float2 v;
+      v.x = __shfl_xor_sync(0xffffffffu, z.x, h);
+      v.y = __shfl_xor_sync(0xffffffffu, z.y, h);
+      if (m & h) z = cmul(csub(v, z), stw[st]);
+      else z = cadd(z, v);
+    }
+    // untangle: W_k = (Z_k + conj Z_{G-k})/2 + w^k (Z_k - conj Z_{G-k})/(2i)
+    float2 zc;
+    zc.x = __shfl_sync(0xffffffffu, z.x, src_lane);
+    zc.y = __shfl_sync(0xffffffffu, z.y, src_lane);
+    if (!valid) continue;
+    float2 outv;
+    if (k == 0) {
+      outv = make_float2(z.x + z.y, z.x - z.y);  // (W_0, W_{O/2})
+    } else {
+      float2 c = cconj(zc);
+      float2 E = cscale(cadd(z, c), 0.5f);
+      float2 D = csub(z, c);  // 2 i O_k
+      float2 Od = make_float2(0.5f * D.y, -0.5f * D.x);
+      outv = cadd(E, cmul(wk, Od));
+    }
+    float* dst = fa.W + ((((int64_t)in * fa.nb + b) * NG + g) * P + n) * GW + e;
+    *reinterpret_cast<float2*>(dst) = outv;
+  }
+}
+
+__host__ __device__ inline size_t time_smem_bytes(int N) {
+  return sizeof(float2) * ((size_t)padded_len(N / 2) + smem_tw_len(N));
+}
+
+template <class PL, bool TABLE, int NTHR, int FOLDG = 0>
+__global__ void __launch_bounds__(NTHR)
     time_stage_kernel(float* __restrict__ data, int64_t ld, int P, int N, FftPlan plan,
-                      const float2* __restrict__ twN, const float2* __restrict__ table,
-                      const float* __restrict__ wtaps, int ntap, float thresh) {
+                      const float2* __restrict__ twN, const float2* __restrict__ tws,
+                      const float2* __restrict__ table, const float* __restrict__ wtaps, int ntap, float thresh,
+                      FoldArgs fa, const float2* __restrict__ tw64) {
   extern __shared__ float2 buf[];
   const int n = blockIdx.x, input = blockIdx.y;
   const int M = N / 2;
+  const int tid = threadIdx.x;
   float* col = data + ((int64_t)input * P + n) * ld;
   const float2* col2 = reinterpret_cast<const float2*>(col);
-  for (int m = threadIdx.x; m < M; m += blockDim.x) buf[m] = col2[m];
+  const SmemTw tw = load_smem_tw(buf + padded_len(M), twN, N, tid, NTHR);
+  for (int m = tid; m < M; m += NTHR) buf[pidx(m)] = col2[m];
   // window taps of this column for the on-the-fly filter
   float w[8];
   if (!TABLE) {
@@ -195,7 +365,7 @@ __global__ void __launch_bounds__(kTimeThreads)
     for (int t = 0; t < 8; t++) w[t] = t < ntap ? __ldg(&wtaps[(int64_t)t * P + n]) : 0.f;
   }
   __syncthreads();
-  dif_forward(buf, plan, twN, N);
+  fft_fwd<PL, NTHR>(buf, plan, tw, N, tws, tid);
 
   const float scale = 0.5f / (float)N;  // irfft 1/N and the untangle's 1/2
   const float t2 = thresh * thresh;
@@ -204,10 +374,12 @@ __global__ void __launch_bounds__(kTimeThreads)
     if (TABLE) {
       h = __ldg(&table[(int64_t)n * (M + 1) + k]);
     } else {
-      float2 m = make_float2(0.f, 0.f);
-      for (int t = 0; t < ntap; t++) {
-        int e = (int)(((int64_t)t * k) % N);
-        float2 z = __ldg(&twN[e]);
+      float2 m = make_float2(w[0], 0.f);
+      int e = 0;
+      for (int t = 1; t < ntap; t++) {
+        e += k;
+        if (e >= N) e -= N;
+        float2 z = tw(e);
         m.x = fmaf(w[t], z.x, m.x);
         m.y = fmaf(w[t], z.y, m.y);
       }
@@ -218,7 +390,7 @@ __global__ void __launch_bounds__(kTimeThreads)
     return cscale(h, scale);
   };
 
-  for (int k = threadIdx.x; k <= M / 2; k += blockDim.x) {
+  for (int k = tid; k <= M / 2; k += NTHR) {
     if (k == 0) {
       float2 z = buf[0];
       float x0 = 2.f * (z.x + z.y), xm = 2.f * (z.x - z.y);  // 2 X[0], 2 X[M] (real)
@@ -226,9 +398,9 @@ __global__ void __launch_bounds__(kTimeThreads)
       buf[0] = make_float2(y0 + ym, y0 - ym);
       continue;
     }
-    int pk = fft_pos(plan, k), pc = fft_pos(plan, M - k);
+    int pk = pidx(fpos<PL>(plan, k)), pc = pidx(fpos<PL>(plan, M - k));
     float2 zk = buf[pk], zc = buf[pc];
-    float2 w1 = __ldg(&twN[k]);                  // exp(-2 pi i k / N)
+    float2 w1 = tw(k);                           // exp(-2 pi i k / N)
     float2 E = cadd(zk, cconj(zc));              // 2 E_k
     float2 Od = csub(zk, cconj(zc));             // 2 i O_k
     float2 O = make_float2(Od.y, -Od.x);         // 2 O_k = (2 i O_k) / i
@@ -244,59 +416,170 @@ __global__ void __launch_bounds__(kTimeThreads)
     if (pc != pk) buf[pc] = cadd(cconj(Et), make_float2(Ot.y, Ot.x));  // conj(Et) + i conj(Ot)
   }
   __syncthreads();
-  dit_inverse(buf, plan, twN, N);
-  float2* out2 = reinterpret_cast<float2*>(col);
-  for (int m = threadIdx.x; m < M; m += blockDim.x) out2[m] = buf[m];
+  fft_inv<PL, NTHR>(buf, plan, tw, N, tws, tid);
+  if constexpr (FOLDG == 0) {
+    float2* out2 = reinterpret_cast<float2*>(col);
+    for (int m = tid; m < M; m += NTHR) out2[m] = buf[pidx(m)];
+  } else {
+    // fused PFB fold: previous tail rows -> shared memory, fold all blocks,
+    // then store this chunk's last 4*O rows as the next chunk's tail
+    constexpr int O = 2 * FOLDG;
+    float* stail = reinterpret_cast<float*>(buf + padded_len(M) + smem_tw_len(N));
+    float* st = fa.state + ((int64_t)input * P + n) * (4 * O);
+    for (int i = tid; i < 4 * O; i += NTHR) stail[i] = st[i];
+    __syncthreads();
+    fold_blocks<FOLDG>(buf, stail, fa, P, n, input, tw64);
+    __syncthreads();
+    const float* fbuf = reinterpret_cast<const float*>(buf);
+    for (int i = tid; i < 4 * O; i += NTHR) {
+      int64_t r = (int64_t)fa.acclen - 4 * O + i;
+      float v = 0.f;
+      if (r >= 0) {
+        int t = (int)(fa.cut + r);
+        v = fbuf[2 * pidx(t >> 1) + (t & 1)];
+      } else {
+        v = stail[r + 4 * O];  // acclen < 4*O: keep older rows
+      }
+      st[i] = v;
+    }
+  }
 }
 
-int launch_row_stage_packed4(const Packed4Src& src, int nant, int nrows, int P, const FftPlan& plan,
+template <class K>
+static int set_smem_attr(K kernel, size_t bytes) {
+  AB_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+  return AB_OK;
+}
+
+int launch_row_stage_packed4(ab_ctx* ctx, const Packed4Src& src, int nant, int nrows, int P, const FftPlan& plan,
                              const float2* twP, float* out, int64_t ld, cudaStream_t s) {
-  size_t smem = sizeof(float2) * (size_t)P * kRowFftsPerCta;
-  static bool attr_set = false;
-  if (!attr_set) {
-    AB_CUDA(cudaFuncSetAttribute(row_stage_packed4_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
-    attr_set = true;
-  }
-  AB_CHECK_ARG(smem <= 96 * 1024, "row stage: lblock %d too large", P);
+  size_t smem = row_smem_bytes(P);
+  AB_CHECK_ARG(smem <= ctx->smem_optin, "row stage: lblock %d too large", P);
   dim3 grid((unsigned)((nrows + kRowFftsPerCta - 1) / kRowFftsPerCta), (unsigned)nant);
-  row_stage_packed4_kernel<<<grid, kRowFftsPerCta * kRowThreadsPerFft, smem, s>>>(src, nrows, plan, twP, out, ld);
+  if (P == Plan4096::N) {
+    const float2* tws;
+    AB_TRY(get_twiddle_stream(ctx, P, {16, 16, 16}, &tws));
+    AB_TRY(set_smem_attr(row_stage_packed4_kernel<Plan4096>, smem));
+    row_stage_packed4_kernel<Plan4096><<<grid, kRowFftsPerCta * kRowThreadsPerFft, smem, s>>>(src, nrows, plan, twP,
+                                                                                               tws, out, ld);
+  } else {
+    AB_TRY(set_smem_attr(row_stage_packed4_kernel<NoPlan>, smem));
+    row_stage_packed4_kernel<NoPlan><<<grid, kRowFftsPerCta * kRowThreadsPerFft, smem, s>>>(src, nrows, plan, twP,
+                                                                                             nullptr, out, ld);
+  }
   AB_LAUNCH_CHECK();
   return AB_OK;
 }
 
-int launch_row_stage_c64(const float2* dat, int64_t nslice, int P, const FftPlan& plan, const float2* twP,
-                         float* out, int64_t ld, cudaStream_t s) {
-  size_t smem = sizeof(float2) * (size_t)P * kRowFftsPerCta;
-  static bool attr_set = false;
-  if (!attr_set) {
-    AB_CUDA(cudaFuncSetAttribute(row_stage_c64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024));
-    attr_set = true;
-  }
-  AB_CHECK_ARG(smem <= 96 * 1024, "row stage: lblock %d too large", P);
+int launch_row_stage_c64(ab_ctx* ctx, const float2* dat, int64_t nslice, int P, const FftPlan& plan,
+                         const float2* twP, float* out, int64_t ld, cudaStream_t s) {
+  size_t smem = row_smem_bytes(P);
+  AB_CHECK_ARG(smem <= ctx->smem_optin, "row stage: lblock %d too large", P);
   int64_t nfft = (nslice + 1) / 2;
   dim3 grid((unsigned)((nfft + kRowFftsPerCta - 1) / kRowFftsPerCta));
-  row_stage_c64_kernel<<<grid, kRowFftsPerCta * kRowThreadsPerFft, smem, s>>>(dat, nslice, plan, twP, out, ld);
+  if (P == Plan4096::N) {
+    const float2* tws;
+    AB_TRY(get_twiddle_stream(ctx, P, {16, 16, 16}, &tws));
+    AB_TRY(set_smem_attr(row_stage_c64_kernel<Plan4096>, smem));
+    row_stage_c64_kernel<Plan4096><<<grid, kRowFftsPerCta * kRowThreadsPerFft, smem, s>>>(dat, nslice, plan, twP,
+                                                                                           tws, out, ld);
+  } else {
+    AB_TRY(set_smem_attr(row_stage_c64_kernel<NoPlan>, smem));
+    row_stage_c64_kernel<NoPlan><<<grid, kRowFftsPerCta * kRowThreadsPerFft, smem, s>>>(dat, nslice, plan, twP,
+                                                                                         nullptr, out, ld);
+  }
   AB_LAUNCH_CHECK();
   return AB_OK;
 }
 
-int launch_time_stage(float* buf, int64_t ld, int ninputs, int P, int N, const FftPlan& planM,
-                      const float2* twN, const float2* table, const float* wtaps, int ntap, float thresh,
-                      size_t smem_optin, cudaStream_t s) {
-  size_t smem = sizeof(float2) * (size_t)(N / 2);
-  AB_CHECK_ARG(smem <= smem_optin, "time stage: nslice %d needs %zu bytes of shared memory (max %zu)", N, smem,
-               smem_optin);
-  AB_CHECK_ARG(table || (wtaps && ntap >= 1 && ntap <= 8), "time stage: need a filter table or 1..8 window taps");
+template <class PL, int NTHR>
+static int launch_time_t(ab_ctx* ctx, float* buf, int64_t ld, int ninputs, int P, int N, const FftPlan& planM,
+                         const float2* twN, const float2* tws, const float2* table, const float* wtaps, int ntap,
+                         float thresh, size_t smem, cudaStream_t s) {
   dim3 grid((unsigned)P, (unsigned)ninputs);
   if (table) {
-    AB_CUDA(cudaFuncSetAttribute(time_stage_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_optin));
-    time_stage_kernel<true><<<grid, kTimeThreads, smem, s>>>(buf, ld, P, N, planM, twN, table, wtaps, ntap, thresh);
+    AB_TRY(set_smem_attr(time_stage_kernel<PL, true, NTHR>, smem));
+    time_stage_kernel<PL, true, NTHR><<<grid, NTHR, smem, s>>>(buf, ld, P, N, planM, twN, tws, table, wtaps, ntap,
+                                                              thresh, FoldArgs{}, nullptr);
   } else {
-    AB_CUDA(cudaFuncSetAttribute(time_stage_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_optin));
-    time_stage_kernel<false><<<grid, kTimeThreads, smem, s>>>(buf, ld, P, N, planM, twN, table, wtaps, ntap, thresh);
+    AB_TRY(set_smem_attr(time_stage_kernel<PL, false, NTHR>, smem));
+    time_stage_kernel<PL, false, NTHR><<<grid, NTHR, smem, s>>>(buf, ld, P, N, planM, twN, tws, table, wtaps, ntap,
+                                                               thresh, FoldArgs{}, nullptr);
   }
   AB_LAUNCH_CHECK();
   return AB_OK;
+}
+
+int launch_time_stage(ab_ctx* ctx, float* buf, int64_t ld, int ninputs, int P, int N, const FftPlan& planM,
+                      const float2* twN, const float2* table, const float* wtaps, int ntap, float thresh,
+                      cudaStream_t s) {
+  size_t smem = time_smem_bytes(N);
+  AB_CHECK_ARG(smem <= ctx->smem_optin, "time stage: nslice %d needs %zu bytes of shared memory (max %zu)", N, smem,
+               ctx->smem_optin);
+  AB_CHECK_ARG(table || (wtaps && ntap >= 1 && ntap <= 8), "time stage: need a filter table or 1..8 window taps");
+  const int M = N / 2;
+  const float2* tws = nullptr;
+  if (M == Plan16464::N) {
+    AB_TRY(get_twiddle_stream(ctx, M, {7, 7, 7, 3, 16}, &tws));
+    return launch_time_t<Plan16464, 512>(ctx, buf, ld, ninputs, P, N, planM, twN, tws, table, wtaps, ntap, thresh,
+                                         smem, s);
+  }
+  if (M == Plan16384::N) {
+    AB_TRY(get_twiddle_stream(ctx, M, {4, 16, 16, 16}, &tws));
+    return launch_time_t<Plan16384, 512>(ctx, buf, ld, ninputs, P, N, planM, twN, tws, table, wtaps, ntap, thresh,
+                                         smem, s);
+  }
+  return launch_time_t<NoPlan, kTimeThreads>(ctx, buf, ld, ninputs, P, N, planM, twN, nullptr, table, wtaps, ntap,
+                                             thresh, smem, s);
+}
+
+template <class PL, int NTHR, int G>
+static int launch_fold_t(float* buf, int64_t ld, int ninputs, int P, int N, const FftPlan& planM, const float2* twN,
+                         const float2* tws, const float* wtaps, int ntap, float thresh, const FoldArgs& fa,
+                         const float2* tw64, size_t smem, cudaStream_t s) {
+  dim3 grid((unsigned)P, (unsigned)ninputs);
+  AB_TRY(set_smem_attr(time_stage_kernel<PL, false, NTHR, G>, smem));
+  time_stage_kernel<PL, false, NTHR, G><<<grid, NTHR, smem, s>>>(buf, ld, P, N, planM, twN, tws, nullptr, wtaps,
+                                                                 ntap, thresh, fa, tw64);
+  AB_LAUNCH_CHECK();
+  return AB_OK;
+}
+
+template <class PL, int NTHR>
+static int launch_fold_o(float* buf, int64_t ld, int ninputs, int P, int N, const FftPlan& planM, const float2* twN,
+                         const float2* tws, const float* wtaps, int ntap, float thresh, const FoldArgs& fa,
+                         const float2* tw64, size_t smem, cudaStream_t s) {
+  switch (fa.O) {
+    case 4: return launch_fold_t<PL, NTHR, 2>(buf, ld, ninputs, P, N, planM, twN, tws, wtaps, ntap, thresh, fa, tw64, smem, s);
+    case 8: return launch_fold_t<PL, NTHR, 4>(buf, ld, ninputs, P, N, planM, twN, tws, wtaps, ntap, thresh, fa, tw64, smem, s);
+    case 16: return launch_fold_t<PL, NTHR, 8>(buf, ld, ninputs, P, N, planM, twN, tws, wtaps, ntap, thresh, fa, tw64, smem, s);
+    case 32: return launch_fold_t<PL, NTHR, 16>(buf, ld, ninputs, P, N, planM, twN, tws, wtaps, ntap, thresh, fa, tw64, smem, s);
+    case 64: return launch_fold_t<PL, NTHR, 32>(buf, ld, ninputs, P, N, planM, twN, tws, wtaps, ntap, thresh, fa, tw64, smem, s);
+    default:
+      set_error("fused fold: osamp %d not supported (4..64)", fa.O);
+      return AB_ERR_UNSUPPORTED;
+  }
+}
+
+int launch_time_fold(ab_ctx* ctx, float* buf, int64_t ld, int ninputs, int P, int N, const FftPlan& planM,
+                     const float2* twN, const float* wtaps, int ntap, float thresh, const FoldArgs& fa,
+                     const float2* tw64, cudaStream_t s) {
+  size_t smem = time_smem_bytes(N) + sizeof(float) * 4 * 64;
+  AB_CHECK_ARG(smem <= ctx->smem_optin, "time stage: nslice %d needs %zu bytes of shared memory (max %zu)", N, smem,
+               ctx->smem_optin);
+  AB_CHECK_ARG(wtaps && ntap >= 1 && ntap <= 8 && fa.ntap >= 1 && fa.ntap <= 8, "fused fold: bad ntap");
+  const int M = N / 2;
+  const float2* tws = nullptr;
+  if (M == Plan16464::N) {
+    AB_TRY(get_twiddle_stream(ctx, M, {7, 7, 7, 3, 16}, &tws));
+    return launch_fold_o<Plan16464, 512>(buf, ld, ninputs, P, N, planM, twN, tws, wtaps, ntap, thresh, fa, tw64, smem, s);
+  }
+  if (M == Plan16384::N) {
+    AB_TRY(get_twiddle_stream(ctx, M, {4, 16, 16, 16}, &tws));
+    return launch_fold_o<Plan16384, 512>(buf, ld, ninputs, P, N, planM, twN, tws, wtaps, ntap, thresh, fa, tw64, smem, s);
+  }
+  return launch_fold_o<NoPlan, kTimeThreads>(buf, ld, ninputs, P, N, planM, twN, nullptr, wtaps, ntap, thresh, fa,
+                                             tw64, smem, s);
 }
 
 }  // namespace ab
@@ -384,8 +667,7 @@ extern "C" int ab_ipfb(ab_ctx* ctx, const float* dat, const float* filt, float* 
   AB_TRY(get_twiddles(ctx, P, &twP));
   AB_TRY(get_twiddles(ctx, nslice, &twN));
   cudaStream_t s = as_stream(stream);
-  AB_TRY(launch_row_stage_c64((const float2*)dat, nslice, P, planP, twP, out, nslice, s));
-  AB_TRY(launch_time_stage(out, nslice, 1, P, (int)nslice, planM, twN, (const float2*)filt, nullptr, 0, 0.f,
-                           ctx->smem_optin, s));
+  AB_TRY(launch_row_stage_c64(ctx, (const float2*)dat, nslice, P, planP, twP, out, nslice, s));
+  AB_TRY(launch_time_stage(ctx, out, nslice, 1, P, (int)nslice, planM, twN, (const float2*)filt, nullptr, 0, 0.f, s));
   return AB_OK;
 }

@@ -26,20 +26,46 @@ struct Packed4Src {
 
 // Row stage for packed 4-bit input: local rows t in [0, nrows) of every
 // antenna; output input m = 2a+p into out (ld = column stride).
-int launch_row_stage_packed4(const Packed4Src& src, int nant, int nrows, int P, const FftPlan& plan,
+int launch_row_stage_packed4(ab_ctx* ctx, const Packed4Src& src, int nant, int nrows, int P, const FftPlan& plan,
                              const float2* twP, float* out, int64_t ld, cudaStream_t s);
 
 // Row stage for dense c64 rows (nslice, P/2+1): out (P, ld) for one input.
-int launch_row_stage_c64(const float2* dat, int64_t nslice, int P, const FftPlan& plan, const float2* twP,
-                         float* out, int64_t ld, cudaStream_t s);
+int launch_row_stage_c64(ab_ctx* ctx, const float2* dat, int64_t nslice, int P, const FftPlan& plan,
+                         const float2* twP, float* out, int64_t ld, cudaStream_t s);
 
 // Time stage, in place on ninputs columns sets of (P, ld) floats with
 // nslice = N valid rows.  Filter either from a c64 table (P, N/2+1) or, when
 // table == nullptr, evaluated on the fly from the window taps wtaps
 // (ntap, P) float32 and thresh.
-int launch_time_stage(float* buf, int64_t ld, int ninputs, int P, int N, const FftPlan& planM,
+int launch_time_stage(ab_ctx* ctx, float* buf, int64_t ld, int ninputs, int P, int N, const FftPlan& planM,
                       const float2* twN, const float2* table, const float* wtaps, int ntap, float thresh,
-                      size_t smem_optin, cudaStream_t s);
+                      cudaStream_t s);
+
+// Fused PFB fold epilogue of the time stage (streaming chain).  After the
+// inverse transform the CTA holds this chunk's IPFB output of one sample
+// phase n; timestream row r of the chunk is IPFB row cut + r (r in
+// [0, acclen)), rows r < 0 come from `state` (the previous chunk's last
+// 4*osamp rows of the same column, zero before the first chunk) and rows
+// >= acclen read as zero.  For blocks b in [0, nb) starting at row
+// row0 + b*osamp the kernel folds ntap taps with the fine window and takes the
+// osamp-point real DFT over the block's rows, writing W in the layout of
+// launch_pfb_stage_a; then it stores this chunk's last 4*osamp rows to state.
+struct FoldArgs {
+  int O;               // osamp (4..64, power of two)
+  int ntap;
+  int cut;
+  int acclen;
+  int64_t row0;        // local row of block 0 (may be negative)
+  int64_t nb;          // blocks to produce
+  const float* win;    // fine window (ntap * P * O)
+  float* W;            // stage-A output
+  float* state;        // (ninputs, P, 4*O) tail rows, read then rewritten
+};
+
+// Time stage with the fused fold epilogue (the column is not written back).
+int launch_time_fold(ab_ctx* ctx, float* buf, int64_t ld, int ninputs, int P, int N, const FftPlan& planM,
+                     const float2* twN, const float* wtaps, int ntap, float thresh, const FoldArgs& fa,
+                     const float2* tw64, cudaStream_t s);
 
 // sinc-Hamming window of ntap*lblock samples in double (pfb_utils.py:4-7)
 void sinc_hamming_host(int ntap, int64_t lblock, std::vector<double>& w);

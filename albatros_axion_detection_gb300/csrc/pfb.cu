@@ -2,17 +2,25 @@
 //   y[b, k] = sum_{i<ntap} ts[(b+i) L + k] win[i L + k];  out[b] = rfft(y[b])
 // computed as stage A (tap fold + O-point real DFT over t', k = n + P t')
 // and stage B (twiddle + P-point DFT over n), see pfb.cuh.
+#include <type_traits>
+
+#include "fft_static.cuh"
 #include "pfb.cuh"
 
 namespace ab {
 
 constexpr int kFoldCols = 32;   // sample phases per CTA (one warp lane each)
-constexpr int kFoldBlocks = 8;  // output blocks per CTA (one warp each)
+constexpr int kFoldBlocks = 16; // output blocks per CTA (one warp each)
+
+// shared memory of a stage-A CTA: data tile [kFoldCols][pitch] + window [ntap*O][kFoldCols]
+__host__ __device__ inline size_t stage_a_smem(int O, int ntap) {
+  return sizeof(float) * ((size_t)kFoldCols * ((kFoldBlocks + ntap - 1) * O + 1) + (size_t)ntap * O * kFoldCols);
+}
 
 template <int O>
 __global__ void __launch_bounds__(kFoldCols* kFoldBlocks)
     pfb_stage_a_kernel(TsSrc src, int P, int ntap, int64_t row0, int64_t nb, const float* __restrict__ win,
-                       float* __restrict__ W, const float2* __restrict__ tw64) {
+                       float* __restrict__ W, const float2* __restrict__ tw64, int vec4) {
   extern __shared__ float tile[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int n0 = blockIdx.y * kFoldCols;
@@ -20,7 +28,10 @@ __global__ void __launch_bounds__(kFoldCols* kFoldBlocks)
   const int in = blockIdx.z;
   const int RW = (kFoldBlocks + ntap - 1) * O;  // rows in the tile
   const int pitch = RW + 1;                     // odd pitch: conflict-free columns
+  float* wsm = tile + (size_t)kFoldCols * pitch;  // window [ntap*O][kFoldCols]
   const int64_t rbase = row0 + b0 * O;          // first tile row (timestream row)
+  // ---- window slice of these sample phases
+  for (int k = warp; k < ntap * O; k += kFoldBlocks) wsm[k * kFoldCols + lane] = __ldg(&win[(int64_t)k * P + n0 + lane]);
   // ---- load tile[n][r] = ts(rbase + r, n0 + n) ----
   if (src.natural) {
     for (int r = warp; r < RW; r += kFoldBlocks) {
@@ -28,6 +39,34 @@ __global__ void __launch_bounds__(kFoldCols* kFoldBlocks)
       float v = 0.f;
       if (rr >= 0 && rr < src.nrows_valid) v = __ldg(&src.cur[rr * P + n0 + lane]);
       tile[lane * pitch + r] = v;
+    }
+  } else if (vec4) {
+    // column layout, 16-byte aligned rows: float4 loads along t
+    const int RW4 = RW / 4;
+    for (int c = warp; c < kFoldCols; c += kFoldBlocks) {
+      const int64_t colbase = ((int64_t)in * P + n0 + c) * src.ld;
+      for (int q = lane; q < RW4; q += 32) {
+        int64_t rr = rbase + 4 * q;
+        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (rr + 3 < src.nrows_valid && rr >= 0) {
+          v = __ldg(reinterpret_cast<const float4*>(src.cur + colbase + src.off + rr));
+        } else if (rr + 3 < 0) {
+          if (src.prev) v = __ldg(reinterpret_cast<const float4*>(src.prev + colbase + src.prev_off + rr));
+        } else {
+          float e[4];
+          for (int u = 0; u < 4; u++) {
+            int64_t r1 = rr + u;
+            e[u] = 0.f;
+            if (r1 < src.nrows_valid) {
+              if (r1 >= 0) e[u] = src.cur[colbase + src.off + r1];
+              else if (src.prev) e[u] = src.prev[colbase + src.prev_off + r1];
+            }
+          }
+          v = make_float4(e[0], e[1], e[2], e[3]);
+        }
+        float* d = tile + c * pitch + 4 * q;
+        d[0] = v.x; d[1] = v.y; d[2] = v.z; d[3] = v.w;
+      }
     }
   } else {
     for (int c = warp; c < kFoldCols; c += kFoldBlocks) {
@@ -54,10 +93,10 @@ __global__ void __launch_bounds__(kFoldCols* kFoldBlocks)
 #pragma unroll
   for (int m = 0; m < H; m++) z[m] = make_float2(0.f, 0.f);
   for (int i = 0; i < ntap; i++) {
-    const float* wrow = win + (int64_t)i * O * P + n;
+    const float* wrow = wsm + i * O * kFoldCols + lane;
 #pragma unroll
     for (int tp = 0; tp < O; tp++) {
-      float v = col[i * O + tp] * __ldg(&wrow[(int64_t)tp * P]);
+      float v = col[i * O + tp] * wrow[tp * kFoldCols];
       if (O == 1) z[0].x += v;
       else if (tp & 1) z[tp >> 1].y += v;
       else z[tp >> 1].x += v;
@@ -77,9 +116,9 @@ __global__ void __launch_bounds__(kFoldCols* kFoldBlocks)
     for (int k = 1; k < H; k++) {
       float2 zk = z[k], zc = cconj(z[H - k]);
       float2 E = cscale(cadd(zk, zc), 0.5f);
-      float2 Dd = csub(zk, zc);                        // 2 i O_k
+      float2 Dd = csub(zk, zc);                            // 2 i O_k
       float2 Od = make_float2(0.5f * Dd.y, -0.5f * Dd.x);  // O_k
-      float2 w = tw64[k * (64 / O)];                   // exp(-2 pi i k / O)
+      float2 w = tw64[k * (64 / O)];                       // exp(-2 pi i k / O)
       float2 Wk = cadd(E, cmul(w, Od));
       out[2 * k] = Wk.x;
       out[2 * k + 1] = Wk.y;
@@ -104,17 +143,23 @@ __global__ void __launch_bounds__(kFoldCols* kFoldBlocks)
 // floats, then for each fine offset s carried by the group forms
 // V_s[n] = W_s[n] exp(-2 pi i s n / L) and its P-point DFT.
 constexpr int kStageBThreads = 512;
+struct NoPlanB {};
 
+template <class PL>
 __global__ void __launch_bounds__(kStageBThreads)
     pfb_stage_b_kernel(const float* __restrict__ W, int P, int O, int64_t nb, FftPlan plan,
-                       const float2* __restrict__ twL, int u0, int u1, float2* __restrict__ out) {
+                       const float2* __restrict__ twL, const float2* __restrict__ tws, int u0, int u1,
+                       float2* __restrict__ out) {
+  constexpr bool kStatic = !std::is_same<PL, NoPlanB>::value;
   extern __shared__ float4 smem4[];
   const int GW = O < 8 ? O : 8, NG = O / GW;
   const int g = blockIdx.y;
   const int64_t b = blockIdx.x;
   const int in = blockIdx.z;
-  float* wt = reinterpret_cast<float*>(smem4);          // P * GW floats
-  float2* buf = reinterpret_cast<float2*>(wt + (size_t)P * GW);  // P complex
+  const int64_t L = (int64_t)P * O;
+  float* wt = reinterpret_cast<float*>(smem4);                   // P * GW floats
+  float2* buf = reinterpret_cast<float2*>(wt + (size_t)P * GW);  // padded P complex
+  const SmemTw tw = load_smem_tw(buf + padded_len(P), twL, (int)L, threadIdx.x, blockDim.x);
   const float* src = W + ((((int64_t)in * nb + b) * NG + g) * P) * GW;
   if (GW >= 4) {
     const float4* s4 = reinterpret_cast<const float4*>(src);
@@ -123,7 +168,6 @@ __global__ void __launch_bounds__(kStageBThreads)
     for (int i = threadIdx.x; i < P * GW; i += blockDim.x) wt[i] = __ldg(&src[i]);
   }
   __syncthreads();
-  const int64_t L = (int64_t)P * O;
   const bool full = u1 < 0;
   const int64_t nq = full ? L / 2 + 1 : (int64_t)(u1 - u0) * O;
   float2* ob = out + ((int64_t)in * nb + b) * nq;
@@ -144,21 +188,95 @@ __global__ void __launch_bounds__(kStageBThreads)
           x = make_float2(wt[n * GW + e], wt[n * GW + e + 1]);
           if (v) x.y = -x.y;
         }
-        if (s) x = cmul(x, __ldg(&twL[(int64_t)s * n]));
-        buf[n] = x;
+        if (s) x = cmul(x, tw(s * n));
+        buf[pidx(n)] = x;
       }
       __syncthreads();
-      dif_forward(buf, plan, twL, (int)L);
+      if constexpr (kStatic) sdif<PL, kStageBThreads>(buf, tws, threadIdx.x);
+      else dif_forward(buf, plan, tw, (int)L, threadIdx.x, blockDim.x);
+      auto pos = [&](int u) -> int {
+        if constexpr (kStatic) return spos<PL>(u);
+        else return fft_pos(plan, u);
+      };
       // extract
       if (full) {
         int umax = (s == 0) ? P / 2 : P / 2 - 1;
-        for (int u = threadIdx.x; u <= umax; u += blockDim.x) ob[(int64_t)u * O + s] = buf[fft_pos(plan, u)];
+        for (int u = threadIdx.x; u <= umax; u += blockDim.x) ob[(int64_t)u * O + s] = buf[pidx(pos(u))];
       } else {
         for (int u = u0 + threadIdx.x; u < u1; u += blockDim.x)
-          ob[(int64_t)(u - u0) * O + s] = buf[fft_pos(plan, u)];
+          ob[(int64_t)(u - u0) * O + s] = buf[pidx(pos(u))];
       }
       __syncthreads();
     }
+  }
+}
+
+// Stage B specialised for P = 4096 and osamp >= 8 (8 floats per group): the
+// group's W tile is stored transposed ([float][n]) so the V build reads
+// consecutive n, and the CTA's two halves (256 threads each) transform two
+// fine offsets at once: s = c and s = O - c of the same complex slot c.
+constexpr int kB2Threads = 512;
+__host__ __device__ inline size_t stage_b2_smem() {
+  return sizeof(float) * 8 * 4096 + sizeof(float2) * (2 * (size_t)padded_len(4096) + 1024);
+}
+
+__global__ void __launch_bounds__(kB2Threads)
+    pfb_stage_b4096_kernel(const float* __restrict__ W, int O, int64_t nb, const float2* __restrict__ twL,
+                           const float2* __restrict__ tws, int u0, int u1, float2* __restrict__ out) {
+  constexpr int P = 4096, GW = 8, PLN = padded_len(4096);
+  extern __shared__ float4 smem4[];
+  const int NG = O / GW;
+  const int g = blockIdx.y;
+  const int64_t b = blockIdx.x;
+  const int in = blockIdx.z;
+  const int L = P * O;
+  const int tid = threadIdx.x, half = tid >> 8, ltid = tid & 255;
+  float* wt = reinterpret_cast<float*>(smem4);                  // [8][4096]
+  float2* bufs = reinterpret_cast<float2*>(wt + 8 * P);          // 2 padded buffers
+  float2* vtw = bufs + 2 * PLN;                                  // hi[512], lo[512]: exp(-2 pi i e / L)
+  const int nhi = (L + 511) / 512;
+  for (int i = tid; i < nhi; i += kB2Threads) vtw[i] = __ldg(&twL[(int64_t)i * 512]);
+  for (int i = tid; i < 512; i += kB2Threads) vtw[512 + i] = i < L ? __ldg(&twL[i]) : make_float2(1.f, 0.f);
+  const float4* s4 = reinterpret_cast<const float4*>(W + ((((int64_t)in * nb + b) * NG + g) * P) * GW);
+  for (int i = tid; i < P * GW / 4; i += kB2Threads) {
+    float4 v = __ldg(&s4[i]);
+    int n = i >> 1, e0 = (i & 1) * 4;
+    wt[(e0 + 0) * P + n] = v.x;
+    wt[(e0 + 1) * P + n] = v.y;
+    wt[(e0 + 2) * P + n] = v.z;
+    wt[(e0 + 3) * P + n] = v.w;
+  }
+  __syncthreads();
+  const bool full = u1 < 0;
+  const int64_t nq = full ? L / 2 + 1 : (int64_t)(u1 - u0) * O;
+  float2* ob = out + ((int64_t)in * nb + b) * nq;
+  float2* buf = bufs + half * PLN;
+  for (int e = 0; e < GW; e += 2) {
+    const int c = (g * GW + e) / 2;
+    int s;
+    if (c == 0) s = half == 0 ? 0 : O / 2;
+    else s = half == 0 ? c : O - c;
+    const float* wr = wt + e * P;
+    const float* wi = wt + (e + 1) * P;
+    for (int n = ltid; n < P; n += 256) {
+      float2 x;
+      if (c == 0) x = make_float2(half == 0 ? wr[n] : wi[n], 0.f);
+      else x = make_float2(wr[n], half == 0 ? wi[n] : -wi[n]);
+      if (s) {
+        int ex = s * n;
+        x = cmul(x, cmul(vtw[ex >> 9], vtw[512 + (ex & 511)]));
+      }
+      buf[pidx(n)] = x;
+    }
+    __syncthreads();
+    sdif<Plan4096, 256>(buf, tws, ltid);
+    if (full) {
+      int umax = (s == 0) ? P / 2 : P / 2 - 1;
+      for (int u = ltid; u <= umax; u += 256) ob[(int64_t)u * O + s] = buf[pidx(spos<Plan4096>(u))];
+    } else {
+      for (int u = u0 + ltid; u < u1; u += 256) ob[(int64_t)(u - u0) * O + s] = buf[pidx(spos<Plan4096>(u))];
+    }
+    __syncthreads();
   }
 }
 
@@ -167,14 +285,18 @@ int launch_pfb_stage_a(const TsSrc& src, int ninputs, int P, int O, int ntap, in
   AB_CHECK_ARG(P % kFoldCols == 0, "pfb: lblock/osamp %d must be a multiple of %d", P, kFoldCols);
   AB_CHECK_ARG(ntap >= 1 && ntap <= 16, "pfb: ntap %d out of range", ntap);
   if (nb <= 0) return AB_OK;
-  size_t smem = sizeof(float) * (size_t)kFoldCols * ((kFoldBlocks + ntap - 1) * O + 1);
-  AB_CHECK_ARG(smem <= 200 * 1024, "pfb: tile of %zu bytes too large (osamp %d, ntap %d)", smem, O, ntap);
+  size_t smem = stage_a_smem(O, ntap);
+  AB_CHECK_ARG(smem <= 220 * 1024, "pfb: tile of %zu bytes too large (osamp %d, ntap %d)", smem, O, ntap);
+  // float4 tile loads need 16-byte aligned column rows
+  const int vec4 = !src.natural && src.ld % 4 == 0 && src.off % 4 == 0 && src.prev_off % 4 == 0 &&
+                   row0 % 4 == 0 && ((kFoldBlocks + ntap - 1) * O) % 4 == 0 && ((uintptr_t)src.cur & 15) == 0 &&
+                   ((uintptr_t)src.prev & 15) == 0;
   dim3 grid((unsigned)((nb + kFoldBlocks - 1) / kFoldBlocks), (unsigned)(P / kFoldCols), (unsigned)ninputs);
   dim3 block(kFoldCols * kFoldBlocks);
 #define AB_STAGE_A(OO)                                                                                        \
   case OO:                                                                                                   \
-    AB_CUDA(cudaFuncSetAttribute(pfb_stage_a_kernel<OO>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024)); \
-    pfb_stage_a_kernel<OO><<<grid, block, smem, s>>>(src, P, ntap, row0, nb, win, W, tw64);                   \
+    AB_CUDA(cudaFuncSetAttribute(pfb_stage_a_kernel<OO>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024)); \
+    pfb_stage_a_kernel<OO><<<grid, block, smem, s>>>(src, P, ntap, row0, nb, win, W, tw64, vec4);             \
     break;
   switch (O) {
     AB_STAGE_A(1)
@@ -193,15 +315,28 @@ int launch_pfb_stage_a(const TsSrc& src, int ninputs, int P, int O, int ntap, in
   return AB_OK;
 }
 
-int launch_pfb_stage_b(const float* W, int ninputs, int P, int O, int64_t nb, const FftPlan& planP,
+int launch_pfb_stage_b(ab_ctx* ctx, const float* W, int ninputs, int P, int O, int64_t nb, const FftPlan& planP,
                        const float2* twL, int u0, int u1, float2* out, cudaStream_t s) {
   if (nb <= 0) return AB_OK;
   const int GW = O < 8 ? O : 8;
-  size_t smem = sizeof(float) * (size_t)P * GW + sizeof(float2) * (size_t)P;
+  size_t smem = sizeof(float) * (size_t)P * GW + sizeof(float2) * ((size_t)padded_len(P) + smem_tw_len(P * O));
   AB_CHECK_ARG(smem <= 220 * 1024, "pfb: stage B needs %zu bytes of shared memory", smem);
-  AB_CUDA(cudaFuncSetAttribute(pfb_stage_b_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
   dim3 grid((unsigned)nb, (unsigned)(O / GW), (unsigned)ninputs);
-  pfb_stage_b_kernel<<<grid, kStageBThreads, smem, s>>>(W, P, O, nb, planP, twL, u0, u1, out);
+  if (P == Plan4096::N && O >= 8) {
+    const float2* tws;
+    AB_TRY(get_twiddle_stream(ctx, P, {16, 16, 16}, &tws));
+    size_t sm2 = stage_b2_smem();
+    AB_CUDA(cudaFuncSetAttribute(pfb_stage_b4096_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm2));
+    pfb_stage_b4096_kernel<<<grid, kB2Threads, sm2, s>>>(W, O, nb, twL, tws, u0, u1, out);
+  } else if (P == Plan4096::N) {
+    const float2* tws;
+    AB_TRY(get_twiddle_stream(ctx, P, {16, 16, 16}, &tws));
+    AB_CUDA(cudaFuncSetAttribute(pfb_stage_b_kernel<Plan4096>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
+    pfb_stage_b_kernel<Plan4096><<<grid, kStageBThreads, smem, s>>>(W, P, O, nb, planP, twL, tws, u0, u1, out);
+  } else {
+    AB_CUDA(cudaFuncSetAttribute(pfb_stage_b_kernel<NoPlanB>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024));
+    pfb_stage_b_kernel<NoPlanB><<<grid, kStageBThreads, smem, s>>>(W, P, O, nb, planP, twL, nullptr, u0, u1, out);
+  }
   AB_LAUNCH_CHECK();
   return AB_OK;
 }
@@ -245,7 +380,7 @@ static int pfb_common(ab_ctx* ctx, const float* ts, int64_t nsamp, const float* 
   TsSrc src{ts, nullptr, 0, 0, 0, nsamp / P, 1};
   cudaStream_t s = as_stream(stream);
   AB_TRY(launch_pfb_stage_a(src, 1, P, O, (int)ntap, 0, nblock, win, (float*)Wv, ctx->tw64, s));
-  AB_TRY(launch_pfb_stage_b((const float*)Wv, 1, P, O, nblock, planP, twL, u0, u1, (float2*)out, s));
+  AB_TRY(launch_pfb_stage_b(ctx, (const float*)Wv, 1, P, O, nblock, planP, twL, u0, u1, (float2*)out, s));
   return AB_OK;
 }
 

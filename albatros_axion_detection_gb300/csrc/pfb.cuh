@@ -36,7 +36,7 @@ int launch_pfb_stage_a(const TsSrc& src, int ninputs, int P, int O, int ntap, in
 
 // Stage B.  band: u in [u0, u1), out[(in*nb + b)*(u1-u0)*O + (u-u0)*O + s];
 // full (u1 < 0): out[(in*nb + b)*(L/2+1) + q] for q <= L/2.
-int launch_pfb_stage_b(const float* W, int ninputs, int P, int O, int64_t nb, const FftPlan& planP,
+int launch_pfb_stage_b(ab_ctx* ctx, const float* W, int ninputs, int P, int O, int64_t nb, const FftPlan& planP,
                        const float2* twL, int u0, int u1, float2* out, cudaStream_t s);
 
 }  // namespace ab

@@ -132,9 +132,11 @@ def stage_bytes(sc):
 
 def run_ours(args):
     import torch
-    global NSPEC
+    global NSPEC, NANT
     if args.chunks:
         NSPEC = ACCLEN * args.chunks
+    if args.nant:
+        NANT = args.nant
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -317,6 +319,7 @@ def main():
     ap.add_argument("--chunks", type=int, default=None,
                     help="stream only this many 2^15-spectrum chunks (smaller case for profiling; "
                          "every launch keeps its full size)")
+    ap.add_argument("--nant", type=int, default=None, help="antennas (profiling case; default 2)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
