@@ -123,8 +123,10 @@ def stage_bytes(sc):
     L = P * OSAMP
     return {
         "row_ifft": NANT * nslice * 2 * NCHAN_RAW + M * P * nslice * 4,      # packets in, f32 rows out
-        "time_deconv": 2 * M * P * nslice * 4,                              # column in + out
-        "pfb_fold": M * P * ACCLEN * 4 + M * nb * L * 4,                     # timestream in, W out
+        # time-axis deconvolution with the PFB fold fused in: IPFB column in,
+        # folded/DFT'd fine blocks (W) out
+        "time_deconv": M * P * nslice * 4 + M * nb * L * 4,
+        "pfb_fold": 0,                                                      # fused into time_deconv
         "pfb_dft": M * nb * L * 4 + M * nb * nq * 8,                         # W in, band spectra out
         "xcorr": M * nb * nq * 8,                                           # band spectra in
     }
