@@ -379,6 +379,70 @@ extern "C" int ab_xcorr_coarse_4bit(ab_ctx* ctx, const uint8_t* raw, int64_t ant
                           (long long*)G, out_re, out_im, as_stream(stream));
 }
 
+// ---------------------------------------------------------------------------
+// Allocation-free coarse correlator.
+//
+// Some callers cannot allocate device memory while they run: a correlator
+// service that reserves its whole device-memory budget at start-up and must
+// not grow it, a host application whose own allocator owns the device memory
+// and forbids raw cudaMalloc, or a latency-critical loop where an allocation
+// (which can synchronise the device or fail under memory pressure) is not
+// acceptable.  For them this entry point keeps its int64 partial sums in a
+// fixed buffer compiled into the library instead of the context's scratch.
+//
+// The buffer is a file-scope __device__ array of kNoAllocScratchBytes (16 MiB);
+// every GPU that loads this library holds it until the process exits.  In
+// host code the array's name is only a host-side stand-in, so its device
+// address is fetched once per device with cudaGetSymbolAddress the first time
+// the entry point runs on that device; make that first call before any stream
+// capture.  All calls share the one buffer: the entry point clears it at the
+// start of every call, and calls whose work overlaps on the GPU (different
+// streams, or several host threads on one device) race on it.
+constexpr size_t kNoAllocScratchBytes = 16u << 20;
+static __device__ __align__(256) long long g_noalloc_scratch[kNoAllocScratchBytes / sizeof(long long)];
+
+namespace {
+std::mutex g_noalloc_mu;
+void* g_noalloc_addr[128] = {nullptr};
+}  // namespace
+
+extern "C" int ab_xcorr_coarse_4bit_noalloc(const uint8_t* raw, int64_t ant_stride, int64_t nant, int64_t nspec,
+                                            int64_t nchan, int64_t rowstart, int64_t nrows, const int32_t* rows,
+                                            const int64_t* channels, int64_t ncols, int64_t chunk_rows,
+                                            int64_t* out_re, int64_t* out_im, void* stream) {
+  AB_CHECK_ARG(raw && channels && out_re && out_im, "ab_xcorr_coarse_4bit_noalloc: NULL pointer");
+  AB_CHECK_ARG(nant >= 1 && nant <= 32 && nchan >= 1 && ncols >= 1 && nrows >= 1,
+               "ab_xcorr_coarse_4bit_noalloc: bad sizes (1 <= nant <= 32)");
+  AB_CHECK_ARG(rows || (rowstart >= 0 && rowstart + nrows <= nspec), "ab_xcorr_coarse_4bit_noalloc: rows out of range");
+  AB_CHECK_ARG(ant_stride >= nspec * 2 * nchan || nant == 1, "ab_xcorr_coarse_4bit_noalloc: antenna stride too small");
+  if (chunk_rows <= 0 || chunk_rows > nrows) chunk_rows = nrows;
+  AB_CHECK_ARG(chunk_rows <= (1ll << 24), "ab_xcorr_coarse_4bit_noalloc: chunk_rows must be <= 2^24");
+  const size_t need = coarse_xcorr_scratch_bytes(nant, nrows, ncols, chunk_rows);
+  AB_CHECK_ARG(need <= kNoAllocScratchBytes,
+               "ab_xcorr_coarse_4bit_noalloc: this call needs %zu bytes of scratch but the built-in buffer holds "
+               "%zu; split it into calls with fewer channels or chunks, or use ab_xcorr_coarse_4bit",
+               need, kNoAllocScratchBytes);
+  int dev = 0;
+  AB_CUDA(cudaGetDevice(&dev));
+  AB_CHECK_ARG(dev >= 0 && dev < 128, "ab_xcorr_coarse_4bit_noalloc: device index %d out of range", dev);
+  void* G = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+      void* p = nullptr;
+      cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+      if (e != cudaSuccess || !p) {
+        set_error("ab_xcorr_coarse_4bit_noalloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
+        return AB_ERR_CUDA;
+      }
+      g_noalloc_addr[dev] = p;
+    }
+    G = g_noalloc_addr[dev];
+  }
+  return coarse_xcorr_run(nullptr, raw, ant_stride, nant, nchan, rowstart, nrows, rows, channels, ncols, chunk_rows,
+                          (long long*)G, out_re, out_im, as_stream(stream));
+}
+
 extern "C" int ab_avg_xcorr_4bit_pairs(const uint8_t* data0, const uint8_t* data1, const int32_t* rows0,
                                        const int32_t* rows1, int64_t nmatch, int64_t ncol, int64_t* re, int64_t* im,
                                        void* stream) {

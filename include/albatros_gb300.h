@@ -147,6 +147,21 @@ int ab_xcorr_coarse_4bit(ab_ctx *ctx, const uint8_t *raw, int64_t ant_stride, in
                          const int64_t *channels, int64_t ncols, int64_t chunk_rows, int64_t *out_re,
                          int64_t *out_im, void *stream);
 
+/* ab_xcorr_coarse_4bit_noalloc: no counterpart in the reference.  Same
+ * arguments and results as ab_xcorr_coarse_4bit without the context, for
+ * callers that must not allocate device memory while they run (a service
+ * that fixes its memory budget at start-up, a host whose own allocator owns
+ * the device, a loop where an allocation could stall or fail).  Its partial
+ * sums live in a 16 MiB buffer built into the library (held on every device
+ * that loads it until exit); calls needing more scratch than that, i.e.
+ * nchunks * ncols * (16*ceil(nant/4))^2 * 8 bytes, return AB_ERR_ARG.  The
+ * first call on a device looks up the buffer's device address and should come
+ * before any stream capture.  All calls share the buffer (cleared at the start
+ * of each call), so calls that overlap on the GPU race. */
+int ab_xcorr_coarse_4bit_noalloc(const uint8_t *raw, int64_t ant_stride, int64_t nant, int64_t nspec, int64_t nchan,
+                                 int64_t rowstart, int64_t nrows, const int32_t *rows, const int64_t *channels,
+                                 int64_t ncols, int64_t chunk_rows, int64_t *out_re, int64_t *out_im, void *stream);
+
 /* ab_avg_xcorr_4bit_pairs: device form of avg_xcorr_4bit / avg_xcorr_4bit_2ant
  * (albatros_analysis/src/correlations/correlations_cpu.c:128-271) on sortpols'd
  * 4-bit data (rows, ncol). rows0/rows1: device int32 matched row indices
