@@ -369,19 +369,20 @@ __global__ void __launch_bounds__(NTHR)
 
   const float scale = 0.5f / (float)N;  // irfft 1/N and the untangle's 1/2
   const float t2 = thresh * thresh;
-  auto filt = [&](int k) -> float2 {
+  // filter at bin k from z = exp(-2 pi i k / N): m = sum_t w_t z^t (Horner),
+  // H = m (1 + t^2) / (t^2 + |m|^2), or 1/conj(m) without threshold
+  auto filt_z = [&](int k, float2 z) -> float2 {
     float2 h;
     if (TABLE) {
       h = __ldg(&table[(int64_t)n * (M + 1) + k]);
     } else {
-      float2 m = make_float2(w[0], 0.f);
-      int e = 0;
-      for (int t = 1; t < ntap; t++) {
-        e += k;
-        if (e >= N) e -= N;
-        float2 z = tw(e);
-        m.x = fmaf(w[t], z.x, m.x);
-        m.y = fmaf(w[t], z.y, m.y);
+      float2 m = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int t = 7; t >= 0; t--) {
+        if (t < ntap) {
+          m = cmul(m, z);
+          m.x += w[t];
+        }
       }
       float a2 = fmaf(m.x, m.x, m.y * m.y);
       float g = thresh > 0.f ? (1.f + t2) / (t2 + a2) : 1.f / a2;
@@ -394,21 +395,23 @@ __global__ void __launch_bounds__(NTHR)
     if (k == 0) {
       float2 z = buf[0];
       float x0 = 2.f * (z.x + z.y), xm = 2.f * (z.x - z.y);  // 2 X[0], 2 X[M] (real)
-      float y0 = x0 * filt(0).x, ym = xm * filt(M).x;          // real parts only (irfft)
-      buf[0] = make_float2(y0 + ym, y0 - ym);
+      // z^0 = 1 and z^M = -1 (exp(-i pi))
+      float y0 = x0 * filt_z(0, make_float2(1.f, 0.f)).x, ym = xm * filt_z(M, make_float2(-1.f, 0.f)).x;
+      buf[0] = make_float2(y0 + ym, y0 - ym);  // real parts only (irfft)
       continue;
     }
     int pk = pidx(fpos<PL>(plan, k)), pc = pidx(fpos<PL>(plan, M - k));
     float2 zk = buf[pk], zc = buf[pc];
     float2 w1 = tw(k);                           // exp(-2 pi i k / N)
+    const float2 w1c = make_float2(-w1.x, w1.y);  // exp(-2 pi i (M-k) / N) = -conj(w1)
     float2 E = cadd(zk, cconj(zc));              // 2 E_k
     float2 Od = csub(zk, cconj(zc));             // 2 i O_k
     float2 O = make_float2(Od.y, -Od.x);         // 2 O_k = (2 i O_k) / i
     float2 wO = cmul(w1, O);
     float2 Xk = cadd(E, wO);                     // 2 X_k
     float2 Xc = cconj(csub(E, wO));              // 2 X_{M-k}
-    float2 Yk = cmul(Xk, filt(k));
-    float2 Yc = cmul(Xc, filt(M - k));
+    float2 Yk = cmul(Xk, filt_z(k, w1));
+    float2 Yc = cmul(Xc, filt_z(M - k, w1c));
     float2 Et = cadd(Yk, cconj(Yc));
     float2 Ot = cmulc(csub(Yk, cconj(Yc)), w1);  // (Y_k - conj Y_{M-k}) conj(w)
     float2 iOt = make_float2(-Ot.y, Ot.x);
@@ -521,12 +524,12 @@ int launch_time_stage(ab_ctx* ctx, float* buf, int64_t ld, int ninputs, int P, i
   const float2* tws = nullptr;
   if (M == Plan16464::N) {
     AB_TRY(get_twiddle_stream(ctx, M, {7, 7, 7, 3, 16}, &tws));
-    return launch_time_t<Plan16464, 512>(ctx, buf, ld, ninputs, P, N, planM, twN, tws, table, wtaps, ntap, thresh,
+    return launch_time_t<Plan16464, 1024>(ctx, buf, ld, ninputs, P, N, planM, twN, tws, table, wtaps, ntap, thresh,
                                          smem, s);
   }
   if (M == Plan16384::N) {
     AB_TRY(get_twiddle_stream(ctx, M, {4, 16, 16, 16}, &tws));
-    return launch_time_t<Plan16384, 512>(ctx, buf, ld, ninputs, P, N, planM, twN, tws, table, wtaps, ntap, thresh,
+    return launch_time_t<Plan16384, 1024>(ctx, buf, ld, ninputs, P, N, planM, twN, tws, table, wtaps, ntap, thresh,
                                          smem, s);
   }
   return launch_time_t<NoPlan, kTimeThreads>(ctx, buf, ld, ninputs, P, N, planM, twN, nullptr, table, wtaps, ntap,
@@ -572,11 +575,11 @@ int launch_time_fold(ab_ctx* ctx, float* buf, int64_t ld, int ninputs, int P, in
   const float2* tws = nullptr;
   if (M == Plan16464::N) {
     AB_TRY(get_twiddle_stream(ctx, M, {7, 7, 7, 3, 16}, &tws));
-    return launch_fold_o<Plan16464, 512>(buf, ld, ninputs, P, N, planM, twN, tws, wtaps, ntap, thresh, fa, tw64, smem, s);
+    return launch_fold_o<Plan16464, 1024>(buf, ld, ninputs, P, N, planM, twN, tws, wtaps, ntap, thresh, fa, tw64, smem, s);
   }
   if (M == Plan16384::N) {
     AB_TRY(get_twiddle_stream(ctx, M, {4, 16, 16, 16}, &tws));
-    return launch_fold_o<Plan16384, 512>(buf, ld, ninputs, P, N, planM, twN, tws, wtaps, ntap, thresh, fa, tw64, smem, s);
+    return launch_fold_o<Plan16384, 1024>(buf, ld, ninputs, P, N, planM, twN, tws, wtaps, ntap, thresh, fa, tw64, smem, s);
   }
   return launch_fold_o<NoPlan, kTimeThreads>(buf, ld, ninputs, P, N, planM, twN, nullptr, wtaps, ntap, thresh, fa,
                                              tw64, smem, s);

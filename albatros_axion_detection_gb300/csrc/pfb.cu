@@ -280,6 +280,72 @@ __global__ void __launch_bounds__(kB2Threads)
   }
 }
 
+// Stage B, one CTA per (complex slot c, block, input) for P = 4096: the two
+// fine offsets carried by slot c (s = c and O - c; for c = 0 the real W_0 and
+// W_{O/2}) are transformed at once by the CTA's two 256-thread halves.  Each
+// thread keeps W_c of 8 sample phases in registers while building V, so the
+// CTA needs only the two FFT buffers in shared memory (two CTAs per SM).
+constexpr int kBSThreads = 512;
+__host__ __device__ inline size_t stage_bslot_smem() {
+  return sizeof(float2) * (2 * (size_t)padded_len(4096) + 1024);
+}
+
+__global__ void __launch_bounds__(kBSThreads, 2)
+    pfb_stage_bslot_kernel(const float* __restrict__ W, int O, int64_t nb, const float2* __restrict__ twL,
+                           const float2* __restrict__ tws, int u0, int u1, float2* __restrict__ out) {
+  constexpr int P = 4096, PLN = padded_len(4096), PER = P / kBSThreads;
+  extern __shared__ float2 sm2[];
+  const int GW = O < 8 ? O : 8, NG = O / GW;
+  const int c = blockIdx.x;
+  const int64_t b = blockIdx.y;
+  const int in = blockIdx.z;
+  const int L = P * O;
+  const int tid = threadIdx.x, half = tid >> 8, ltid = tid & 255;
+  float2* bufs = sm2;
+  float2* vtw = bufs + 2 * PLN;  // hi[512], lo[512]: exp(-2 pi i e / L)
+  const int nhi = (L + 511) / 512;
+  for (int i = tid; i < nhi; i += kBSThreads) vtw[i] = __ldg(&twL[(int64_t)i * 512]);
+  for (int i = tid; i < 512; i += kBSThreads) vtw[512 + i] = i < L ? __ldg(&twL[i]) : make_float2(1.f, 0.f);
+  // W_c of sample phases n = tid + 512 q
+  const int g = (2 * c) / GW, e = (2 * c) % GW;
+  const float* src = W + ((((int64_t)in * nb + b) * NG + g) * P) * GW + e;
+  float2 wv[PER];
+#pragma unroll
+  for (int q = 0; q < PER; q++) wv[q] = __ldg(reinterpret_cast<const float2*>(src + (size_t)(tid + q * kBSThreads) * GW));
+  const int s0 = c, s1 = (c == 0) ? O / 2 : O - c;
+  __syncthreads();
+#pragma unroll
+  for (int h = 0; h < 2; h++) {
+    const int s = h ? s1 : s0;
+    float2* buf = bufs + h * PLN;
+#pragma unroll
+    for (int q = 0; q < PER; q++) {
+      const int n = tid + q * kBSThreads;
+      float2 x;
+      if (c == 0) x = make_float2(h ? wv[q].y : wv[q].x, 0.f);
+      else x = h ? cconj(wv[q]) : wv[q];
+      if (s) {
+        const int ex = s * n;
+        x = cmul(x, cmul(vtw[ex >> 9], vtw[512 + (ex & 511)]));
+      }
+      buf[pidx(n)] = x;
+    }
+  }
+  __syncthreads();
+  float2* buf = bufs + half * PLN;
+  sdif<Plan4096, 256>(buf, tws, ltid);
+  const int s = half ? s1 : s0;
+  const bool full = u1 < 0;
+  const int64_t nq = full ? L / 2 + 1 : (int64_t)(u1 - u0) * O;
+  float2* ob = out + ((int64_t)in * nb + b) * nq;
+  if (full) {
+    int umax = (s == 0) ? P / 2 : P / 2 - 1;
+    for (int u = ltid; u <= umax; u += 256) ob[(int64_t)u * O + s] = buf[pidx(spos<Plan4096>(u))];
+  } else {
+    for (int u = u0 + ltid; u < u1; u += 256) ob[(int64_t)(u - u0) * O + s] = buf[pidx(spos<Plan4096>(u))];
+  }
+}
+
 int launch_pfb_stage_a(const TsSrc& src, int ninputs, int P, int O, int ntap, int64_t row0, int64_t nb,
                        const float* win, float* W, const float2* tw64, cudaStream_t s) {
   AB_CHECK_ARG(P % kFoldCols == 0, "pfb: lblock/osamp %d must be a multiple of %d", P, kFoldCols);
@@ -322,7 +388,14 @@ int launch_pfb_stage_b(ab_ctx* ctx, const float* W, int ninputs, int P, int O, i
   size_t smem = sizeof(float) * (size_t)P * GW + sizeof(float2) * ((size_t)padded_len(P) + smem_tw_len(P * O));
   AB_CHECK_ARG(smem <= 220 * 1024, "pfb: stage B needs %zu bytes of shared memory", smem);
   dim3 grid((unsigned)nb, (unsigned)(O / GW), (unsigned)ninputs);
-  if (P == Plan4096::N && O >= 8) {
+  if (P == Plan4096::N && O >= 2 && nb <= 65535) {
+    const float2* tws;
+    AB_TRY(get_twiddle_stream(ctx, P, {16, 16, 16}, &tws));
+    size_t sm = stage_bslot_smem();
+    AB_CUDA(cudaFuncSetAttribute(pfb_stage_bslot_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    dim3 g2((unsigned)(O / 2), (unsigned)nb, (unsigned)ninputs);
+    pfb_stage_bslot_kernel<<<g2, kBSThreads, sm, s>>>(W, O, nb, twL, tws, u0, u1, out);
+  } else if (P == Plan4096::N && O >= 8) {
     const float2* tws;
     AB_TRY(get_twiddle_stream(ctx, P, {16, 16, 16}, &tws));
     size_t sm2 = stage_b2_smem();
