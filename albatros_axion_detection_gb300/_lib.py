@@ -39,7 +39,7 @@ SIGNATURES = {
     "ab_xcorr_coarse_4bit_noalloc": (I32, [P, I64, I64, I64, I64, I64, I64, P, P, I64, I64, P, P, P]),
     "ab_avg_xcorr_4bit_pairs": (I32, [P, P, P, P, I64, I64, P, P, P]),
     "ab_avg_xcorr_1bit_pairs": (I32, [P, P, P, P, I64, I64, I64, P, P]),
-    "ab_stream_create": (I32, [P, I64, I64, P, P, I64, I64, I64, I64, I64, D, I64, I64, I64, I64,
+    "ab_stream_create": (I32, [P, I64, I64, I64, P, P, I64, I64, I64, I64, I64, D, I64, I64, I64, I64,
                                ctypes.POINTER(P)]),
     "ab_stream_destroy": (I32, [P]),
     "ab_stream_reset": (I32, [P, P]),

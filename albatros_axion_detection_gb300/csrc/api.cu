@@ -39,6 +39,55 @@ bool make_plan(int n, FftPlan* p) {
   return true;
 }
 
+bool make_plan_from(int n, const std::vector<int>& radices, FftPlan* p) {
+  if ((int)radices.size() > kMaxPasses) return false;
+  p->n = n;
+  p->npass = (int)radices.size();
+  int prod = 1;
+  for (int q = 0; q < p->npass; q++) {
+    p->radix[q] = radices[q];
+    prod *= radices[q];
+    p->span[q] = n / prod;
+  }
+  return prod == n;
+}
+
+static int host_pos(const FftPlan& p, int f) {
+  int pos = 0;
+  for (int q = 0; q < p.npass; q++) {
+    pos += (f % p.radix[q]) * p.span[q];
+    f /= p.radix[q];
+  }
+  return pos;
+}
+static int host_pidx(int i) { return i + (i >> 4); }
+
+int get_pair_table(ab_ctx* ctx, const FftPlan& p, const int2** out) {
+  std::vector<int> key(p.radix, p.radix + p.npass);
+  key.insert(key.begin(), p.n);
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  auto it = ctx->pair_tables.find(key);
+  if (it != ctx->pair_tables.end()) {
+    *out = it->second;
+    return AB_OK;
+  }
+  const int M = p.n;
+  std::vector<int2> h((size_t)M / 2 + 1);
+  for (int k = 0; k <= M / 2; k++) {
+    int c = (M - k) % M;
+    h[(size_t)k] = make_int2(host_pidx(host_pos(p, k)), host_pidx(host_pos(p, c)));
+  }
+  int2* d = nullptr;
+  if (cudaMalloc(&d, sizeof(int2) * h.size()) != cudaSuccess) {
+    set_error("cudaMalloc of a pair table failed");
+    return AB_ERR_NOMEM;
+  }
+  AB_CUDA(cudaMemcpy(d, h.data(), sizeof(int2) * h.size(), cudaMemcpyHostToDevice));
+  ctx->pair_tables[key] = d;
+  *out = d;
+  return AB_OK;
+}
+
 int get_twiddles(ab_ctx* ctx, int64_t T, const float2** out) {
   std::lock_guard<std::mutex> lk(ctx->mu);
   auto it = ctx->twiddles.find(T);
@@ -192,6 +241,7 @@ int ab_ctx_destroy(ab_ctx* ctx) {
   cudaSetDevice(ctx->device);
   for (auto& kv : ctx->twiddles) cudaFree(kv.second);
   for (auto& kv : ctx->streams) cudaFree(kv.second);
+  for (auto& kv : ctx->pair_tables) cudaFree(kv.second);
   for (auto& kv : ctx->scratch)
     if (kv.second.first) cudaFree(kv.second.first);
   delete ctx;

@@ -36,6 +36,7 @@ struct ab_stream {
   ab_ctx* ctx = nullptr;
   int nant = 0, M = 0, P = 4096, O = 1, ntap = 4;
   int64_t nchan_raw = 0, nsel = 0, acclen = 0, cut = 0, nslice = 0;
+  int bits = 4;
   int64_t nblock = 0, njobs = 0, q0 = 0, q1 = 0, nq = 0;
   float thresh = 0.f;
   FftPlan planP{}, planM{};
@@ -85,11 +86,13 @@ static void stream_free(ab_stream* st) {
     }                                                                     \
   } while (0)
 
-extern "C" int ab_stream_create(ab_ctx* ctx, int64_t nant, int64_t nchan_raw, const int64_t* chan_cols,
+extern "C" int ab_stream_create(ab_ctx* ctx, int64_t nant, int64_t nchan_raw, int64_t bits, const int64_t* chan_cols,
                                 const int64_t* chan_abs, int64_t nsel, int64_t acclen, int64_t cut, int64_t osamp,
                                 int64_t ntap, double thresh, int64_t nblock, int64_t njobs, int64_t q0, int64_t q1,
                                 ab_stream** out) {
   AB_CHECK_ARG(ctx && chan_cols && chan_abs && out, "ab_stream_create: NULL pointer");
+  AB_CHECK_ARG(bits == 4 || bits == 1, "ab_stream_create: bits must be 4 or 1");
+  AB_CHECK_ARG(bits == 4 || nchan_raw % 2 == 0, "ab_stream_create: 1-bit data needs an even channel count");
   AB_CHECK_ARG(nant >= 1 && nchan_raw >= 1 && nsel >= 1 && acclen >= 1 && cut >= 1 && ntap >= 1 && ntap <= 8,
                "ab_stream_create: bad sizes (cut >= 1, 1 <= ntap <= 8)");
   AB_CHECK_ARG(acclen >= 2 * cut, "ab_stream_create: acclen must be >= 2*cut");
@@ -112,6 +115,7 @@ extern "C" int ab_stream_create(ab_ctx* ctx, int64_t nant, int64_t nchan_raw, co
   st->O = (int)osamp;
   st->ntap = (int)ntap;
   st->nchan_raw = nchan_raw;
+  st->bits = (int)bits;
   st->nsel = nsel;
   st->acclen = acclen;
   st->cut = cut;
@@ -141,7 +145,7 @@ extern "C" int ab_stream_create(ab_ctx* ctx, int64_t nant, int64_t nchan_raw, co
   }
   const int64_t L = (int64_t)P * osamp;
   const int M = st->M;
-  st->fused = osamp >= 4;
+  st->fused = osamp >= 4 && ntap == 4;
   // largest number of fine blocks one push produces (the last push also
   // produces the zero-padded tail of the planned jobs)
   {
@@ -284,8 +288,9 @@ static int stream_push(ab_stream* st, const uint8_t* raw, int64_t ant_stride, co
   AB_CHECK_ARG(!st->fused || nb_all <= st->nb_max, "ab_stream_push: %lld blocks exceed the buffer", (long long)nb_all);
   AB_CHECK_ARG(row0_all >= -4 * (int64_t)O || chunk == 0 || !st->fused, "ab_stream_push: block bookkeeping error");
   // 1. row stage
-  Packed4Src src{raw, ant_stride, 2 * st->nchan_raw, spec_map, map_stride, chunk * acclen - 2 * cut,
-                 st->d_cols, st->d_abs, (int)st->nsel};
+  Packed4Src src{raw,       ant_stride, st->bits == 4 ? 2 * st->nchan_raw : st->nchan_raw / 2,
+                 spec_map,  map_stride, chunk * acclen - 2 * cut,
+                 st->d_cols, st->d_abs, (int)st->nsel, st->bits};
   {
     StageTimer t(st, s, 0);
     AB_TRY(launch_row_stage_packed4(st->ctx, src, st->nant, (int)nslice, P, st->planP, st->twP, cur, nslice, s));

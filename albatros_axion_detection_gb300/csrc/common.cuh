@@ -69,6 +69,7 @@ struct ab_ctx {
   // twiddle tables exp(-2 pi i e / T), e in [0, T), keyed by T
   std::map<int64_t, float2*> twiddles;
   std::map<std::vector<int>, float2*> streams;
+  std::map<std::vector<int>, int2*> pair_tables;
   // grow-only scratch buffers keyed by slot
   std::map<int, std::pair<void*, size_t>> scratch;
   float2* tw64 = nullptr;  // exp(-2 pi i e / 64)
@@ -81,6 +82,12 @@ int get_twiddles(ab_ctx* ctx, int64_t T, const float2** out);
 // Device twiddle stream of a plan (radices applied in order), cached in ctx:
 // stream_q[(k-1) S_q + j] = exp(-2 pi i j k / (R_q S_q)), q = 0..npass-1.
 int get_twiddle_stream(ab_ctx* ctx, int n, const std::vector<int>& radices, const float2** out);
+// Factorise n with the given radix order (for plans whose order matters).
+bool make_plan_from(int n, const std::vector<int>& radices, FftPlan* p);
+// Device table of the real-FFT untangle pairs of a plan of M points: for
+// k in [0, M/2], (pidx(pos(k)), pidx(pos(M-k))) where pos is the storage
+// position after the forward DIF and pidx the padded shared-memory index.
+int get_pair_table(ab_ctx* ctx, const FftPlan& p, const int2** out);
 // Grow-only device scratch; the pointer stays valid until a larger request
 // for the same slot.
 int get_scratch(ab_ctx* ctx, int slot, size_t bytes, void** out);

@@ -147,9 +147,18 @@ __global__ void __launch_bounds__(kRowFftsPerCta* kRowThreadsPerFft)
   if (rawrow >= 0) {
     const uint8_t* row = src.raw + (int64_t)a * src.ant_stride + rawrow * src.row_bytes;
     for (int k = ltid; k < src.nsel; k += kRowThreadsPerFft) {
-      uchar2 b = *reinterpret_cast<const uchar2*>(row + 2 * __ldg(&src.chan_cols[k]));
-      float2 A = make_float2(dec4f(b.x >> 4), dec4f(b.x & 15u));
-      float2 B = make_float2(dec4f(b.y >> 4), dec4f(b.y & 15u));
+      const int c = __ldg(&src.chan_cols[k]);
+      float2 A, B;
+      if (src.bits == 4) {
+        uchar2 b = *reinterpret_cast<const uchar2*>(row + 2 * c);
+        A = make_float2(dec4f(b.x >> 4), dec4f(b.x & 15u));
+        B = make_float2(dec4f(b.y >> 4), dec4f(b.y & 15u));
+      } else {
+        // 1-bit (unpacking.c:207-246): a set bit is +1, a clear bit -1
+        const unsigned v = (row[c >> 1] >> ((c & 1) ? 0 : 4)) & 15u;  // r0 i0 r1 i1
+        A = make_float2((float)(((v >> 3) & 1u) * 2) - 1.f, (float)(((v >> 2) & 1u) * 2) - 1.f);
+        B = make_float2((float)(((v >> 1) & 1u) * 2) - 1.f, (float)((v & 1u) * 2) - 1.f);
+      }
       put_pair_t<PL>(buf, plan, P, __ldg(&src.chan_abs[k]), A, B);
     }
   }
@@ -230,113 +239,104 @@ constexpr int kTimeThreads = 1024;
 // G = O/2 lanes owns one block: lane m of the group folds rows 2m, 2m+1 of
 // the block (z_m = y[2m] + i y[2m+1]), the group takes a G-point complex DFT
 // by shuffles (decimation in frequency, output in bit-reversed lane order),
-// and untangles the real-input spectrum W_k, k = 0..O/2.
-template <int G>
+// and untangles the real-input spectrum W_k, k = 0..O/2.  NTAP is the number
+// of PFB taps (compile time).
+template <int G, int NTAP>
 __device__ __forceinline__ void fold_blocks(const float2* buf, const float* stail, const FoldArgs& fa, int P, int n,
                                             int in, const float2* __restrict__ tw64) {
   constexpr int O = 2 * G;
   constexpr int LOG = G == 1 ? 0 : G == 2 ? 1 : G == 4 ? 2 : G == 8 ? 3 : G == 16 ? 4 : 5;
   constexpr int GW = O < 8 ? O : 8;
-  constexpr int NG = O / GW;
   constexpr int BPW = 32 / G;  // blocks per warp
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   const int m = lane % G, grp = lane / G;
-  const int gbase = grp * G;
   // window taps of rows 2m, 2m+1 for this sample phase
-  float w0[8], w1[8];
+  float w0[NTAP], w1[NTAP];
 #pragma unroll
-  for (int i = 0; i < 8; i++) {
-    w0[i] = i < fa.ntap ? __ldg(&fa.win[(int64_t)(i * O + 2 * m) * P + n]) : 0.f;
-    w1[i] = i < fa.ntap ? __ldg(&fa.win[(int64_t)(i * O + 2 * m + 1) * P + n]) : 0.f;
+  for (int i = 0; i < NTAP; i++) {
+    w0[i] = __ldg(&fa.win[(int64_t)(i * O + 2 * m) * P + n]);
+    w1[i] = __ldg(&fa.win[(int64_t)(i * O + 2 * m + 1) * P + n]);
   }
-  // per-stage DIF twiddles exp(-2 pi i (m mod h) / (2h)) and untangle twiddle
+  // per-stage DIF twiddles exp(-2 pi i (m mod h) / (2h)) and lane roles
   float2 stw[LOG > 0 ? LOG : 1];
+  bool upper[LOG > 0 ? LOG : 1];
 #pragma unroll
   for (int st = 0; st < LOG; st++) {
-    int h = G >> (st + 1);
-    stw[st] = tw64[(m % h) * (32 / h)];  // exp(-2 pi i (m mod h)/(2h)) = w64^((m mod h) * 64/(2h))
+    const int h = G >> (st + 1);
+    stw[st] = tw64[(m % h) * (32 / h)];
+    upper[st] = (m & h) != 0;
   }
-  // bit-reversed frequency held by this lane after the DFT
-  int k = 0;
+  // bit-reversed frequency held by this lane after the DFT, and its partner
+  int k = 0, src_lane = 0;
 #pragma unroll
   for (int bit = 0; bit < LOG; bit++) k |= ((m >> bit) & 1) << (LOG - 1 - bit);
-  const int kc = (G - k) % G;  // partner frequency G - k
-  int src_lane = 0;
+  const int kc = (G - k) % G;
 #pragma unroll
   for (int bit = 0; bit < LOG; bit++) src_lane |= ((kc >> bit) & 1) << (LOG - 1 - bit);
-  src_lane += gbase;
+  src_lane += grp * G;
   const float2 wk = tw64[(k * (64 / O)) & 63];  // exp(-2 pi i k / O)
-  const int p = 2 * k;                        // packed float position (k >= 1), 0 for k = 0
-  const int g = p / GW, e = p % GW;
-  const int64_t nbw = (fa.nb + BPW - 1) / BPW;
+  const bool kzero = (k == 0);
+  const int pk = 2 * k;                       // packed float position ((W_0, W_{O/2}) for k = 0)
+  // W[in][b][g][n][GW] with g = pk / GW, e = pk % GW
+  float* const wbase = fa.W + (int64_t)in * fa.nb * ((int64_t)O * P) + ((int64_t)(pk / GW) * P + n) * GW + (pk % GW);
+  const int64_t bstride = (int64_t)O * P;
+  const int nb = (int)fa.nb, row0 = (int)fa.row0, cut = fa.cut, acclen = fa.acclen;
+  const int nbw = (nb + BPW - 1) / BPW;
   const float* fbuf = reinterpret_cast<const float*>(buf);
   // rows of a block start at an even IPFB row when cut + row0 is even: then
   // each lane's pair (2m, 2m+1) is one float2 slot of the column buffer
-  const bool even = ((fa.cut + fa.row0) & 1) == 0;
-  const int ntap = fa.ntap;
-  const int cut = fa.cut, acclen = fa.acclen;
-  for (int64_t wb = warp; wb < nbw; wb += nwarps) {
-    const int64_t b = wb * BPW + grp;
-    const bool valid = b < fa.nb;
+  const bool even = ((cut + row0) & 1) == 0;
+  for (int wb = warp; wb < nbw; wb += nwarps) {
+    const int b = wb * BPW + grp;
+    const bool valid = b < nb;
+    const int rfirst = row0 + b * O;
     float2 z = make_float2(0.f, 0.f);
     if (valid) {
-      // first row of this lane's pair (int32: rows of one chunk)
-      const int rb = (int)(fa.row0 + b * O) + 2 * m;
-      const int rfirst = (int)(fa.row0 + b * O), rlast = rfirst + ntap * O;  // block's row span
-      if (even && rfirst >= 0 && rlast <= acclen) {
-        // all rows inside this chunk: one float2 slot per tap
-        const int s0 = (cut + rb) >> 1;
+      if (even && rfirst >= 0 && rfirst + NTAP * O <= acclen) {
+        const int s0 = ((cut + rfirst) >> 1) + m;  // slot of rows (2m, 2m+1)
+        const int ps0 = pidx(s0);
 #pragma unroll
-        for (int i = 0; i < 8; i++) {
-          if (i < ntap) {
-            float2 v = buf[pidx(s0 + i * (O / 2))];
-            z.x = fmaf(v.x, w0[i], z.x);
-            z.y = fmaf(v.y, w1[i], z.y);
-          }
+        for (int i = 0; i < NTAP; i++) {
+          const float2 v = buf[(G % 16 == 0) ? ps0 + i * (G + G / 16) : pidx(s0 + i * G)];
+          z.x = fmaf(v.x, w0[i], z.x);
+          z.y = fmaf(v.y, w1[i], z.y);
         }
       } else {
         auto get = [&](int rr) -> float {
           if (rr < 0) return stail[rr + 4 * O];
           if (rr >= acclen) return 0.f;
-          int t = cut + rr;
+          const int t = cut + rr;
           return fbuf[2 * pidx(t >> 1) + (t & 1)];
         };
+        const int rb = rfirst + 2 * m;
 #pragma unroll
-        for (int i = 0; i < 8; i++) {
-          if (i < ntap) {
-            z.x = fmaf(get(rb + i * O), w0[i], z.x);
-            z.y = fmaf(get(rb + i * O + 1), w1[i], z.y);
-          }
+        for (int i = 0; i < NTAP; i++) {
+          z.x = fmaf(get(rb + i * O), w0[i], z.x);
+          z.y = fmaf(get(rb + i * O + 1), w1[i], z.y);
         }
       }
     }
-    // G-point DIF across the group
+    // G-point DIF across the group (branch-free)
 #pragma unroll
     for (int st = 0; st < LOG; st++) {
       const int h = G >> (st + 1);
       float2 v;
       v.x = __shfl_xor_sync(0xffffffffu, z.x, h);
       v.y = __shfl_xor_sync(0xffffffffu, z.y, h);
-      if (m & h) z = cmul(csub(v, z), stw[st]);
-      else z = cadd(z, v);
+      const float2 lo = cadd(z, v), hi = cmul(csub(v, z), stw[st]);
+      z = upper[st] ? hi : lo;
     }
     // untangle: W_k = (Z_k + conj Z_{G-k})/2 + w^k (Z_k - conj Z_{G-k})/(2i)
     float2 zc;
     zc.x = __shfl_sync(0xffffffffu, z.x, src_lane);
     zc.y = __shfl_sync(0xffffffffu, z.y, src_lane);
-    if (!valid) continue;
-    float2 outv;
-    if (k == 0) {
-      outv = make_float2(z.x + z.y, z.x - z.y);  // (W_0, W_{O/2})
-    } else {
-      float2 c = cconj(zc);
-      float2 E = cscale(cadd(z, c), 0.5f);
-      float2 D = csub(z, c);  // 2 i O_k
-      float2 Od = make_float2(0.5f * D.y, -0.5f * D.x);
-      outv = cadd(E, cmul(wk, Od));
-    }
-    float* dst = fa.W + ((((int64_t)in * fa.nb + b) * NG + g) * P + n) * GW + e;
-    *reinterpret_cast<float2*>(dst) = outv;
+    const float2 c = cconj(zc);
+    const float2 E = cscale(cadd(z, c), 0.5f);
+    const float2 D = csub(z, c);  // 2 i O_k
+    const float2 Od = make_float2(0.5f * D.y, -0.5f * D.x);
+    float2 outv = cadd(E, cmul(wk, Od));
+    if (kzero) outv = make_float2(z.x + z.y, z.x - z.y);  // (W_0, W_{O/2})
+    if (valid) *reinterpret_cast<float2*>(wbase + (int64_t)b * bstride) = outv;
   }
 }
 
@@ -344,12 +344,14 @@ __host__ __device__ inline size_t time_smem_bytes(int N) {
   return sizeof(float2) * ((size_t)padded_len(N / 2) + smem_tw_len(N));
 }
 
-template <class PL, bool TABLE, int NTHR, int FOLDG = 0>
+// NTAP: number of window taps of the on-the-fly filter and of the fused PFB
+// fold (compile time); 0 = runtime `ntap` (filter only, no fold).
+template <class PL, bool TABLE, int NTHR, int FOLDG = 0, int NTAP = 0>
 __global__ void __launch_bounds__(NTHR)
     time_stage_kernel(float* __restrict__ data, int64_t ld, int P, int N, FftPlan plan,
                       const float2* __restrict__ twN, const float2* __restrict__ tws,
                       const float2* __restrict__ table, const float* __restrict__ wtaps, int ntap, float thresh,
-                      FoldArgs fa, const float2* __restrict__ tw64) {
+                      FoldArgs fa, const float2* __restrict__ tw64, const int2* __restrict__ pairs) {
   extern __shared__ float2 buf[];
   const int n = blockIdx.x, input = blockIdx.y;
   const int M = N / 2;
@@ -377,15 +379,24 @@ __global__ void __launch_bounds__(NTHR)
       h = __ldg(&table[(int64_t)n * (M + 1) + k]);
     } else {
       float2 m = make_float2(0.f, 0.f);
+      if constexpr (NTAP > 0) {
+        m.x = w[NTAP - 1];
 #pragma unroll
-      for (int t = 7; t >= 0; t--) {
-        if (t < ntap) {
+        for (int t = NTAP - 2; t >= 0; t--) {
           m = cmul(m, z);
           m.x += w[t];
         }
+      } else {
+#pragma unroll
+        for (int t = 7; t >= 0; t--) {
+          if (t < ntap) {
+            m = cmul(m, z);
+            m.x += w[t];
+          }
+        }
       }
       float a2 = fmaf(m.x, m.x, m.y * m.y);
-      float g = thresh > 0.f ? (1.f + t2) / (t2 + a2) : 1.f / a2;
+      float g = thresh > 0.f ? __fdividef(1.f + t2, t2 + a2) : __fdividef(1.f, a2);
       h = make_float2(m.x * g, m.y * g);
     }
     return cscale(h, scale);
@@ -400,7 +411,8 @@ __global__ void __launch_bounds__(NTHR)
       buf[0] = make_float2(y0 + ym, y0 - ym);  // real parts only (irfft)
       continue;
     }
-    int pk = pidx(fpos<PL>(plan, k)), pc = pidx(fpos<PL>(plan, M - k));
+    const int2 pp = __ldg(&pairs[k]);
+    const int pk = pp.x, pc = pp.y;
     float2 zk = buf[pk], zc = buf[pc];
     float2 w1 = tw(k);                           // exp(-2 pi i k / N)
     const float2 w1c = make_float2(-w1.x, w1.y);  // exp(-2 pi i (M-k) / N) = -conj(w1)
@@ -431,7 +443,7 @@ __global__ void __launch_bounds__(NTHR)
     float* st = fa.state + ((int64_t)input * P + n) * (4 * O);
     for (int i = tid; i < 4 * O; i += NTHR) stail[i] = st[i];
     __syncthreads();
-    fold_blocks<FOLDG>(buf, stail, fa, P, n, input, tw64);
+    fold_blocks<FOLDG, NTAP>(buf, stail, fa, P, n, input, tw64);
     __syncthreads();
     const float* fbuf = reinterpret_cast<const float*>(buf);
     for (int i = tid; i < 4 * O; i += NTHR) {
@@ -497,17 +509,17 @@ int launch_row_stage_c64(ab_ctx* ctx, const float2* dat, int64_t nslice, int P, 
 
 template <class PL, int NTHR>
 static int launch_time_t(ab_ctx* ctx, float* buf, int64_t ld, int ninputs, int P, int N, const FftPlan& planM,
-                         const float2* twN, const float2* tws, const float2* table, const float* wtaps, int ntap,
-                         float thresh, size_t smem, cudaStream_t s) {
+                         const float2* twN, const float2* tws, const int2* pairs, const float2* table,
+                         const float* wtaps, int ntap, float thresh, size_t smem, cudaStream_t s) {
   dim3 grid((unsigned)P, (unsigned)ninputs);
   if (table) {
     AB_TRY(set_smem_attr(time_stage_kernel<PL, true, NTHR>, smem));
     time_stage_kernel<PL, true, NTHR><<<grid, NTHR, smem, s>>>(buf, ld, P, N, planM, twN, tws, table, wtaps, ntap,
-                                                              thresh, FoldArgs{}, nullptr);
+                                                              thresh, FoldArgs{}, nullptr, pairs);
   } else {
     AB_TRY(set_smem_attr(time_stage_kernel<PL, false, NTHR>, smem));
     time_stage_kernel<PL, false, NTHR><<<grid, NTHR, smem, s>>>(buf, ld, P, N, planM, twN, tws, table, wtaps, ntap,
-                                                               thresh, FoldArgs{}, nullptr);
+                                                               thresh, FoldArgs{}, nullptr, pairs);
   }
   AB_LAUNCH_CHECK();
   return AB_OK;
@@ -522,46 +534,57 @@ int launch_time_stage(ab_ctx* ctx, float* buf, int64_t ld, int ninputs, int P, i
   AB_CHECK_ARG(table || (wtaps && ntap >= 1 && ntap <= 8), "time stage: need a filter table or 1..8 window taps");
   const int M = N / 2;
   const float2* tws = nullptr;
+  const int2* pairs = nullptr;
+  FftPlan sp;
   if (M == Plan16464::N) {
     AB_TRY(get_twiddle_stream(ctx, M, {7, 7, 7, 3, 16}, &tws));
-    return launch_time_t<Plan16464, 1024>(ctx, buf, ld, ninputs, P, N, planM, twN, tws, table, wtaps, ntap, thresh,
-                                         smem, s);
+    make_plan_from(M, {7, 7, 7, 3, 16}, &sp);
+    AB_TRY(get_pair_table(ctx, sp, &pairs));
+    return launch_time_t<Plan16464, 1024>(ctx, buf, ld, ninputs, P, N, planM, twN, tws, pairs, table, wtaps, ntap,
+                                         thresh, smem, s);
   }
   if (M == Plan16384::N) {
     AB_TRY(get_twiddle_stream(ctx, M, {4, 16, 16, 16}, &tws));
-    return launch_time_t<Plan16384, 1024>(ctx, buf, ld, ninputs, P, N, planM, twN, tws, table, wtaps, ntap, thresh,
-                                         smem, s);
+    make_plan_from(M, {4, 16, 16, 16}, &sp);
+    AB_TRY(get_pair_table(ctx, sp, &pairs));
+    return launch_time_t<Plan16384, 1024>(ctx, buf, ld, ninputs, P, N, planM, twN, tws, pairs, table, wtaps, ntap,
+                                         thresh, smem, s);
   }
-  return launch_time_t<NoPlan, kTimeThreads>(ctx, buf, ld, ninputs, P, N, planM, twN, nullptr, table, wtaps, ntap,
-                                             thresh, smem, s);
+  AB_TRY(get_pair_table(ctx, planM, &pairs));
+  return launch_time_t<NoPlan, kTimeThreads>(ctx, buf, ld, ninputs, P, N, planM, twN, nullptr, pairs, table, wtaps,
+                                             ntap, thresh, smem, s);
 }
 
 template <class PL, int NTHR, int G>
 static int launch_fold_t(float* buf, int64_t ld, int ninputs, int P, int N, const FftPlan& planM, const float2* twN,
-                         const float2* tws, const float* wtaps, int ntap, float thresh, const FoldArgs& fa,
-                         const float2* tw64, size_t smem, cudaStream_t s) {
+                         const float2* tws, const int2* pairs, const float* wtaps, int ntap, float thresh,
+                         const FoldArgs& fa, const float2* tw64, size_t smem, cudaStream_t s) {
   dim3 grid((unsigned)P, (unsigned)ninputs);
-  AB_TRY(set_smem_attr(time_stage_kernel<PL, false, NTHR, G>, smem));
-  time_stage_kernel<PL, false, NTHR, G><<<grid, NTHR, smem, s>>>(buf, ld, P, N, planM, twN, tws, nullptr, wtaps,
-                                                                 ntap, thresh, fa, tw64);
+  AB_TRY(set_smem_attr(time_stage_kernel<PL, false, NTHR, G, 4>, smem));
+  time_stage_kernel<PL, false, NTHR, G, 4><<<grid, NTHR, smem, s>>>(buf, ld, P, N, planM, twN, tws, nullptr, wtaps,
+                                                                    ntap, thresh, fa, tw64, pairs);
   AB_LAUNCH_CHECK();
   return AB_OK;
 }
 
 template <class PL, int NTHR>
 static int launch_fold_o(float* buf, int64_t ld, int ninputs, int P, int N, const FftPlan& planM, const float2* twN,
-                         const float2* tws, const float* wtaps, int ntap, float thresh, const FoldArgs& fa,
-                         const float2* tw64, size_t smem, cudaStream_t s) {
+                         const float2* tws, const int2* pairs, const float* wtaps, int ntap, float thresh,
+                         const FoldArgs& fa, const float2* tw64, size_t smem, cudaStream_t s) {
+#define AB_FOLD_CASE(OO, GG) \
+  case OO:                 \
+    return launch_fold_t<PL, NTHR, GG>(buf, ld, ninputs, P, N, planM, twN, tws, pairs, wtaps, ntap, thresh, fa, tw64, smem, s);
   switch (fa.O) {
-    case 4: return launch_fold_t<PL, NTHR, 2>(buf, ld, ninputs, P, N, planM, twN, tws, wtaps, ntap, thresh, fa, tw64, smem, s);
-    case 8: return launch_fold_t<PL, NTHR, 4>(buf, ld, ninputs, P, N, planM, twN, tws, wtaps, ntap, thresh, fa, tw64, smem, s);
-    case 16: return launch_fold_t<PL, NTHR, 8>(buf, ld, ninputs, P, N, planM, twN, tws, wtaps, ntap, thresh, fa, tw64, smem, s);
-    case 32: return launch_fold_t<PL, NTHR, 16>(buf, ld, ninputs, P, N, planM, twN, tws, wtaps, ntap, thresh, fa, tw64, smem, s);
-    case 64: return launch_fold_t<PL, NTHR, 32>(buf, ld, ninputs, P, N, planM, twN, tws, wtaps, ntap, thresh, fa, tw64, smem, s);
+    AB_FOLD_CASE(4, 2)
+    AB_FOLD_CASE(8, 4)
+    AB_FOLD_CASE(16, 8)
+    AB_FOLD_CASE(32, 16)
+    AB_FOLD_CASE(64, 32)
     default:
       set_error("fused fold: osamp %d not supported (4..64)", fa.O);
       return AB_ERR_UNSUPPORTED;
   }
+#undef AB_FOLD_CASE
 }
 
 int launch_time_fold(ab_ctx* ctx, float* buf, int64_t ld, int ninputs, int P, int N, const FftPlan& planM,
@@ -570,19 +593,28 @@ int launch_time_fold(ab_ctx* ctx, float* buf, int64_t ld, int ninputs, int P, in
   size_t smem = time_smem_bytes(N) + sizeof(float) * 4 * 64;
   AB_CHECK_ARG(smem <= ctx->smem_optin, "time stage: nslice %d needs %zu bytes of shared memory (max %zu)", N, smem,
                ctx->smem_optin);
-  AB_CHECK_ARG(wtaps && ntap >= 1 && ntap <= 8 && fa.ntap >= 1 && fa.ntap <= 8, "fused fold: bad ntap");
+  AB_CHECK_ARG(wtaps && ntap == 4 && fa.ntap == 4, "fused fold: needs ntap = 4");
   const int M = N / 2;
   const float2* tws = nullptr;
+  const int2* pairs = nullptr;
+  FftPlan sp;
   if (M == Plan16464::N) {
     AB_TRY(get_twiddle_stream(ctx, M, {7, 7, 7, 3, 16}, &tws));
-    return launch_fold_o<Plan16464, 1024>(buf, ld, ninputs, P, N, planM, twN, tws, wtaps, ntap, thresh, fa, tw64, smem, s);
+    make_plan_from(M, {7, 7, 7, 3, 16}, &sp);
+    AB_TRY(get_pair_table(ctx, sp, &pairs));
+    return launch_fold_o<Plan16464, 1024>(buf, ld, ninputs, P, N, planM, twN, tws, pairs, wtaps, ntap, thresh, fa,
+                                          tw64, smem, s);
   }
   if (M == Plan16384::N) {
     AB_TRY(get_twiddle_stream(ctx, M, {4, 16, 16, 16}, &tws));
-    return launch_fold_o<Plan16384, 1024>(buf, ld, ninputs, P, N, planM, twN, tws, wtaps, ntap, thresh, fa, tw64, smem, s);
+    make_plan_from(M, {4, 16, 16, 16}, &sp);
+    AB_TRY(get_pair_table(ctx, sp, &pairs));
+    return launch_fold_o<Plan16384, 1024>(buf, ld, ninputs, P, N, planM, twN, tws, pairs, wtaps, ntap, thresh, fa,
+                                          tw64, smem, s);
   }
-  return launch_fold_o<NoPlan, kTimeThreads>(buf, ld, ninputs, P, N, planM, twN, nullptr, wtaps, ntap, thresh, fa,
-                                             tw64, smem, s);
+  AB_TRY(get_pair_table(ctx, planM, &pairs));
+  return launch_fold_o<NoPlan, kTimeThreads>(buf, ld, ninputs, P, N, planM, twN, nullptr, pairs, wtaps, ntap, thresh,
+                                             fa, tw64, smem, s);
 }
 
 }  // namespace ab

@@ -15,13 +15,15 @@ namespace ab {
 struct Packed4Src {
   const uint8_t* raw;        // antenna a at raw + a * ant_stride
   int64_t ant_stride;        // bytes
-  int64_t row_bytes;         // 2 * nchan_raw
+  int64_t row_bytes;         // 2 * nchan_raw (4-bit) or nchan_raw / 2 (1-bit)
   const int32_t* spec_map;   // optional: raw row of global spectrum g (or <0)
   int64_t map_stride;        // per-antenna stride of spec_map
   int64_t g0;                // global spectrum of local row 0 (may be negative)
   const int32_t* chan_cols;  // device (nsel): raw column per selected channel
   const int32_t* chan_abs;   // device (nsel): absolute bin 0..P/2
   int nsel;
+  int bits;                  // 4: one byte per channel per pol; 1: sign bits,
+                             // byte j = channels 2j, 2j+1 (r0 i0 r1 i1 each, MSB first)
 };
 
 // Row stage for packed 4-bit input: local rows t in [0, nrows) of every

@@ -74,8 +74,12 @@ class StreamCorrelator:
     """Device state of one streaming run; push chunks in order, read vis."""
 
     def __init__(self, nant: int, channels, chanstart: int, chanend: int, acclen: int, nchunks: int, nblock: int,
-                 osamp: int, cut: int = 10, filt_thresh: float = 0.45, ntap: int = 4, nchan_raw: Optional[int] = None):
+                 osamp: int, cut: int = 10, filt_thresh: float = 0.45, ntap: int = 4, nchan_raw: Optional[int] = None,
+                 bits: int = 4):
         ch = host_int64(channels)
+        if bits not in (1, 4):
+            raise ValueError("bits must be 1 or 4")
+        self.bits = int(bits)
         self.nant, self.M = int(nant), 2 * int(nant)
         self.nchan_raw = int(nchan_raw if nchan_raw is not None else ch.size)
         self.acclen, self.nchunks, self.nblock = int(acclen), int(nchunks), int(nblock)
@@ -87,7 +91,7 @@ class StreamCorrelator:
         absch = np.ascontiguousarray(ch[chanstart:chanend])
         self._cols, self._abs = cols, absch
         out = ctypes.c_void_p()
-        _lib.call("ab_stream_create", _lib.ctx(), self.nant, self.nchan_raw, cols.ctypes.data, absch.ctypes.data,
+        _lib.call("ab_stream_create", _lib.ctx(), self.nant, self.nchan_raw, self.bits, cols.ctypes.data, absch.ctypes.data,
                   cols.size, self.acclen, self.cut, self.osamp, self.ntap, self.filt_thresh, self.nblock,
                   len(self.jobs), self.q0, self.q1, ctypes.byref(out))
         self._h = out.value
@@ -114,8 +118,9 @@ class StreamCorrelator:
         need = (int(chunk) + 1) * self.acclen
         if spec_map is None and raw.shape[1] < need:
             raise ValueError(f"raw holds {raw.shape[1]} spectra, chunk {chunk} needs {need}")
-        if raw.shape[0] != self.nant or raw.shape[2] != 2 * self.nchan_raw or not raw.is_contiguous():
-            raise ValueError("raw must be contiguous (nant, nspec, 2*nchan_raw)")
+        row_bytes = 2 * self.nchan_raw if self.bits == 4 else self.nchan_raw // 2
+        if raw.shape[0] != self.nant or raw.shape[2] != row_bytes or not raw.is_contiguous():
+            raise ValueError(f"raw must be contiguous (nant, nspec, {row_bytes}) uint8")
         mp, mstride = 0, 0
         if spec_map is not None:
             if spec_map.dtype != torch.int32 or spec_map.shape[0] != self.nant or spec_map.shape[1] < need \
@@ -158,18 +163,20 @@ def _device_view(addr: int, n: int) -> torch.Tensor:
 
 
 def repfb_xcorr_avg(raw, channels, acclen: int, nchunks: int, nblock: int, chanstart: int, chanend: int, osamp: int,
-                    cut: int = 10, filt_thresh: float = 0.45, ntap: int = 4, spec_map=None):
+                    cut: int = 10, filt_thresh: float = 0.45, ntap: int = 4, spec_map=None, bits: int = 4):
     """Streaming unpack -> IPFB -> PFB -> xcorr over device-resident packets.
 
-    raw: (nant, nspec, 2*nchan_raw) uint8 device array; channels: absolute
+    raw: (nant, nspec, 2*nchan_raw) uint8 device array of 4-bit packets, or
+    (nant, nspec, nchan_raw/2) of 1-bit packets with bits=1; channels: absolute
     channel numbers of the raw columns; [chanstart, chanend) selects the
     coarse channels.  Returns (vis, freqs): vis (M, M, nchan, njobs) complex64
     F-ordered (numpy, NaNs masked as the reference does) and the fine
     channel numbers."""
     r = device_array(raw, torch.uint8, "raw")
     ch = host_int64(channels)
+    nchan_raw = r.shape[2] // 2 if bits == 4 else r.shape[2] * 2
     sc = StreamCorrelator(r.shape[0], ch, chanstart, chanend, acclen, nchunks, nblock, osamp, cut, filt_thresh, ntap,
-                          nchan_raw=r.shape[2] // 2)
+                          nchan_raw=nchan_raw, bits=bits)
     try:
         for j in range(nchunks):
             sc.push(r, j, spec_map, final=(j == nchunks - 1))

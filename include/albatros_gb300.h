@@ -183,15 +183,17 @@ int ab_avg_xcorr_1bit_pairs(const uint8_t *data0, const uint8_t *data1, const in
  * The streaming unpack -> IPFB -> PFB(osamp) -> fine xcorr of
  * repfb_xcorr_avg (albatros_analysis/scripts/xcorr/helper_gpu_stream_clean.py:295-456),
  * with the IPFB overlap rows and the ntap-1 PFB overlap blocks kept on the
- * device between chunks.  Inputs are 4-bit packets of nant antennas,
- * 2 pols each (M = 2*nant inputs).
+ * device between chunks.  Inputs are 4-bit or 1-bit packets of nant
+ * antennas, 2 pols each (M = 2*nant inputs).
  *
  * ab_stream_create: acclen new spectra per chunk, nslice = acclen + 2*cut;
+ * bits: 4 (rows of 2*nchan_raw bytes) or 1 (rows of nchan_raw/2 bytes, the
+ * sign-bit format of albatros_analysis/src/correlations/unpacking.c:207-246);
  * chan_cols / chan_abs: HOST int64 arrays (nsel) of raw column index and
  * absolute channel number (0..2048) of the selected coarse channels;
  * fine band [q0, q1) (multiples of osamp); nblock fine rows per job, njobs
  * jobs (from the reference's job planner). Allocates all device state. */
-int ab_stream_create(ab_ctx *ctx, int64_t nant, int64_t nchan_raw, const int64_t *chan_cols,
+int ab_stream_create(ab_ctx *ctx, int64_t nant, int64_t nchan_raw, int64_t bits, const int64_t *chan_cols,
                      const int64_t *chan_abs, int64_t nsel, int64_t acclen, int64_t cut, int64_t osamp,
                      int64_t ntap, double thresh, int64_t nblock, int64_t njobs, int64_t q0, int64_t q1,
                      ab_stream **out);
@@ -202,7 +204,8 @@ int ab_stream_reset(ab_stream *st, void *stream);
  * (nant arrays of ant_stride bytes, rows of 2*nchan_raw bytes); spectrum
  * g (global, 0-based) of antenna a is row spec_map[a*map_stride + g] when
  * spec_map != NULL (negative = missing, zero-filled), else row g. Rows for
- * g in [chunk*acclen - 2*cut, (chunk+1)*acclen) are read. */
+ * g in [chunk*acclen - 2*cut, (chunk+1)*acclen) are read.  Rows are
+ * 2*nchan_raw bytes (4-bit) or nchan_raw/2 bytes (1-bit). */
 int ab_stream_push(ab_stream *st, const uint8_t *raw, int64_t ant_stride, const int32_t *spec_map,
                    int64_t map_stride, int64_t chunk, void *stream);
 /* The last chunk: as ab_stream_push, then every remaining fine block of the

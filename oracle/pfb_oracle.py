@@ -136,6 +136,19 @@ def unpack_1bit_np(raw2d: np.ndarray, rowstart: int, rowend: int, chanstart: int
     return p0, p1
 
 
+def unpack_1bit_channels(raw2d: np.ndarray, rowstart: int, rowend: int, channels):
+    """1-bit decode of arbitrary channel indices: channel c lives in byte c//2,
+    high half-byte for even c, bits (r0, i0, r1, i1) MSB first, set bit = +1
+    (src/correlations/unpacking.c:207-246)."""
+    ch = np.asarray(channels, dtype=np.int64)
+    b = raw2d[rowstart:rowend][:, ch // 2].astype(np.int64)
+    v = np.where((ch % 2) == 0, b >> 4, b) & 15
+    pm = lambda x: 2 * x - 1
+    p0 = pm((v >> 3) & 1) + 1j * pm((v >> 2) & 1)
+    p1 = pm((v >> 1) & 1) + 1j * pm(v & 1)
+    return p0, p1
+
+
 def make_continuous(spec, chan_specnum, start_specnum, channels, nspec, nchans=2049):
     """Place rows at (specnum-start) % nspec and columns at absolute channel
     numbers, zeros elsewhere (src/correlations/baseband_data_classes.py:48-73)."""
@@ -179,11 +192,12 @@ def band_edges(channels, chanstart: int, chanend: int, osamp: int):
 def repfb_xcorr_avg(raw: np.ndarray, channels, acclen: int, nchunks: int, nblock: int,
                     chanstart: int, chanend: int, osamp: int, cut: int = 10,
                     filt_thresh: float = 0.45, ntap: int = 4, spec_present=None,
-                    filt=None):
+                    filt=None, bits: int = 4):
     """Streaming unpack -> IPFB -> PFB -> xcorr, FP64 restatement of
     repfb_xcorr_avg (scripts/xcorr/helper_gpu_stream_clean.py:295-402).
 
-    raw: (nant, nspec, 2*nchan_raw) uint8 4-bit packets, one spectrum per row.
+    raw: (nant, nspec, 2*nchan_raw) uint8 4-bit packets, one spectrum per row
+    (bits=4), or (nant, nspec, nchan_raw/2) 1-bit packets (bits=1).
     channels: absolute channel numbers of the raw columns.
     spec_present: optional (nant, nchunks*acclen) bool; False rows are missing
     (zero-filled, as make_continuous does for absent specnums).
@@ -205,7 +219,10 @@ def repfb_xcorr_avg(raw: np.ndarray, channels, acclen: int, nchunks: int, nblock
         prev = [np.zeros((2 * cut, 2049), np.complex128) for _ in range(npol)]
         for j in range(nchunks):
             rows = np.arange(j * acclen, (j + 1) * acclen)
-            pols = unpack_4bit_np(raw[a], rows[0], rows[-1] + 1, sel)
+            if bits == 4:
+                pols = unpack_4bit_np(raw[a], rows[0], rows[-1] + 1, sel)
+            else:
+                pols = unpack_1bit_channels(raw[a], rows[0], rows[-1] + 1, sel)
             for p in range(npol):
                 spec = pols[p]
                 if spec_present is not None:

@@ -15,6 +15,7 @@ TOL = 1e-5
 def run(raw, channels, **kw):
     from albatros_axion_detection_gb300 import stream
     spec_map = kw.pop("spec_map", None)
+    kw.setdefault("bits", 4)
     vis, freqs = stream.repfb_xcorr_avg(torch.from_numpy(raw).cuda(), channels,
                                         spec_map=None if spec_map is None else torch.from_numpy(spec_map).cuda(), **kw)
     return np.asarray(vis), freqs
@@ -67,6 +68,19 @@ def test_stream_channel_subset_and_gap_in_channel_numbers():
     kw = dict(acclen=512, nchunks=2, nblock=20, chanstart=5, chanend=9, osamp=4, cut=32)
     vis, _ = run(raw, channels, **kw)
     ref, _ = po.repfb_xcorr_avg(raw, channels, **kw)
+    check(vis, ref)
+
+
+@pytest.mark.parametrize("chs,osamp", [((0, 32), 16), ((6, 13), 64)])
+def test_stream_1bit_vs_oracle(chs, osamp):
+    """1-bit sign packets through the chain (the 1-bit files of a mixed batch)."""
+    nant, nchan_raw, acclen, cut, nchunks = 2, 32, 512, 32, 3
+    raw = gen.raw_1bit(seed=osamp, nspec=nant * nchunks * acclen, nchan=nchan_raw).reshape(nant, nchunks * acclen, -1)
+    channels = np.arange(300, 300 + nchan_raw)
+    kw = dict(acclen=acclen, nchunks=nchunks, nblock=6, chanstart=chs[0], chanend=chs[1], osamp=osamp, cut=cut)
+    vis, freqs = run(raw, channels, bits=1, **kw)
+    ref, (q0, q1) = po.repfb_xcorr_avg(raw, channels, bits=1, **kw)
+    assert freqs[0] == q0 and len(freqs) == q1 - q0
     check(vis, ref)
 
 
