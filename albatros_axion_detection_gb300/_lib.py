@@ -23,6 +23,8 @@ SIGNATURES = {
     "ab_last_error": (ctypes.c_char_p, []),
     "ab_ctx_create": (I32, [I32, ctypes.POINTER(P)]),
     "ab_ctx_destroy": (I32, [P]),
+    "ab_ctx_set_fft_plan": (I32, [P, I64, P, I64]),
+    "ab_ctx_set_time_filter": (I32, [P, I32, I32]),
     "ab_unpack_4bit": (I32, [P, P, P, I64, I64, P, I64, I64, P]),
     "ab_unpack_4bit_range": (I32, [P, P, P, I64, I64, I64, I64, I64, P]),
     "ab_unpack_1bit": (I32, [P, P, P, I64, I64, P, I64, I64, P]),
@@ -49,6 +51,9 @@ SIGNATURES = {
     "ab_stream_profile": (I32, [P, I32]),
     "ab_stream_stage_times": (I32, [P, P, P]),
     "ab_stream_kernel_launches": (I64, [P]),
+    "ab_stream_workspace_bytes": (I64, [P]),
+    "ab_stream_fir_taps": (I64, [P]),
+    "ab_stream_set_workspace": (I32, [P, P, I64]),
 }
 
 _lib = None

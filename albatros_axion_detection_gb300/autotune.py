@@ -1,0 +1,274 @@
+"""Autotuner for the chain's time stage: FIR row tile, or FFT radix order.
+
+The IPFB time-axis deconvolution has two forms in the library.  The FIR form
+(the default wherever the reference's Wiener filter decays fast enough) has one
+tunable tile: the kept rows per thread (16 or 32), which sets the rows a CTA
+filters and how many CTAs share an SM.  The FFT form runs one real FFT of
+nslice = acclen + 2*cut points per coarse sample phase (a complex FFT of
+n = nslice/2 points) and its inverse; two lengths have compile-time plans
+(n = 16464 for acclen 2^15, cut 80, and n = 16384), every other length runs
+the runtime mixed-radix plan whose radix order decides how many shared-memory
+passes and twiddle loads it makes.  The reference delegates all of this to
+cuFFT's planner (albatros_analysis/src/utils/pycufft.cu:201-303).  Here each
+candidate (FIR tiles, the FFT's built-in plan, and the orderings of n's
+factorisation over the radices the kernels carry: 8, 4, 2, 7, 5, 3) is timed
+on the streaming chain's own time stage, and the fastest is installed in the
+library context (``ab_ctx_set_time_filter``, ``ab_ctx_set_fft_plan``).
+
+Results are cached per device name and configuration in a JSON file
+(``$ALBATROS_GB300_TUNE_CACHE``, default ``~/.cache/albatros_gb300/autotune.json``).
+"""
+from __future__ import annotations
+
+import ctypes
+import itertools
+import json
+import os
+import threading
+from typing import Dict, Iterable, List, Optional, Sequence, Tuple
+
+import numpy as np
+import torch
+
+from . import _lib
+
+BUILTIN = "builtin"          # the library's own plan (compile-time where one exists)
+STATIC_LENGTHS = (16464, 16384)
+_lock = threading.Lock()
+
+
+def cache_path() -> str:
+    return os.environ.get("ALBATROS_GB300_TUNE_CACHE",
+                          os.path.join(os.path.expanduser("~"), ".cache", "albatros_gb300", "autotune.json"))
+
+
+def _load_cache() -> Dict[str, object]:
+    try:
+        with open(cache_path()) as f:
+            d = json.load(f)
+        return d if isinstance(d, dict) else {}
+    except (OSError, ValueError):
+        return {}
+
+
+def _save_cache(d: Dict[str, object]) -> None:
+    path = cache_path()
+    try:
+        os.makedirs(os.path.dirname(path), exist_ok=True)
+        tmp = path + ".tmp"
+        with open(tmp, "w") as f:
+            json.dump(d, f, indent=1, sort_keys=True)
+        os.replace(tmp, path)
+    except OSError:
+        pass  # a read-only home only loses the cache
+
+
+def factorise(n: int) -> Optional[Dict[int, int]]:
+    """Exponents of 2, 3, 5, 7 in n (None if n has another prime factor)."""
+    e = {}
+    for p in (2, 3, 5, 7):
+        k = 0
+        while n % p == 0:
+            n //= p
+            k += 1
+        e[p] = k
+    return e if n == 1 else None
+
+
+def _pow2_splits(k: int) -> List[Tuple[int, ...]]:
+    """Ways to write 2^k as radices 8/4/2, with at most one 4 and one 2
+    beyond the 8s (more small radices only add passes)."""
+    out = []
+    for n8 in range(k // 3, -1, -1):
+        r = k - 3 * n8
+        for n4 in range(r // 2, -1, -1):
+            n2 = r - 2 * n4
+            if n4 + n2 <= 2:
+                out.append((8,) * n8 + (4,) * n4 + (2,) * n2)
+    return out
+
+
+def candidate_orders(n: int, limit: int = 40) -> List[Tuple[int, ...]]:
+    """Distinct radix orders of n, fewest passes first; at most `limit`."""
+    e = factorise(n)
+    if e is None or n < 2:
+        return []
+    odd = (3,) * e[3] + (5,) * e[5] + (7,) * e[7]
+    seen, cands = set(), []
+    for p2 in _pow2_splits(e[2]):
+        ms = tuple(sorted(p2 + odd, reverse=True))
+        if len(ms) > 12:
+            continue
+        for perm in itertools.permutations(ms):
+            if perm not in seen:
+                seen.add(perm)
+                cands.append(perm)
+    cands.sort(key=lambda r: (len(r), [-x for x in r]))
+    # keep every order with the fewest passes first, then the rest
+    return cands[:limit]
+
+
+def set_plan(n: int, radices: Optional[Sequence[int]], device: Optional[int] = None) -> None:
+    """Install (or clear, with None) the radix order for length n."""
+    c = _lib.ctx(device)
+    if radices is None:
+        _lib.call("ab_ctx_set_fft_plan", c, int(n), None, 0)
+        return
+    arr = (ctypes.c_int32 * len(radices))(*[int(r) for r in radices])
+    _lib.call("ab_ctx_set_fft_plan", c, int(n), ctypes.cast(arr, ctypes.c_void_p), len(radices))
+
+
+DEFAULT_MODE = 2
+_filter_setting = {"mode": DEFAULT_MODE, "row_tile": 32}
+
+
+def set_time_filter(mode: int = DEFAULT_MODE, row_tile: int = 0, device: Optional[int] = None) -> None:
+    """Time stage of streams created from now on: mode 0 = FIR where it is
+    accurate (else FFT), 1 = FFT only, 2 = FFT where it runs (else FIR, the
+    default); row_tile 16/32 (0 keeps it)."""
+    _lib.call("ab_ctx_set_time_filter", _lib.ctx(device), int(mode), int(row_tile))
+    _filter_setting["mode"] = int(mode)
+    if row_tile:
+        _filter_setting["row_tile"] = int(row_tile)
+
+
+def _time_chain(acclen: int, cut: int, osamp: int, nchunks: int = 2, reps: int = 2, mode: int = 0,
+                row_tile: int = 32) -> Tuple[float, int]:
+    """(ms per launch of the chain's time stage for one antenna, FIR J) with
+    the given time-filter setting; the previous setting is restored."""
+    from .stream import StreamCorrelator
+    prev = dict(_filter_setting)
+    set_time_filter(mode, row_tile)
+    try:
+        return _time_chain_now(acclen, cut, osamp, nchunks, reps)
+    finally:
+        set_time_filter(prev["mode"], prev["row_tile"])
+
+
+def _time_chain_now(acclen: int, cut: int, osamp: int, nchunks: int, reps: int) -> Tuple[float, int]:
+    from .stream import StreamCorrelator
+    dev = torch.device("cuda", torch.cuda.current_device())
+    nch = 8
+    g = torch.Generator(device=dev)
+    g.manual_seed(7)
+    raw = torch.randint(0, 256, (1, nchunks * acclen, 2 * nch), generator=g, device=dev, dtype=torch.uint8)
+    channels = np.arange(100, 100 + nch)
+    nblock = max(acclen // osamp, 1)
+    sc = StreamCorrelator(1, channels, 0, nch, acclen, nchunks, nblock, osamp, cut, 0.45, 4, nchan_raw=nch)
+    try:
+        for j in range(nchunks):  # warm-up (tables, attributes)
+            sc.push(raw, j, final=(j == nchunks - 1))
+        best = float("inf")
+        for _ in range(reps):
+            sc.reset()
+            sc.profile(True)
+            for j in range(nchunks):
+                sc.push(raw, j, final=(j == nchunks - 1))
+            ms, nl = sc.stage_times()["time_deconv"]
+            sc.profile(False)
+            best = min(best, ms / max(nl, 1))
+        return best, sc.fir_taps()
+    finally:
+        sc.close()
+
+
+def tune_time_fft(acclen: int, cut: int, osamp: int = 64, *, use_cache: bool = True, limit: int = 24,
+                  verbose: bool = False) -> Tuple[object, float]:
+    """Choose the radix order for the time-axis FFT of nslice = acclen + 2*cut
+    (n = nslice/2 points) and install it.  Returns (choice, ms per launch),
+    choice = BUILTIN or the radix tuple."""
+    _lib.require_cuda()
+    n = (acclen + 2 * cut) // 2
+    key = f"{torch.cuda.get_device_name()}|time_fft|{n}"
+    with _lock:
+        cache = _load_cache() if use_cache else {}
+        hit = cache.get(key)
+    if hit is not None:
+        choice = BUILTIN if hit["radices"] == BUILTIN else tuple(hit["radices"])
+        set_plan(n, None if choice == BUILTIN else choice)
+        return choice, float(hit["ms"])
+    results = []
+    set_plan(n, None)
+    try:
+        results.append((BUILTIN, _time_chain(acclen, cut, osamp, mode=1)[0]))
+    except (ValueError, _lib.AlbatrosError):
+        pass  # no default plan for this length in the FFT kernels' limits
+    for r in candidate_orders(n, limit):
+        set_plan(n, r)
+        try:
+            results.append((r, _time_chain(acclen, cut, osamp, mode=1)[0]))
+        except (ValueError, _lib.AlbatrosError):
+            continue
+        if verbose:
+            print(f"n={n} radices={r}: {results[-1][1]:.3f} ms", flush=True)
+    if not results:
+        set_plan(n, None)
+        raise ValueError(f"no FFT plan of length {n} runs in the time stage")
+    choice, ms = min(results, key=lambda x: x[1])
+    set_plan(n, None if choice == BUILTIN else choice)
+    with _lock:
+        cache = _load_cache()
+        cache[key] = {"radices": BUILTIN if choice == BUILTIN else list(choice), "ms": ms,
+                      "candidates": len(results), "builtin_ms": results[0][1]}
+        if use_cache:
+            _save_cache(cache)
+    return choice, ms
+
+
+def tune_time_stage(acclen: int, cut: int, osamp: int = 64, *, use_cache: bool = True, limit: int = 24,
+                    verbose: bool = False) -> Dict[str, object]:
+    """Choose the time stage for (acclen, cut, osamp): the FIR form with the
+    faster row tile, or the FFT form with its tuned radix order, whichever is
+    faster on this device.  Returns {"mode", "row_tile", "radices", "ms",
+    "fir_J"}; ``apply`` installs it."""
+    _lib.require_cuda()
+    key = f"{torch.cuda.get_device_name()}|time_stage|{acclen}|{cut}|{osamp}"
+    with _lock:
+        hit = (_load_cache() if use_cache else {}).get(key)
+    if hit is not None:
+        apply(hit)
+        return hit
+    cands = []
+    for tile in (32, 16):
+        ms, J = _time_chain(acclen, cut, osamp, mode=0, row_tile=tile)
+        if J == 0:
+            break  # the FIR form does not apply to this filter
+        cands.append({"mode": 0, "row_tile": tile, "radices": None, "ms": ms, "fir_J": J})
+        if verbose:
+            print(f"acclen={acclen} cut={cut} osamp={osamp} FIR J={J} tile={tile}: {ms:.3f} ms", flush=True)
+    try:
+        radices, ms = tune_time_fft(acclen, cut, osamp, use_cache=use_cache, limit=limit if not cands else 0,
+                                    verbose=verbose)
+        cands.append({"mode": 1, "row_tile": _filter_setting["row_tile"],
+                      "radices": radices if radices == BUILTIN else list(radices), "ms": ms, "fir_J": 0})
+    except (ValueError, _lib.AlbatrosError):
+        pass
+    if not cands:
+        raise ValueError(f"no time stage runs for acclen={acclen}, cut={cut}, osamp={osamp}")
+    best = min(cands, key=lambda c: c["ms"])
+    best = dict(best, candidates=[(c["mode"], c["row_tile"], c["ms"]) for c in cands])
+    with _lock:
+        cache = _load_cache()
+        cache[key] = best
+        if use_cache:
+            _save_cache(cache)
+    apply(best)
+    return best
+
+
+def apply(choice: Dict[str, object]) -> None:
+    """Install a ``tune_time_stage`` result for the streams created next."""
+    set_time_filter(int(choice["mode"]), int(choice["row_tile"]))
+    if int(choice["mode"]) == 1 and choice.get("radices") not in (None, BUILTIN):
+        r = tuple(choice["radices"])
+        set_plan(int(np.prod(r)), r)
+
+
+def tune_configs(configs: Iterable[Tuple[int, int, int]], **kw) -> Dict[Tuple[int, int, int], Dict[str, object]]:
+    """tune_time_stage once per distinct (acclen, cut, osamp)."""
+    out = {}
+    for cfg in configs:
+        cfg = tuple(int(x) for x in cfg)
+        if cfg not in out:
+            out[cfg] = tune_time_stage(*cfg, **kw)
+    return out

@@ -52,6 +52,19 @@ bool make_plan_from(int n, const std::vector<int>& radices, FftPlan* p) {
   return prod == n;
 }
 
+bool ctx_plan(ab_ctx* ctx, int n, FftPlan* p, bool* overridden) {
+  if (overridden) *overridden = false;
+  if (ctx) {
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    auto it = ctx->plan_override.find(n);
+    if (it != ctx->plan_override.end()) {
+      if (overridden) *overridden = true;
+      return make_plan_from(n, it->second, p);
+    }
+  }
+  return make_plan(n, p);
+}
+
 static int host_pos(const FftPlan& p, int f) {
   int pos = 0;
   for (int q = 0; q < p.npass; q++) {
@@ -236,12 +249,47 @@ int ab_ctx_create(int device, ab_ctx** out) {
   return AB_OK;
 }
 
+int ab_ctx_set_fft_plan(ab_ctx* ctx, int64_t n, const int32_t* radices, int64_t npass) {
+  AB_CHECK_ARG(ctx, "ab_ctx_set_fft_plan: NULL context");
+  AB_CHECK_ARG(n >= 1 && npass >= 0 && npass <= ab::kMaxPasses, "ab_ctx_set_fft_plan: bad sizes");
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  if (npass == 0) {  // clear
+    ctx->plan_override.erase((int)n);
+    return AB_OK;
+  }
+  AB_CHECK_ARG(radices, "ab_ctx_set_fft_plan: NULL radices");
+  std::vector<int> r;
+  long long prod = 1;
+  for (int64_t q = 0; q < npass; q++) {
+    int R = radices[q];
+    AB_CHECK_ARG(R == 2 || R == 3 || R == 4 || R == 5 || R == 7 || R == 8,
+                 "ab_ctx_set_fft_plan: radix %d not supported (2, 3, 4, 5, 7, 8)", R);
+    r.push_back(R);
+    prod *= R;
+  }
+  AB_CHECK_ARG(prod == n, "ab_ctx_set_fft_plan: radices multiply to %lld, not %lld", prod, (long long)n);
+  ctx->plan_override[(int)n] = r;
+  return AB_OK;
+}
+
+int ab_ctx_set_time_filter(ab_ctx* ctx, int32_t mode, int32_t row_tile) {
+  AB_CHECK_ARG(ctx, "ab_ctx_set_time_filter: NULL context");
+  AB_CHECK_ARG(mode >= 0 && mode <= 2,
+               "ab_ctx_set_time_filter: mode must be 0 (FIR first), 1 (FFT only) or 2 (FFT first)");
+  AB_CHECK_ARG(row_tile == 0 || row_tile == 16 || row_tile == 32, "ab_ctx_set_time_filter: row_tile must be 0, 16 or 32");
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  ctx->time_filter_mode = mode;
+  if (row_tile) ctx->fir_row_tile = row_tile;
+  return AB_OK;
+}
+
 int ab_ctx_destroy(ab_ctx* ctx) {
   if (!ctx) return AB_OK;
   cudaSetDevice(ctx->device);
   for (auto& kv : ctx->twiddles) cudaFree(kv.second);
   for (auto& kv : ctx->streams) cudaFree(kv.second);
   for (auto& kv : ctx->pair_tables) cudaFree(kv.second);
+  for (auto& kv : ctx->fir_taps) cudaFree((void*)kv.second.second);
   for (auto& kv : ctx->scratch)
     if (kv.second.first) cudaFree(kv.second.first);
   delete ctx;

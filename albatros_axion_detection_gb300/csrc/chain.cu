@@ -46,10 +46,14 @@ struct ab_stream {
   float* d_win = nullptr;    // PFB window (ntap * L)
   float* interm[2] = {nullptr, nullptr};
   bool fused = false;        // PFB fold fused into the time stage (osamp >= 4)
-  float* state = nullptr;    // fused: last 4*osamp timestream rows per column
+  float* state = nullptr;    // fused: last 4*osamp timestream rows per column (x2 for the FIR path)
+  int fir_J = 0;             // > 0: time stage as a (2J+1)-tap FIR (fir.cu)
+  int fir_row_tile = 32;     // kept rows per thread of the FIR stage
+  const float* fir_taps = nullptr;
   float* W = nullptr;
   float2* Y = nullptr;
   float2* vis = nullptr;
+  bool owns_scratch = true;  // interm[0], W, Y allocated here (not a shared workspace)
   int64_t nb_max = 0;
   int64_t chunks_done = 0;  // next chunk expected
   int64_t blocks_done = 0;  // fine blocks already correlated
@@ -68,12 +72,25 @@ static void stream_free(ab_stream* st) {
   cudaFree(st->d_abs);
   cudaFree(st->d_wtaps);
   cudaFree(st->d_win);
-  cudaFree(st->interm[0]);
+  if (st->owns_scratch) {
+    cudaFree(st->interm[0]);
+    cudaFree(st->W);
+    cudaFree(st->Y);
+  }
   cudaFree(st->interm[1]);
   cudaFree(st->state);
-  cudaFree(st->W);
-  cudaFree(st->Y);
   cudaFree(st->vis);
+}
+
+// Per-push scratch of a fused stream, as carved from one workspace: the IPFB
+// intermediate, the folded fine blocks W and the band spectra Y (each region
+// 256-byte aligned).  Nothing in it outlives a push.
+static size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+static void workspace_parts(const ab_stream* st, size_t part[3]) {
+  const int64_t L = (int64_t)st->P * st->O;
+  part[0] = align256(sizeof(float) * (size_t)st->M * st->P * st->nslice);
+  part[1] = align256(sizeof(float) * (size_t)st->M * st->nb_max * L);
+  part[2] = align256(sizeof(float2) * (size_t)st->M * st->nb_max * st->nq);
 }
 
 #define AB_ALLOC(ptr, bytes)                                              \
@@ -126,26 +143,52 @@ extern "C" int ab_stream_create(ab_ctx* ctx, int64_t nant, int64_t nchan_raw, in
   st->q1 = q1;
   st->nq = q1 - q0;
   st->thresh = (float)thresh;
-  if (st->nslice % 2 || !make_plan((int)(st->nslice / 2), &st->planM) || !make_plan(P, &st->planP)) {
+  st->fused = osamp >= 4 && ntap == 4;
+  {
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    st->fir_row_tile = ctx->fir_row_tile;
+  }
+  int mode;
+  {
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    mode = ctx->time_filter_mode;
+  }
+  // can the FFT time stage run this nslice?
+  FftPlan pm{};
+  const bool fft_ok = st->nslice % 2 == 0 && ctx_plan(ctx, (int)(st->nslice / 2), &pm) &&
+                      (size_t)(st->nslice / 2) * sizeof(float2) <= ctx->smem_optin;
+  if (st->fused && (mode == 0 || (mode == 2 && !fft_ok)) && st->nslice <= (int64_t)1 << 30) {
+    int rc = get_fir_taps(ctx, P, (int)st->nslice, (int)ntap, (float)thresh, &st->fir_J, &st->fir_taps);
+    if (rc != AB_OK) {
+      delete st;
+      return rc;
+    }
+  }
+  if (!ctx_plan(ctx, P, &st->planP)) {
+    set_error("ab_stream_create: no FFT plan for lblock %d", P);
+    delete st;
+    return AB_ERR_UNSUPPORTED;
+  }
+  if (st->fir_J == 0 && (st->nslice % 2 || !ctx_plan(ctx, (int)(st->nslice / 2), &st->planM))) {
     set_error("ab_stream_create: nslice = acclen + 2*cut = %lld must be even with nslice/2 factoring into 2,3,5,7",
               (long long)st->nslice);
     delete st;
     return AB_ERR_UNSUPPORTED;
   }
-  if ((size_t)(st->nslice / 2) * sizeof(float2) > ctx->smem_optin) {
+  if (st->fir_J == 0 && (size_t)(st->nslice / 2) * sizeof(float2) > ctx->smem_optin) {
     set_error("ab_stream_create: nslice %lld exceeds the shared-memory column limit", (long long)st->nslice);
     delete st;
     return AB_ERR_UNSUPPORTED;
   }
   int rc;
-  if ((rc = get_twiddles(ctx, P, &st->twP)) != AB_OK || (rc = get_twiddles(ctx, st->nslice, &st->twN)) != AB_OK ||
+  if ((rc = get_twiddles(ctx, P, &st->twP)) != AB_OK ||
+      (st->fir_J == 0 && (rc = get_twiddles(ctx, st->nslice, &st->twN)) != AB_OK) ||
       (rc = get_twiddles(ctx, (int64_t)P * osamp, &st->twL)) != AB_OK) {
     delete st;
     return rc;
   }
   const int64_t L = (int64_t)P * osamp;
   const int M = st->M;
-  st->fused = osamp >= 4 && ntap == 4;
   // largest number of fine blocks one push produces (the last push also
   // produces the zero-padded tail of the planned jobs)
   {
@@ -167,7 +210,7 @@ extern "C" int ab_stream_create(ab_ctx* ctx, int64_t nant, int64_t nchan_raw, in
   AB_ALLOC(st->d_wtaps, sizeof(float) * ntap * P);
   AB_ALLOC(st->d_win, sizeof(float) * ntap * L);
   for (int i = 0; i < (st->fused ? 1 : 2); i++) AB_ALLOC(st->interm[i], sizeof(float) * (size_t)M * P * st->nslice);
-  if (st->fused) AB_ALLOC(st->state, sizeof(float) * (size_t)M * P * 4 * osamp);
+  if (st->fused) AB_ALLOC(st->state, sizeof(float) * (size_t)2 * M * P * 4 * osamp);
   AB_ALLOC(st->W, sizeof(float) * (size_t)M * st->nb_max * L);
   AB_ALLOC(st->Y, sizeof(float2) * (size_t)M * st->nb_max * st->nq);
   AB_ALLOC(st->vis, sizeof(float2) * (size_t)std::max<int64_t>(njobs, 1) * M * M * st->nq);
@@ -186,7 +229,7 @@ extern "C" int ab_stream_create(ab_ctx* ctx, int64_t nant, int64_t nchan_raw, in
             cudaMemcpy(st->d_wtaps, wf.data(), sizeof(float) * wf.size(), cudaMemcpyHostToDevice) == cudaSuccess &&
             cudaMemcpy(st->d_win, wl.data(), sizeof(float) * wl.size(), cudaMemcpyHostToDevice) == cudaSuccess &&
             cudaMemset(st->vis, 0, sizeof(float2) * (size_t)std::max<int64_t>(njobs, 1) * M * M * st->nq) == cudaSuccess &&
-            (!st->fused || cudaMemset(st->state, 0, sizeof(float) * (size_t)M * P * 4 * osamp) == cudaSuccess);
+            (!st->fused || cudaMemset(st->state, 0, sizeof(float) * (size_t)2 * M * P * 4 * osamp) == cudaSuccess);
   if (!ok) {
     set_error("ab_stream_create: upload failed");
     stream_free(st);
@@ -212,7 +255,7 @@ extern "C" int ab_stream_reset(ab_stream* st, void* stream) {
   AB_CUDA(cudaMemsetAsync(st->vis, 0, sizeof(float2) * (size_t)std::max<int64_t>(st->njobs, 1) * st->M * st->M * st->nq,
                           as_stream(stream)));
   if (st->fused)
-    AB_CUDA(cudaMemsetAsync(st->state, 0, sizeof(float) * (size_t)st->M * st->P * 4 * st->O, as_stream(stream)));
+    AB_CUDA(cudaMemsetAsync(st->state, 0, sizeof(float) * (size_t)2 * st->M * st->P * 4 * st->O, as_stream(stream)));
   return AB_OK;
 }
 
@@ -239,8 +282,43 @@ extern "C" int ab_stream_stage_times(const ab_stream* st, double* ms, int64_t* l
   return AB_OK;
 }
 
+extern "C" int64_t ab_stream_workspace_bytes(const ab_stream* st) {
+  if (!st || !st->fused) return -1;
+  size_t part[3];
+  workspace_parts(st, part);
+  return (int64_t)(part[0] + part[1] + part[2]);
+}
+
+extern "C" int ab_stream_set_workspace(ab_stream* st, void* ws, int64_t bytes) {
+  AB_CHECK_ARG(st, "ab_stream_set_workspace: NULL stream object");
+  if (!st->fused) {
+    set_error("ab_stream_set_workspace: only streams with the fused PFB fold (osamp >= 4, ntap = 4) keep no "
+              "state in their scratch");
+    return AB_ERR_UNSUPPORTED;
+  }
+  AB_CHECK_ARG(ws && ((uintptr_t)ws & 255) == 0, "ab_stream_set_workspace: workspace must be 256-byte aligned");
+  size_t part[3];
+  workspace_parts(st, part);
+  AB_CHECK_ARG(bytes >= (int64_t)(part[0] + part[1] + part[2]),
+               "ab_stream_set_workspace: %lld bytes given, %lld needed", (long long)bytes,
+               (long long)(part[0] + part[1] + part[2]));
+  if (st->owns_scratch) {
+    AB_CUDA(cudaDeviceSynchronize());  // no push of this stream may still use the old buffers
+    cudaFree(st->interm[0]);
+    cudaFree(st->W);
+    cudaFree(st->Y);
+  }
+  char* p = (char*)ws;
+  st->interm[0] = (float*)p;
+  st->W = (float*)(p + part[0]);
+  st->Y = (float2*)(p + part[0] + part[1]);
+  st->owns_scratch = false;
+  return AB_OK;
+}
+
 extern "C" const float* ab_stream_vis(const ab_stream* st) { return st ? (const float*)st->vis : nullptr; }
 extern "C" int64_t ab_stream_kernel_launches(const ab_stream* st) { return st ? st->launches : -1; }
+extern "C" int64_t ab_stream_fir_taps(const ab_stream* st) { return st ? st->fir_J : -1; }
 
 // Stage timing (profiling mode only): events around one stage, synchronised
 // immediately, so this mode serialises the host with the device.
@@ -297,7 +375,16 @@ static int stream_push(ab_stream* st, const uint8_t* raw, int64_t ant_stride, co
     t.done(1);
   }
   // 2. time stage (with the PFB fold fused in when osamp >= 4)
-  if (st->fused) {
+  if (st->fir_J > 0) {
+    StageTimer t(st, s, 1);
+    const size_t half = (size_t)M * P * 4 * O;
+    FirArgs fa_fir{cur, nslice, P, M, (int)nslice, (int)cut, (int)acclen, st->fir_taps, st->fir_J,
+                   st->fir_row_tile, st->state + (chunk & 1) * half, st->state + ((chunk + 1) & 1) * half,
+                   st->ctx->tw64};
+    FoldArgs fa{O, st->ntap, (int)cut, (int)acclen, row0_all, nb_all, st->d_win, st->W, nullptr};
+    AB_TRY(launch_fir_fold(fa_fir, fa, s));
+    t.done(1);
+  } else if (st->fused) {
     StageTimer t(st, s, 1);
     FoldArgs fa{O, st->ntap, (int)cut, (int)acclen, row0_all, nb_all, st->d_win, st->W, st->state};
     AB_TRY(launch_time_fold(st->ctx, cur, nslice, M, P, (int)nslice, st->planM, st->twN, st->d_wtaps, st->ntap,

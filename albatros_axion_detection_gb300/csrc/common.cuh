@@ -70,6 +70,16 @@ struct ab_ctx {
   std::map<int64_t, float2*> twiddles;
   std::map<std::vector<int>, float2*> streams;
   std::map<std::vector<int>, int2*> pair_tables;
+  // FFT plans chosen by the autotuner: length -> radix order (forces the
+  // runtime-plan kernels for that length)
+  std::map<int, std::vector<int>> plan_override;
+  // FIR taps of the time stage keyed by (P, nslice, ntap, thresh bits):
+  // (J, device (P, 2J+1) floats or null when J = 0)
+  std::map<std::vector<int64_t>, std::pair<int, const float*>> fir_taps;
+  // 0: FIR where accurate, else FFT; 1: always FFT; 2: FFT where it runs,
+  // else FIR
+  int time_filter_mode = 2;
+  int fir_row_tile = 32;     // kept rows per thread of the FIR time stage
   // grow-only scratch buffers keyed by slot
   std::map<int, std::pair<void*, size_t>> scratch;
   float2* tw64 = nullptr;  // exp(-2 pi i e / 64)
@@ -82,6 +92,9 @@ int get_twiddles(ab_ctx* ctx, int64_t T, const float2** out);
 // Device twiddle stream of a plan (radices applied in order), cached in ctx:
 // stream_q[(k-1) S_q + j] = exp(-2 pi i j k / (R_q S_q)), q = 0..npass-1.
 int get_twiddle_stream(ab_ctx* ctx, int n, const std::vector<int>& radices, const float2** out);
+// Plan of length n for this context: the tuned override if one is set,
+// else the default factorisation.  *overridden tells whether it was tuned.
+bool ctx_plan(ab_ctx* ctx, int n, FftPlan* p, bool* overridden = nullptr);
 // Factorise n with the given radix order (for plans whose order matters).
 bool make_plan_from(int n, const std::vector<int>& radices, FftPlan* p);
 // Device table of the real-FFT untangle pairs of a plan of M points: for

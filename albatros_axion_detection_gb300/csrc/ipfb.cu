@@ -14,6 +14,7 @@
 #include <type_traits>
 
 #include "fft_static.cuh"
+#include "fold.cuh"
 #include "ipfb.cuh"
 
 namespace ab {
@@ -235,111 +236,6 @@ __global__ void __launch_bounds__(kRowFftsPerCta* kRowThreadsPerFft)
 // multiply by the filter, inverse.  All in shared memory, one CTA per column.
 constexpr int kTimeThreads = 1024;
 
-// Warp-level fold + osamp-point real DFT for the fused epilogue.  A group of
-// G = O/2 lanes owns one block: lane m of the group folds rows 2m, 2m+1 of
-// the block (z_m = y[2m] + i y[2m+1]), the group takes a G-point complex DFT
-// by shuffles (decimation in frequency, output in bit-reversed lane order),
-// and untangles the real-input spectrum W_k, k = 0..O/2.  NTAP is the number
-// of PFB taps (compile time).
-template <int G, int NTAP>
-__device__ __forceinline__ void fold_blocks(const float2* buf, const float* stail, const FoldArgs& fa, int P, int n,
-                                            int in, const float2* __restrict__ tw64) {
-  constexpr int O = 2 * G;
-  constexpr int LOG = G == 1 ? 0 : G == 2 ? 1 : G == 4 ? 2 : G == 8 ? 3 : G == 16 ? 4 : 5;
-  constexpr int GW = O < 8 ? O : 8;
-  constexpr int BPW = 32 / G;  // blocks per warp
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-  const int m = lane % G, grp = lane / G;
-  // window taps of rows 2m, 2m+1 for this sample phase
-  float w0[NTAP], w1[NTAP];
-#pragma unroll
-  for (int i = 0; i < NTAP; i++) {
-    w0[i] = __ldg(&fa.win[(int64_t)(i * O + 2 * m) * P + n]);
-    w1[i] = __ldg(&fa.win[(int64_t)(i * O + 2 * m + 1) * P + n]);
-  }
-  // per-stage DIF twiddles exp(-2 pi i (m mod h) / (2h)) and lane roles
-  float2 stw[LOG > 0 ? LOG : 1];
-  bool upper[LOG > 0 ? LOG : 1];
-#pragma unroll
-  for (int st = 0; st < LOG; st++) {
-    const int h = G >> (st + 1);
-    stw[st] = tw64[(m % h) * (32 / h)];
-    upper[st] = (m & h) != 0;
-  }
-  // bit-reversed frequency held by this lane after the DFT, and its partner
-  int k = 0, src_lane = 0;
-#pragma unroll
-  for (int bit = 0; bit < LOG; bit++) k |= ((m >> bit) & 1) << (LOG - 1 - bit);
-  const int kc = (G - k) % G;
-#pragma unroll
-  for (int bit = 0; bit < LOG; bit++) src_lane |= ((kc >> bit) & 1) << (LOG - 1 - bit);
-  src_lane += grp * G;
-  const float2 wk = tw64[(k * (64 / O)) & 63];  // exp(-2 pi i k / O)
-  const bool kzero = (k == 0);
-  const int pk = 2 * k;                       // packed float position ((W_0, W_{O/2}) for k = 0)
-  // W[in][b][g][n][GW] with g = pk / GW, e = pk % GW
-  float* const wbase = fa.W + (int64_t)in * fa.nb * ((int64_t)O * P) + ((int64_t)(pk / GW) * P + n) * GW + (pk % GW);
-  const int64_t bstride = (int64_t)O * P;
-  const int nb = (int)fa.nb, row0 = (int)fa.row0, cut = fa.cut, acclen = fa.acclen;
-  const int nbw = (nb + BPW - 1) / BPW;
-  const float* fbuf = reinterpret_cast<const float*>(buf);
-  // rows of a block start at an even IPFB row when cut + row0 is even: then
-  // each lane's pair (2m, 2m+1) is one float2 slot of the column buffer
-  const bool even = ((cut + row0) & 1) == 0;
-  for (int wb = warp; wb < nbw; wb += nwarps) {
-    const int b = wb * BPW + grp;
-    const bool valid = b < nb;
-    const int rfirst = row0 + b * O;
-    float2 z = make_float2(0.f, 0.f);
-    if (valid) {
-      if (even && rfirst >= 0 && rfirst + NTAP * O <= acclen) {
-        const int s0 = ((cut + rfirst) >> 1) + m;  // slot of rows (2m, 2m+1)
-        const int ps0 = pidx(s0);
-#pragma unroll
-        for (int i = 0; i < NTAP; i++) {
-          const float2 v = buf[(G % 16 == 0) ? ps0 + i * (G + G / 16) : pidx(s0 + i * G)];
-          z.x = fmaf(v.x, w0[i], z.x);
-          z.y = fmaf(v.y, w1[i], z.y);
-        }
-      } else {
-        auto get = [&](int rr) -> float {
-          if (rr < 0) return stail[rr + 4 * O];
-          if (rr >= acclen) return 0.f;
-          const int t = cut + rr;
-          return fbuf[2 * pidx(t >> 1) + (t & 1)];
-        };
-        const int rb = rfirst + 2 * m;
-#pragma unroll
-        for (int i = 0; i < NTAP; i++) {
-          z.x = fmaf(get(rb + i * O), w0[i], z.x);
-          z.y = fmaf(get(rb + i * O + 1), w1[i], z.y);
-        }
-      }
-    }
-    // G-point DIF across the group (branch-free)
-#pragma unroll
-    for (int st = 0; st < LOG; st++) {
-      const int h = G >> (st + 1);
-      float2 v;
-      v.x = __shfl_xor_sync(0xffffffffu, z.x, h);
-      v.y = __shfl_xor_sync(0xffffffffu, z.y, h);
-      const float2 lo = cadd(z, v), hi = cmul(csub(v, z), stw[st]);
-      z = upper[st] ? hi : lo;
-    }
-    // untangle: W_k = (Z_k + conj Z_{G-k})/2 + w^k (Z_k - conj Z_{G-k})/(2i)
-    float2 zc;
-    zc.x = __shfl_sync(0xffffffffu, z.x, src_lane);
-    zc.y = __shfl_sync(0xffffffffu, z.y, src_lane);
-    const float2 c = cconj(zc);
-    const float2 E = cscale(cadd(z, c), 0.5f);
-    const float2 D = csub(z, c);  // 2 i O_k
-    const float2 Od = make_float2(0.5f * D.y, -0.5f * D.x);
-    float2 outv = cadd(E, cmul(wk, Od));
-    if (kzero) outv = make_float2(z.x + z.y, z.x - z.y);  // (W_0, W_{O/2})
-    if (valid) *reinterpret_cast<float2*>(wbase + (int64_t)b * bstride) = outv;
-  }
-}
-
 __host__ __device__ inline size_t time_smem_bytes(int N) {
   return sizeof(float2) * ((size_t)padded_len(N / 2) + smem_tw_len(N));
 }
@@ -443,7 +339,7 @@ __global__ void __launch_bounds__(NTHR)
     float* st = fa.state + ((int64_t)input * P + n) * (4 * O);
     for (int i = tid; i < 4 * O; i += NTHR) stail[i] = st[i];
     __syncthreads();
-    fold_blocks<FOLDG, NTAP>(buf, stail, fa, P, n, input, tw64);
+    fold_blocks<FOLDG, NTAP, false>(buf, stail, fa, P, n, input, tw64, 0, (int)fa.nb);
     __syncthreads();
     const float* fbuf = reinterpret_cast<const float*>(buf);
     for (int i = tid; i < 4 * O; i += NTHR) {
@@ -471,7 +367,9 @@ int launch_row_stage_packed4(ab_ctx* ctx, const Packed4Src& src, int nant, int n
   size_t smem = row_smem_bytes(P);
   AB_CHECK_ARG(smem <= ctx->smem_optin, "row stage: lblock %d too large", P);
   dim3 grid((unsigned)((nrows + kRowFftsPerCta - 1) / kRowFftsPerCta), (unsigned)nant);
-  if (P == Plan4096::N) {
+  bool tuned = false;
+  { FftPlan tmp; ctx_plan(ctx, P, &tmp, &tuned); }
+  if (P == Plan4096::N && !tuned) {
     const float2* tws;
     AB_TRY(get_twiddle_stream(ctx, P, {16, 16, 16}, &tws));
     AB_TRY(set_smem_attr(row_stage_packed4_kernel<Plan4096>, smem));
@@ -492,7 +390,9 @@ int launch_row_stage_c64(ab_ctx* ctx, const float2* dat, int64_t nslice, int P, 
   AB_CHECK_ARG(smem <= ctx->smem_optin, "row stage: lblock %d too large", P);
   int64_t nfft = (nslice + 1) / 2;
   dim3 grid((unsigned)((nfft + kRowFftsPerCta - 1) / kRowFftsPerCta));
-  if (P == Plan4096::N) {
+  bool tuned = false;
+  { FftPlan tmp; ctx_plan(ctx, P, &tmp, &tuned); }
+  if (P == Plan4096::N && !tuned) {
     const float2* tws;
     AB_TRY(get_twiddle_stream(ctx, P, {16, 16, 16}, &tws));
     AB_TRY(set_smem_attr(row_stage_c64_kernel<Plan4096>, smem));
@@ -536,14 +436,16 @@ int launch_time_stage(ab_ctx* ctx, float* buf, int64_t ld, int ninputs, int P, i
   const float2* tws = nullptr;
   const int2* pairs = nullptr;
   FftPlan sp;
-  if (M == Plan16464::N) {
+  bool tuned = false;
+  { FftPlan tmp; ctx_plan(ctx, M, &tmp, &tuned); }
+  if (M == Plan16464::N && !tuned) {
     AB_TRY(get_twiddle_stream(ctx, M, {7, 7, 7, 3, 16}, &tws));
     make_plan_from(M, {7, 7, 7, 3, 16}, &sp);
     AB_TRY(get_pair_table(ctx, sp, &pairs));
     return launch_time_t<Plan16464, 1024>(ctx, buf, ld, ninputs, P, N, planM, twN, tws, pairs, table, wtaps, ntap,
                                          thresh, smem, s);
   }
-  if (M == Plan16384::N) {
+  if (M == Plan16384::N && !tuned) {
     AB_TRY(get_twiddle_stream(ctx, M, {4, 16, 16, 16}, &tws));
     make_plan_from(M, {4, 16, 16, 16}, &sp);
     AB_TRY(get_pair_table(ctx, sp, &pairs));
@@ -598,14 +500,16 @@ int launch_time_fold(ab_ctx* ctx, float* buf, int64_t ld, int ninputs, int P, in
   const float2* tws = nullptr;
   const int2* pairs = nullptr;
   FftPlan sp;
-  if (M == Plan16464::N) {
+  bool tuned = false;
+  { FftPlan tmp; ctx_plan(ctx, M, &tmp, &tuned); }
+  if (M == Plan16464::N && !tuned) {
     AB_TRY(get_twiddle_stream(ctx, M, {7, 7, 7, 3, 16}, &tws));
     make_plan_from(M, {7, 7, 7, 3, 16}, &sp);
     AB_TRY(get_pair_table(ctx, sp, &pairs));
     return launch_fold_o<Plan16464, 1024>(buf, ld, ninputs, P, N, planM, twN, tws, pairs, wtaps, ntap, thresh, fa,
                                           tw64, smem, s);
   }
-  if (M == Plan16384::N) {
+  if (M == Plan16384::N && !tuned) {
     AB_TRY(get_twiddle_stream(ctx, M, {4, 16, 16, 16}, &tws));
     make_plan_from(M, {4, 16, 16, 16}, &sp);
     AB_TRY(get_pair_table(ctx, sp, &pairs));
@@ -690,11 +594,11 @@ extern "C" int ab_ipfb(ab_ctx* ctx, const float* dat, const float* filt, float* 
   AB_CHECK_ARG(((uintptr_t)out & 7) == 0, "ab_ipfb: out must be 8-byte aligned");
   int P = (int)(2 * (nchan - 1));
   FftPlan planP, planM;
-  if (!make_plan(P, &planP)) {
+  if (!ctx_plan(ctx, P, &planP)) {
     set_error("ab_ipfb: lblock %d does not factor into 2,3,5,7", P);
     return AB_ERR_UNSUPPORTED;
   }
-  if (!make_plan((int)(nslice / 2), &planM)) {
+  if (!ctx_plan(ctx, (int)(nslice / 2), &planM)) {
     set_error("ab_ipfb: nslice/2 = %lld does not factor into 2,3,5,7", (long long)(nslice / 2));
     return AB_ERR_UNSUPPORTED;
   }

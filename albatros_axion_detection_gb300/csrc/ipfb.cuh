@@ -69,6 +69,27 @@ int launch_time_fold(ab_ctx* ctx, float* buf, int64_t ld, int ninputs, int P, in
                      const float2* twN, const float* wtaps, int ntap, float thresh, const FoldArgs& fa,
                      const float2* tw64, cudaStream_t s);
 
+// FIR form of the time stage (fir.cu).  Taps h_n[j], |j| <= J, of the
+// reference's Wiener filter at nslice bins, FP64-derived, (P, 2J+1) float;
+// J = 0 when no supported J keeps the dropped tail below 1e-7 (then the FFT
+// time stage must run).  Cached in ctx per (P, nslice, ntap, thresh).
+int get_fir_taps(ab_ctx* ctx, int P, int N, int ntap, float thresh, int* J, const float** taps);
+
+struct FirArgs {
+  const float* data;      // [n][t] window columns, column stride ld
+  int64_t ld;
+  int P, ninputs, nslice, cut, acclen;
+  const float* taps;
+  int J;                  // 32 or 64
+  int row_tile;           // kept rows per thread: 16 or 32
+  const float* state_in;  // previous chunk's last 4*O rows (ninputs, P, 4*O)
+  float* state_out;       // this chunk's last 4*O rows (the other buffer)
+  const float2* tw64;
+};
+// Time stage by FIR over the kept rows, fused with the PFB fold (fa: O, ntap
+// = 4, row0, nb, win, W; fa.cut/acclen/state unused).
+int launch_fir_fold(const FirArgs& a, const FoldArgs& fa, cudaStream_t s);
+
 // sinc-Hamming window of ntap*lblock samples in double (pfb_utils.py:4-7)
 void sinc_hamming_host(int ntap, int64_t lblock, std::vector<double>& w);
 

@@ -445,7 +445,7 @@ static int pfb_common(ab_ctx* ctx, const float* ts, int64_t nsamp, const float* 
     AB_CHECK_ARG(u1 <= P / 2 || (u1 == P / 2 + 1 && O == 1), "ab_pfb_band: band beyond Nyquist");
   }
   FftPlan planP;
-  if (!make_plan(P, &planP)) return AB_ERR_UNSUPPORTED;
+  if (!ctx_plan(ctx, P, &planP)) return AB_ERR_UNSUPPORTED;
   const float2* twL;
   AB_TRY(get_twiddles(ctx, L, &twL));
   void* Wv = nullptr;

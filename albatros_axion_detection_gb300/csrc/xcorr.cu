@@ -103,11 +103,75 @@ __global__ void xcorr_accum_kernel(const float2* __restrict__ Y, int M, int64_t 
   }
 }
 
+// Small-M form: a CTA owns kXaF frequencies; its kXaG thread groups take
+// blocks b_lo + g, b_lo + g + kXaG, ... and keep all M(M+1)/2 pair sums of
+// their frequency in registers (each Y element is read once), then the groups
+// are summed through shared memory in a fixed order (deterministic).
+constexpr int kXaF = 32, kXaG = 8;
+
+template <int M>
+__global__ void __launch_bounds__(kXaF * kXaG)
+    xcorr_accum_small_kernel(const float2* __restrict__ Y, int64_t nb, int64_t F, int64_t b_lo, int64_t b_hi,
+                             float2* __restrict__ vis, float scale) {
+  constexpr int NP = M * (M + 1) / 2;
+  __shared__ float2 part[kXaG][NP][kXaF];
+  const int fl = threadIdx.x % kXaF, g = threadIdx.x / kXaF;
+  const int64_t f = (int64_t)blockIdx.x * kXaF + fl;
+  float2 acc[NP];
+#pragma unroll
+  for (int p = 0; p < NP; p++) acc[p] = make_float2(0.f, 0.f);
+  if (f < F) {
+    for (int64_t b = b_lo + g; b < b_hi; b += kXaG) {
+      float2 y[M];
+#pragma unroll
+      for (int i = 0; i < M; i++) y[i] = __ldg(&Y[((int64_t)i * nb + b) * F + f]);
+      int p = 0;
+#pragma unroll
+      for (int i = 0; i < M; i++) {
+#pragma unroll
+        for (int j = i; j < M; j++, p++) {  // y_i conj(y_j)
+          acc[p].x = fmaf(y[i].x, y[j].x, fmaf(y[i].y, y[j].y, acc[p].x));
+          acc[p].y = fmaf(y[i].y, y[j].x, fmaf(-y[i].x, y[j].y, acc[p].y));
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int p = 0; p < NP; p++) part[g][p][fl] = acc[p];
+  __syncthreads();
+  if (f >= F) return;
+  for (int p = g; p < NP; p += kXaG) {
+    float2 t = part[0][p][fl];
+    for (int q = 1; q < kXaG; q++) t = cadd(t, part[q][p][fl]);
+    t = cscale(t, scale);
+    int i = 0, r = p;
+    while (r >= M - i) {
+      r -= M - i;
+      i++;
+    }
+    const int j = i + r;
+    float2* v = vis + ((int64_t)i * M + j) * F + f;
+    *v = cadd(*v, t);
+    if (i != j) {
+      float2* w = vis + ((int64_t)j * M + i) * F + f;
+      *w = cadd(*w, cconj(t));
+    }
+  }
+}
+
 int launch_xcorr_accum(const float2* Y, int M, int64_t nb, int64_t F, int64_t b_lo, int64_t b_hi, float2* vis,
                        float scale, cudaStream_t s) {
   if (b_hi <= b_lo) return AB_OK;
-  dim3 grid((unsigned)((F + 127) / 128), (unsigned)(M * (M + 1) / 2));
-  xcorr_accum_kernel<<<grid, 128, 0, s>>>(Y, M, nb, F, b_lo, b_hi, vis, scale);
+  const dim3 gs((unsigned)((F + kXaF - 1) / kXaF));
+  switch (M) {
+    case 2: xcorr_accum_small_kernel<2><<<gs, kXaF * kXaG, 0, s>>>(Y, nb, F, b_lo, b_hi, vis, scale); break;
+    case 4: xcorr_accum_small_kernel<4><<<gs, kXaF * kXaG, 0, s>>>(Y, nb, F, b_lo, b_hi, vis, scale); break;
+    case 6: xcorr_accum_small_kernel<6><<<gs, kXaF * kXaG, 0, s>>>(Y, nb, F, b_lo, b_hi, vis, scale); break;
+    default: {
+      dim3 grid((unsigned)((F + 127) / 128), (unsigned)(M * (M + 1) / 2));
+      xcorr_accum_kernel<<<grid, 128, 0, s>>>(Y, M, nb, F, b_lo, b_hi, vis, scale);
+    }
+  }
   AB_LAUNCH_CHECK();
   return AB_OK;
 }

@@ -138,6 +138,24 @@ class StreamCorrelator:
         t = _device_view(addr, n)
         return t.view(max(len(self.jobs), 1), self.M, self.M, self.nq)[: len(self.jobs)]
 
+    def fir_taps(self) -> int:
+        """Half-length J of the FIR time stage (0: the FFT time stage runs)."""
+        return int(_lib.load().ab_stream_fir_taps(self._h))
+
+    def workspace_bytes(self) -> int:
+        """Bytes of per-push scratch this stream can take from a shared
+        workspace (-1: it keeps state there and cannot share)."""
+        return int(_lib.load().ab_stream_workspace_bytes(self._h))
+
+    def set_workspace(self, ws: torch.Tensor):
+        """Use ``ws`` (a device uint8 tensor, kept alive here) as this stream's
+        per-push scratch.  Streams sharing one workspace must push in turn on
+        one CUDA stream."""
+        if ws.dtype != torch.uint8 or not ws.is_cuda or not ws.is_contiguous():
+            raise ValueError("workspace must be a contiguous uint8 CUDA tensor")
+        _lib.call("ab_stream_set_workspace", self._h, ws.data_ptr(), ws.numel())
+        self._ws = ws
+
     def kernel_launches(self) -> int:
         return int(_lib.load().ab_stream_kernel_launches(self._h))
 

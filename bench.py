@@ -121,15 +121,34 @@ def stage_bytes(sc):
     M, nslice, nq = 2 * NANT, ACCLEN + 2 * CUT, sc.nq
     nb = ACCLEN // OSAMP
     L = P * OSAMP
+    J = sc.fir_taps()
+    # rows of each IPFB column the time stage must read: all nslice for the
+    # FFT form, the kept rows plus the FIR half-lengths for the FIR form
+    rows_in = nslice if J == 0 else ACCLEN + 2 * J
     return {
         "row_ifft": NANT * nslice * 2 * NCHAN_RAW + M * P * nslice * 4,      # packets in, f32 rows out
         # time-axis deconvolution with the PFB fold fused in: IPFB column in,
         # folded/DFT'd fine blocks (W) out
-        "time_deconv": M * P * nslice * 4 + M * nb * L * 4,
+        "time_deconv": M * P * rows_in * 4 + M * nb * L * 4,
         "pfb_fold": 0,                                                      # fused into time_deconv
         "pfb_dft": M * nb * L * 4 + M * nb * nq * 8,                         # W in, band spectra out
         "xcorr": M * nb * nq * 8,                                           # band spectra in
     }
+
+
+def traffic_per_launch(stage):
+    """DRAM bytes (read + write) per launch of `stage`, from the ncu summary
+    committed in profiles/ (lines `traffic_per_launch <stage> <bytes>`)."""
+    import re
+    path = os.path.join(ROOT, "profiles", "dram_traffic_per_launch.txt")
+    try:
+        for line in open(path):
+            m = re.match(r"traffic_per_launch\s+(\w+)\s+(\d+)", line)
+            if m and m.group(1) == stage:
+                return int(m.group(2))
+    except OSError:
+        pass
+    return None
 
 
 def run_ours(args):
@@ -230,13 +249,7 @@ def run_ours(args):
     per_launch = algo[dom] * nchunks / max(nl, 1)
     peak, peak_kind = peaks()
     achieved = per_launch / (avg_ms / 1e3) / 1e9
-    traffic = None
-    tr_path = os.path.join(ROOT, "profiles", "traffic_per_launch.json")
-    if os.path.exists(tr_path):
-        try:
-            traffic = json.load(open(tr_path)).get(dom)
-        except Exception:
-            traffic = None
+    traffic = traffic_per_launch(dom)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -267,6 +280,87 @@ def run_ours(args):
     sc.close()
     if dist is not None:
         dist.destroy_process_group()
+
+
+BATCH_WORKLOAD = ("uneven batch: 24 files (16 x 4-bit, 8 x 1-bit), 2 ant x 2 pol each, channels from {32,64,128,512}, "
+                  "2^14..2^19 spectra, osamp from {16,64}, acclen 2^14 (cut 40) or 2^15 (cut 80), one captured graph")
+
+
+def _file_job0_error(args):
+    """Relative error of job 0 of one file against the FP64 oracle (runs the
+    oracle on the file's first two chunks, which fully determine job 0)."""
+    import numpy as np
+    from oracle import pfb_oracle as po
+    raw, channels, acclen, cut, osamp, nblock, bits, vis0 = args
+    ref, _ = po.repfb_xcorr_avg(raw, channels, acclen=acclen, nchunks=2, nblock=nblock, chanstart=0,
+                                chanend=len(channels), osamp=osamp, cut=cut, bits=bits)
+    r = ref[..., 0]
+    return float(np.linalg.norm(vis0 - r) / np.linalg.norm(r))
+
+
+def run_batch(args):
+    """The uneven batch in one captured graph (device-resident value; e2e
+    with the packets' H2D and the visibilities' D2H inside the graph)."""
+    import torch
+    from albatros_axion_detection_gb300 import batch
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    specs = batch.uneven_batch_specs(seed=2024)
+    files = batch.files_from_specs(specs, dev, host_copies=True)
+    t0 = time.perf_counter()
+    bc = batch.BatchCorrelator(files, lanes=args.lanes, tune=True, vis_to_host=True)
+    t_setup = time.perf_counter() - t0
+    bc.capture()
+    s = torch.cuda.current_stream(dev)
+    for _ in range(args.warmup):
+        bc.run(io=False)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        e0.record(s)
+        for _ in range(args.steps):
+            bc.run(io=False)
+        e1.record(s)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    bc.run(io=True)
+    torch.cuda.synchronize()
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record(s)
+    for _ in range(args.steps):
+        bc.run(io=True)
+    f1.record(s)
+    torch.cuda.synchronize()
+    ms_e2e = f0.elapsed_time(f1) / args.steps
+    spectra = bc.spectra
+    out = {
+        "metric": METRIC, "value": world * spectra / (ms / 1e3), "unit": "spectra/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded 4-bit Gaussian / 1-bit sign packets)",
+        "config": {"workload": BATCH_WORKLOAD, "spectra_per_step": spectra, "files": len(files), "lanes": len(bc.lanes),
+                   "parallelism": f"replicas x{world}",
+                   "tuned_time_stage": {f"acclen{k[0]}_cut{k[1]}_osamp{k[2]}": v for k, v in bc.tuned.items()},
+                   "setup_s": t_setup, "l2": "inputs larger than L2"},
+        "e2e": {"value": world * spectra / (ms_e2e / 1e3), "unit": "spectra/s", "ms_per_step": ms_e2e,
+                "h2d_bytes_per_step": bc.h2d_bytes, "d2h_bytes_per_step": bc.d2h_bytes},
+        "gpu_launches": int(bc.launches_per_run() * args.steps),
+        "clocks": clk.summary(),
+    }
+    if args.check:
+        import multiprocessing as mp
+        jobs = []
+        for i, f in enumerate(files):
+            two = f.host[:, : 2 * f.acclen].numpy().copy()
+            vis0 = bc.vis_host[i][0].numpy()  # (M, M, nq) of job 0
+            jobs.append((two, f.channels, f.acclen, f.cut, f.osamp, f.nblock, f.bits, vis0))
+        with mp.get_context("spawn").Pool(min(4, os.cpu_count() or 1)) as pool:
+            errs = pool.map(_file_job0_error, jobs)
+        out["per_file_job0_rel_err"] = {f.name: e for f, e in zip(files, errs)}
+        out["max_rel_err"] = max(errs)
+    bc.close()
+    print(json.dumps(out), flush=True)
 
 
 def cpu_baseline_sample(raw_np, sc=None, reps=1):
@@ -322,11 +416,17 @@ def main():
                     help="stream only this many 2^15-spectrum chunks (smaller case for profiling; "
                          "every launch keeps its full size)")
     ap.add_argument("--nant", type=int, default=None, help="antennas (profiling case; default 2)")
+    ap.add_argument("--workload", default="stream", choices=["stream", "uneven-batch"],
+                    help="stream: the 2-antenna 2^20-spectrum chain (default); uneven-batch: 24 mixed files")
+    ap.add_argument("--lanes", type=int, default=4, help="uneven-batch: concurrent CUDA streams")
+    ap.add_argument("--check", action="store_true", help="uneven-batch: job-0 error of every file vs the FP64 oracle")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "uneven-batch":
+        run_batch(args)
     else:
         run_ours(args)
 

@@ -43,6 +43,24 @@ const char *ab_last_error(void);
     albatros_analysis/src/utils/pycufft.py:27-90). */
 int ab_ctx_create(int device, ab_ctx **out);
 int ab_ctx_destroy(ab_ctx *ctx);
+/* Set (npass > 0) or clear (npass = 0) the FFT radix order used for
+ * transforms of length n in this context (radices from {2,3,4,5,7,8}, applied
+ * in order, product n).  Used by the autotuner (albatros_axion_detection_gb300/
+ * autotune.py); a set plan replaces the built-in compile-time plan of that
+ * length.  No reference counterpart: the reference delegates FFT planning to
+ * cuFFT (albatros_analysis/src/utils/pycufft.cu:201-303). */
+int ab_ctx_set_fft_plan(ab_ctx *ctx, int64_t n, const int32_t *radices, int64_t npass);
+/* Time-axis deconvolution of streams created after this call.  The FIR form
+ * is a (2J+1)-tap FIR of the reference's Wiener filter (J = 32 or 64, taps
+ * from the FP64 filter at the same nslice bins), usable when the dropped tail
+ * is below 1e-7 of the filter norm and the PFB fold is fused (osamp >= 4,
+ * ntap = 4); it runs any nslice.  The FFT form needs nslice/2 to factor into
+ * 2,3,5,7.  mode 0: FIR where usable, else FFT; mode 1: FFT only; mode 2
+ * (default): FFT where it runs, else FIR.
+ * row_tile: kept rows per thread of the FIR stage (16 or 32; 0 keeps the
+ * current value), taken by streams created after the call.  No reference counterpart: the reference
+ * always filters with cuFFT (albatros_analysis/src/utils/pfb_gpu_utils.py:56-91). */
+int ab_ctx_set_time_filter(ab_ctx *ctx, int32_t mode, int32_t row_tile);
 
 /* ---- unpacking ----------------------------------------------------------
  * ab_unpack_4bit: replaces unpack_4bit / _unpack_4bit_float_gpu
@@ -226,6 +244,20 @@ const float *ab_stream_vis(const ab_stream *st);
 int ab_stream_profile(ab_stream *st, int enable);
 int ab_stream_stage_times(const ab_stream *st, double *ms, int64_t *launches);
 int64_t ab_stream_kernel_launches(const ab_stream *st);
+/* Shared per-push scratch (no reference counterpart; the reference's driver
+ * holds one buffer set per run, helper_gpu_stream_clean.py:71-167).  A stream
+ * with the fused PFB fold (osamp >= 4, ntap = 4) keeps nothing in its scratch
+ * between pushes, so several streams whose pushes are serialised on one CUDA
+ * stream may share one workspace.  ab_stream_workspace_bytes: bytes needed
+ * (-1 when the stream cannot share).  ab_stream_set_workspace: frees the
+ * stream's own scratch (after a device synchronise) and uses ws (device,
+ * 256-byte aligned, caller-owned, alive until the stream is destroyed).
+ * Pushes of streams sharing a workspace must not overlap in time. */
+/* Half-length J of the FIR time stage this stream runs (0: the FFT time
+ * stage). */
+int64_t ab_stream_fir_taps(const ab_stream *st);
+int64_t ab_stream_workspace_bytes(const ab_stream *st);
+int ab_stream_set_workspace(ab_stream *st, void *ws, int64_t bytes);
 
 #ifdef __cplusplus
 }

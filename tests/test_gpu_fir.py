@@ -1,0 +1,126 @@
+"""GPU tests of the FIR form of the IPFB time stage (csrc/fir.cu): it is
+chosen for the default Wiener threshold, agrees with the FFT form and the FP64
+oracle, reproduces the reference's circular wrap when cut is below the FIR
+half-length (including the reference's default cut = 10, whose nslice has no
+fast FFT), and gives way to the FFT form for thresholds whose filter decays
+too slowly."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import pfb_oracle as po
+from tests.golden import gen
+from tests.test_gpu_stream import check
+
+pytestmark = pytest.mark.gpu
+
+
+def stream_vis(raw_np, channels, mode=0, row_tile=32, thresh=0.45, bits=4, **kw):
+    from albatros_axion_detection_gb300 import autotune, stream
+    autotune.set_time_filter(mode, row_tile)
+    try:
+        sc = stream.StreamCorrelator(raw_np.shape[0], channels, kw["chanstart"], kw["chanend"], kw["acclen"],
+                                     kw["nchunks"], kw["nblock"], kw["osamp"], kw["cut"], thresh, 4,
+                                     nchan_raw=len(channels), bits=bits)
+    finally:
+        autotune.set_time_filter(autotune.DEFAULT_MODE, 32)
+    try:
+        raw = torch.from_numpy(raw_np).cuda()
+        for j in range(kw["nchunks"]):
+            sc.push(raw, j, final=(j == kw["nchunks"] - 1))
+        return sc.vis_device().permute(1, 2, 3, 0).cpu().numpy(), sc.fir_taps()
+    finally:
+        sc.close()
+
+
+CFG = dict(acclen=1024, nchunks=3, nblock=64, chanstart=0, chanend=8, osamp=16, cut=64)
+
+
+def test_fir_chosen_and_matches_fft_and_oracle():
+    raw = gen.raw_4bit(seed=21, nspec=3 * 1024, nchan=8, nant=2)
+    ch = np.arange(600, 608)
+    ref, _ = po.repfb_xcorr_avg(raw, ch, **CFG)
+    v_fir, J = stream_vis(raw, ch, mode=0, **CFG)
+    v_fft, J0 = stream_vis(raw, ch, mode=1, **CFG)
+    assert J == 32 and J0 == 0
+    check(v_fir, ref)
+    check(v_fft, ref)
+    assert np.linalg.norm(v_fir - v_fft) / np.linalg.norm(v_fft) < 2e-6
+
+
+def test_fir_row_tiles_agree_bitwise():
+    raw = gen.raw_4bit(seed=22, nspec=3 * 1024, nchan=8, nant=1)
+    ch = np.arange(100, 108)
+    cfg = dict(CFG, osamp=64, nblock=16)
+    a, _ = stream_vis(raw, ch, row_tile=32, **cfg)
+    b, _ = stream_vis(raw, ch, row_tile=16, **cfg)
+    assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("acclen,cut,osamp,nchunks,bits", [
+    (1024, 10, 16, 3, 4),   # the reference's default cut: nslice 1044 = 4*9*29, FIR only; wrap inside kept rows
+    (512, 8, 4, 4, 4),      # cut < J with 4*osamp = 16
+    (1024, 10, 64, 3, 1),   # 1-bit packets, osamp 64
+])
+def test_fir_circular_wrap_small_cut(acclen, cut, osamp, nchunks, bits):
+    nch = 8
+    if bits == 4:
+        raw = gen.raw_4bit(seed=acclen + cut, nspec=nchunks * acclen, nchan=nch, nant=2)
+    else:
+        rng = np.random.default_rng(acclen + cut)
+        raw = rng.integers(0, 256, (2, nchunks * acclen, nch // 2), dtype=np.uint8)
+    ch = np.arange(700, 700 + nch)
+    kw = dict(acclen=acclen, nchunks=nchunks, nblock=max(acclen // osamp, 1), chanstart=0, chanend=nch,
+              osamp=osamp, cut=cut)
+    ref, _ = po.repfb_xcorr_avg(raw, ch, bits=bits, **kw)
+    v, J = stream_vis(raw, ch, bits=bits, **kw)
+    assert J == 32
+    check(v, ref)
+
+
+def test_threshold_02_uses_long_fir():
+    raw = gen.raw_4bit(seed=24, nspec=3 * 1024, nchan=8, nant=1)
+    ch = np.arange(310, 318)
+    ref, _ = po.repfb_xcorr_avg(raw, ch, filt_thresh=0.2, **CFG)
+    v, J = stream_vis(raw, ch, thresh=0.2, **CFG)
+    assert J == 64  # 0.2 needs 64 taps a side
+    check(v, ref)
+
+
+def test_small_threshold_uses_fft_stage():
+    raw = gen.raw_4bit(seed=23, nspec=3 * 1024, nchan=8, nant=1)
+    ch = np.arange(300, 308)
+    ref, _ = po.repfb_xcorr_avg(raw, ch, filt_thresh=0.1, **CFG)
+    v, J = stream_vis(raw, ch, thresh=0.1, **CFG)
+    assert J == 0  # the thresh 0.1 filter needs more than 64 taps a side
+    check(v, ref)
+
+
+def test_time_stage_tuner(tmp_path, monkeypatch):
+    from albatros_axion_detection_gb300 import autotune
+    monkeypatch.setenv("ALBATROS_GB300_TUNE_CACHE", str(tmp_path / "t.json"))
+    try:
+        best = autotune.tune_time_stage(1024, 64, 16, limit=2)
+        assert best["mode"] in (0, 1) and best["ms"] > 0
+        assert len(best["candidates"]) >= 2
+        again = autotune.tune_time_stage(1024, 64, 16, limit=2)
+        assert again["ms"] == best["ms"]
+    finally:
+        autotune.set_time_filter(autotune.DEFAULT_MODE, 32)
+        autotune.set_plan(576, None)
+
+
+@pytest.mark.parametrize("osamp,row_tile", [(64, 16), (64, 32), (4, 16)])
+def test_fir_multi_segment_columns(osamp, row_tile):
+    """acclen 8192 spans 2-3 segments per column (a segment holds
+    row_tile*256 - 4*osamp new rows): blocks across segment edges and the
+    tail state handed between chunks must match the oracle."""
+    acclen, nchunks = 8192, 2
+    raw = gen.raw_4bit(seed=osamp + row_tile, nspec=nchunks * acclen, nchan=4, nant=1)
+    ch = np.arange(900, 904)
+    kw = dict(acclen=acclen, nchunks=nchunks, nblock=acclen // osamp // 2, chanstart=0, chanend=4, osamp=osamp,
+              cut=64)
+    ref, _ = po.repfb_xcorr_avg(raw, ch, **kw)
+    v, J = stream_vis(raw, ch, row_tile=row_tile, **kw)
+    assert J == 32
+    check(v, ref)

@@ -85,7 +85,20 @@ def test_stream_1bit_vs_oracle(chs, osamp):
 
 
 def test_stream_rejects_bad_config():
-    from albatros_axion_detection_gb300 import stream
+    from albatros_axion_detection_gb300 import autotune, stream
     from albatros_axion_detection_gb300._lib import AlbatrosError
-    with pytest.raises((AlbatrosError, ValueError)):
-        stream.StreamCorrelator(1, np.arange(8), 0, 8, acclen=500, nchunks=2, nblock=4, osamp=4, cut=11)
+    # nslice/2 = 261 = 9*29: only the FIR time stage can run it
+    sc = stream.StreamCorrelator(1, np.arange(8), 0, 8, acclen=500, nchunks=2, nblock=4, osamp=4, cut=11)
+    assert sc.fir_taps() == 32
+    sc.close()
+    autotune.set_time_filter(1)
+    try:
+        with pytest.raises((AlbatrosError, ValueError)):
+            stream.StreamCorrelator(1, np.arange(8), 0, 8, acclen=500, nchunks=2, nblock=4, osamp=4, cut=11)
+    finally:
+        autotune.set_time_filter(autotune.DEFAULT_MODE)
+    for bad in (dict(osamp=3), dict(cut=0), dict(acclen=20, cut=11), dict(osamp=128)):
+        kw = dict(acclen=500, nchunks=2, nblock=4, osamp=4, cut=11)
+        kw.update(bad)
+        with pytest.raises((AlbatrosError, ValueError)):
+            stream.StreamCorrelator(1, np.arange(8), 0, 8, **kw)
