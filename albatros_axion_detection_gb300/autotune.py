@@ -118,14 +118,14 @@ def set_plan(n: int, radices: Optional[Sequence[int]], device: Optional[int] = N
     _lib.call("ab_ctx_set_fft_plan", c, int(n), ctypes.cast(arr, ctypes.c_void_p), len(radices))
 
 
-DEFAULT_MODE = 2
+DEFAULT_MODE = 0
 _filter_setting = {"mode": DEFAULT_MODE, "row_tile": 32}
 
 
 def set_time_filter(mode: int = DEFAULT_MODE, row_tile: int = 0, device: Optional[int] = None) -> None:
     """Time stage of streams created from now on: mode 0 = FIR where it is
-    accurate (else FFT), 1 = FFT only, 2 = FFT where it runs (else FIR, the
-    default); row_tile 16/32 (0 keeps it)."""
+    accurate, else FFT (the default), 1 = FFT only, 2 = FFT where it runs,
+    else FIR; row_tile 16/32 (0 keeps it)."""
     _lib.call("ab_ctx_set_time_filter", _lib.ctx(device), int(mode), int(row_tile))
     _filter_setting["mode"] = int(mode)
     if row_tile:

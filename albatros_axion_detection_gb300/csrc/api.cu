@@ -224,6 +224,8 @@ const char* ab_strerror(int code) {
 
 const char* ab_last_error(void) { return ab::g_err; }
 
+int ab_ctx_destroy(ab_ctx* ctx);
+
 int ab_ctx_create(int device, ab_ctx** out) {
   AB_CHECK_ARG(out != nullptr, "ab_ctx_create: out is NULL");
   AB_CUDA(cudaSetDevice(device));
@@ -245,6 +247,11 @@ int ab_ctx_create(int device, ab_ctx** out) {
     return rc;
   }
   c->tw64 = const_cast<float2*>(t64);
+  rc = ab::fir_init_device();
+  if (rc != AB_OK) {
+    ab_ctx_destroy(c);
+    return rc;
+  }
   *out = c;
   return AB_OK;
 }

@@ -380,7 +380,7 @@ static int stream_push(ab_stream* st, const uint8_t* raw, int64_t ant_stride, co
     const size_t half = (size_t)M * P * 4 * O;
     FirArgs fa_fir{cur, nslice, P, M, (int)nslice, (int)cut, (int)acclen, st->fir_taps, st->fir_J,
                    st->fir_row_tile, st->state + (chunk & 1) * half, st->state + ((chunk + 1) & 1) * half,
-                   st->ctx->tw64};
+                   st->ctx->tw64, st->ctx->num_sms};
     FoldArgs fa{O, st->ntap, (int)cut, (int)acclen, row0_all, nb_all, st->d_win, st->W, nullptr};
     AB_TRY(launch_fir_fold(fa_fir, fa, s));
     t.done(1);

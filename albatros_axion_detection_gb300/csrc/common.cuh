@@ -76,9 +76,9 @@ struct ab_ctx {
   // FIR taps of the time stage keyed by (P, nslice, ntap, thresh bits):
   // (J, device (P, 2J+1) floats or null when J = 0)
   std::map<std::vector<int64_t>, std::pair<int, const float*>> fir_taps;
-  // 0: FIR where accurate, else FFT; 1: always FFT; 2: FFT where it runs,
-  // else FIR
-  int time_filter_mode = 2;
+  // 0: FIR where accurate, else FFT (default); 1: always FFT; 2: FFT where
+  // it runs, else FIR
+  int time_filter_mode = 0;
   int fir_row_tile = 32;     // kept rows per thread of the FIR time stage
   // grow-only scratch buffers keyed by slot
   std::map<int, std::pair<void*, size_t>> scratch;
@@ -104,5 +104,7 @@ int get_pair_table(ab_ctx* ctx, const FftPlan& p, const int2** out);
 // Grow-only device scratch; the pointer stays valid until a larger request
 // for the same slot.
 int get_scratch(ab_ctx* ctx, int slot, size_t bytes, void** out);
+// Per-device constant tables of the FIR time stage (fir.cu).
+int fir_init_device();
 enum ScratchSlot { kScratchPfbW = 1, kScratchXcorrG = 2, kScratchChain = 3, kScratchYband = 4 };
 }  // namespace ab

@@ -218,113 +218,294 @@ int get_fir_taps(ab_ctx* ctx, int P, int N, int ntap, float thresh, int* J_out, 
 }
 
 // ---------------------------------------------------------------------------
-// FIR + fold.  U kept rows per thread (one unit), NTHR threads: a CTA computes
-// up to R = U*NTHR rows, S = R - 4*O of them new (the rest re-create the fine
-// blocks' overlap).  Shared memory: the x window (padded one float per U) and
-// the y rows in the pidx float2 layout the fold reads.
+// FIR + fold.  U kept rows per thread (U odd, so that lanes reading rows U
+// apart hit distinct shared-memory banks), kFirThreads threads: a work item
+// (segment seg of column n of input in) computes up to R = U*kFirThreads rows,
+// S = R - 4*O of them new (the rest re-create the fine blocks' overlap).
+// CTAs are persistent and walk the items with a stride of gridDim.x; while
+// one item is filtered and folded, the next item's x window, taps, window
+// coefficients and (for a first segment) tail rows are copied into the other
+// staging buffer with cp.async, so the global-memory latency overlaps the FMAs.
+// The fold gives each fine block to one thread: it folds the 4 taps into O
+// samples and takes their real DFT in registers (compile-time radix-2 FFT of
+// O/2 points plus the real-input untangle), then writes the O packed floats
+// of W with 16-byte stores.
 constexpr int kFirThreads = 256;
 
-__host__ __device__ constexpr int fir_xpad(int n, int U) { return n + n / U + 1; }
+__constant__ float2 c_fir_tw[64];  // exp(-2 pi i k / 64)
+
+int fir_init_device() {
+  float2 tw[64];
+  for (int k = 0; k < 64; k++) {
+    const double a = -2.0 * M_PI * (double)k / 64.0;
+    tw[k] = make_float2((float)std::cos(a), (float)std::sin(a));
+  }
+  AB_CUDA(cudaMemcpyToSymbol(c_fir_tw, tw, sizeof(tw)));
+  return AB_OK;
+}
+
+template <int J, int U, int O>
+struct FirLayout {
+  static constexpr int R = U * kFirThreads;
+  static constexpr int K = 2 * J + 1;
+  static constexpr int XS = (R + 2 * J + U + 3) & ~3;  // x window (floats, unpadded)
+  static constexpr int TAPS = (K + 3) & ~3;
+  static constexpr int ST = 4 * O;                      // tail rows of the previous chunk
+  static constexpr int WT = 4 * O;                      // window coefficients, float4 per t'
+  static constexpr int STAGE = XS + TAPS + ST + WT;     // floats per staging buffer (multiple of 4)
+  static constexpr int YROWS = R + 8 * O + U;           // y rows held (incl. zeros past the end)
+  static constexpr int YS = YROWS + YROWS / O + 4;      // one pad float per O rows
+  static constexpr size_t bytes() { return sizeof(float) * (2 * (size_t)STAGE + (size_t)YS); }
+};
+
+__device__ __forceinline__ void cp_async4(float* dst, const float* src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async16(float* dst, const float* src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+// d * exp(-2 pi i e / N) for a compile-time e
+template <int N>
+__device__ __forceinline__ float2 tw_mul(float2 d, int e) {
+  if (e == 0) return d;
+  if (4 * e == N) return make_float2(d.y, -d.x);  // * (-i)
+  return cmul(d, c_fir_tw[e * (64 / N)]);
+}
+
+// In-place radix-2 DIF FFT of N points in registers (forward, exp(-2 pi i/N));
+// output in bit-reversed order.  Fully unrolled: indices and twiddles are
+// compile-time.
+template <int N>
+__device__ __forceinline__ void reg_fft_dif(float2 (&a)[N]) {
+#pragma unroll
+  for (int span = N / 2; span >= 1; span >>= 1) {
+#pragma unroll
+    for (int base = 0; base < N; base += 2 * span) {
+#pragma unroll
+      for (int j = 0; j < span; j++) {
+        const float2 u = a[base + j], v = a[base + j + span];
+        a[base + j] = cadd(u, v);
+        a[base + j + span] = tw_mul<N>(csub(u, v), j * (N / (2 * span)));
+      }
+    }
+  }
+}
+
+__host__ __device__ constexpr int bitrev(int k, int bits) {
+  int r = 0;
+  for (int i = 0; i < bits; i++) r |= ((k >> i) & 1) << (bits - 1 - i);
+  return r;
+}
+__host__ __device__ constexpr int ilog2(int n) { return n <= 1 ? 0 : 1 + ilog2(n / 2); }
+
+struct FirItem {
+  int seg, n, in;
+  int s0, s1, ylo, nrows;
+  bool first, last;
+};
+
+__device__ __forceinline__ FirItem fir_item(int item, int nseg, int P, int S, int acclen, int O) {
+  FirItem it;
+  it.seg = item % nseg;
+  const int r = item / nseg;
+  it.n = r % P;
+  it.in = r / P;
+  it.s0 = it.seg * S;
+  it.s1 = min(it.s0 + S, acclen);
+  it.first = it.seg == 0;
+  it.last = it.s0 + S >= acclen;
+  it.ylo = it.first ? 0 : it.s0 - 4 * O;  // first row computed here
+  it.nrows = it.s1 - it.ylo;              // <= R
+  return it;
+}
 
 template <int J, int U, int G>
 __global__ void __launch_bounds__(kFirThreads, J <= 32 ? 2 : 1)
     fir_fold_kernel(const float* __restrict__ data, int64_t ld, int P, int nslice, int cut, int acclen, int S,
-                    const float* __restrict__ taps, FoldArgs fa, const float* __restrict__ state_in,
-                    float* __restrict__ state_out, const float2* __restrict__ tw64) {
-  constexpr int O = 2 * G, K = 2 * J + 1, R = U * kFirThreads;
-  extern __shared__ float2 smem2[];
-  float* xs = reinterpret_cast<float*>(smem2);
-  float2* ys2 = smem2 + (fir_xpad(R + 2 * J + U, U) + 1) / 2;  // float2-aligned
-  float* ys = reinterpret_cast<float*>(ys2);
-  const int seg = blockIdx.x, n = blockIdx.y, in = blockIdx.z, tid = threadIdx.x;
-  const int s0 = seg * S;
-  const int s1 = min(s0 + S, acclen);
-  const bool first = seg == 0, last = s0 + S >= acclen;
-  const int ylo = first ? 0 : s0 - 4 * O;  // first row computed here
-  const int nrows = s1 - ylo;              // <= R
-  const int yoff = ylo - s0 + 4 * O;       // ys row of computed row ylo
-  const float* col = data + ((int64_t)in * P + n) * ld;
-  // x window: xs[e] = x[(cut + ylo - J + e) mod nslice], e < nrows + 2J (+ slack)
-  const int xbase = cut + ylo - J;
-  const int nx = nrows + 2 * J;
-  for (int e = tid; e < nx + U; e += kFirThreads) {
-    float v = 0.f;
-    if (e < nx) {
-      int t = xbase + e;
-      if (t < 0 || t >= nslice) t = ((t % nslice) + nslice) % nslice;
-      v = __ldg(col + t);
-    }
-    xs[e + e / U] = v;
-  }
-  const float* st_in = state_in + ((int64_t)in * P + n) * (4 * O);
-  if (first) {
-    for (int i = tid; i < 4 * O; i += kFirThreads) ys[2 * pidx(i >> 1) + (i & 1)] = st_in[i];
-  }
-  float h[K];
-#pragma unroll
-  for (int k = 0; k < K; k++) h[k] = __ldg(&taps[(int64_t)n * K + k]);
-  __syncthreads();
-  // y[ylo + i] = sum_j h[j + J] x[cut + ylo + i - j] = sum_{k} h[k] xs[i + 2J - k]
-  if (tid * U < nrows) {
-    float acc[U];
-#pragma unroll
-    for (int g = 0; g < U; g++) acc[g] = 0.f;
-    const float* xu = xs + tid * (U + 1);  // xs index of e = tid*U (one pad float per U)
-#pragma unroll
-    for (int ep = 0; ep < U + 2 * J; ep++) {
-      const float v = xu[ep + ep / U];
-#pragma unroll
-      for (int g = 0; g < U; g++) {
-        const int k = g + 2 * J - ep;
-        if (k >= 0 && k < K) acc[g] = fmaf(h[k], v, acc[g]);
+                    int nseg, int nitems, const float* __restrict__ taps, FoldArgs fa,
+                    const float* __restrict__ state_in, float* __restrict__ state_out) {
+  constexpr int O = 2 * G, NC = O / 2, LOGNC = ilog2(NC);
+  constexpr int GW = O < 8 ? O : 8;
+  using Lay = FirLayout<J, U, O>;
+  constexpr int K = Lay::K;
+  extern __shared__ float4 smem4[];
+  float* stage0 = reinterpret_cast<float*>(smem4);
+  float* ys = stage0 + 2 * Lay::STAGE;
+  const int tid = threadIdx.x;
+
+  auto prefetch = [&](int item, float* stage) {
+    const FirItem it = fir_item(item, nseg, P, S, acclen, O);
+    const float* col = data + ((int64_t)it.in * P + it.n) * ld;
+    // x window: stage[e] = x[(cut + ylo - J + e) mod nslice], e < nrows + 2J
+    const int xbase = cut + it.ylo - J;
+    const int nx = it.nrows + 2 * J;
+    const float* src = col + xbase;
+    if (xbase >= 0 && xbase + nx <= nslice && (((uintptr_t)src) & 15) == 0) {
+      const int n4 = nx >> 2;
+      for (int q = tid; q < n4; q += kFirThreads) cp_async16(stage + 4 * q, src + 4 * q);
+      for (int e = 4 * n4 + tid; e < nx; e += kFirThreads) cp_async4(stage + e, src + e);
+    } else {
+      for (int e = tid; e < nx; e += kFirThreads) {
+        int t = xbase + e;
+        if (t < 0 || t >= nslice) t = ((t % nslice) + nslice) % nslice;
+        cp_async4(stage + e, col + t);
       }
     }
-    const int t0 = yoff + tid * U;  // even
-#pragma unroll
-    for (int q = 0; q < U / 2; q++) ys2[pidx((t0 >> 1) + q)] = make_float2(acc[2 * q], acc[2 * q + 1]);
-  }
-  __syncthreads();
-  // blocks whose last row lies in [s0, s0 + S) (the last segment: >= s0)
-  const int row0 = (int)fa.row0, nb = (int)fa.nb;
-  auto first_block_ending_at_or_after = [&](int r) -> int {  // min b with row0 + b*O + 4O - 1 >= r
-    const int num = r - 4 * O + 1 - row0;
-    int b = num <= 0 ? 0 : (num + O - 1) / O;
-    return min(b, nb);
-  };
-  const int b0 = first ? 0 : first_block_ending_at_or_after(s0);
-  const int b1 = last ? nb : first_block_ending_at_or_after(s0 + S);
-  if (b1 > b0) {
-    FoldArgs f2 = fa;
-    f2.cut = 4 * O - s0;  // ys row of chunk row rr is 4O - s0 + rr
-    f2.acclen = s1;       // rows >= s1 are zero (only past the end of the stream)
-    fold_blocks<G, 4, true>(ys2, nullptr, f2, P, n, in, tw64, b0, b1);
-  }
-  if (last) {
-    float* st = state_out + ((int64_t)in * P + n) * (4 * O);
-    for (int i = tid; i < 4 * O; i += kFirThreads) {
-      const int t = 4 * O - s0 + (acclen - 4 * O + i);
-      st[i] = ys[2 * pidx(t >> 1) + (t & 1)];
+    for (int e = nx + tid; e < nx + U; e += kFirThreads) stage[e] = 0.f;
+    float* st_taps = stage + Lay::XS;
+    for (int k = tid; k < K; k += kFirThreads) cp_async4(st_taps + k, taps + (int64_t)it.n * K + k);
+    float* st_tail = st_taps + Lay::TAPS;
+    if (it.first) {
+      const float* st = state_in + ((int64_t)it.in * P + it.n) * (4 * O);
+      for (int q = tid; q < O; q += kFirThreads) cp_async16(st_tail + 4 * q, st + 4 * q);
     }
-  }
-}
+    float* st_win = st_tail + Lay::ST;  // [t'][i] = win[(i*O + t')*P + n]
+    for (int q = tid; q < 4 * O; q += kFirThreads) {
+      const int tp = q >> 2, i = q & 3;
+      cp_async4(st_win + q, fa.win + (int64_t)(i * O + tp) * P + it.n);
+    }
+    cp_async_commit();
+  };
 
-template <int J, int U>
-static size_t fir_smem_bytes(int O) {
-  constexpr int R = U * kFirThreads;
-  const size_t xs2 = (size_t)(fir_xpad(R + 2 * J + U, U) + 1) / 2;
-  return sizeof(float2) * (xs2 + (size_t)padded_len((R + 4 * O + U) / 2 + 1));
+  int item = blockIdx.x, buf = 0;
+  if (item < nitems) prefetch(item, stage0);
+  for (; item < nitems; item += gridDim.x, buf ^= 1) {
+    float* stage = stage0 + buf * Lay::STAGE;
+    const int next = item + gridDim.x;
+    if (next < nitems) {
+      prefetch(next, stage0 + (buf ^ 1) * Lay::STAGE);
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
+    }
+    __syncthreads();
+    const FirItem it = fir_item(item, nseg, P, S, acclen, O);
+    const int yoff = it.ylo - it.s0 + 4 * O;  // y row of computed row ylo
+    // y rows are padded one float per O rows, with the pads at the fine
+    // blocks' first rows (y row phi + k*O): a block's 4*O rows then sit at
+    // base + c + c/O for compile-time c, and blocks O + 1 floats apart fall
+    // in distinct banks
+    const int phi = (((4 * O - it.s0 + (int)fa.row0) % O) + O) % O;
+    auto yidx = [phi](int q) { return q + (q - phi + O) / O; };
+    if (it.first) {
+      const float* st = stage + Lay::XS + Lay::TAPS;
+      for (int i = tid; i < 4 * O; i += kFirThreads) ys[yidx(i)] = st[i];
+    }
+    if (it.last) {  // zeros past the end of the stream (zero-padded final blocks)
+      for (int q = yoff + it.nrows + tid; q < yoff + it.nrows + 4 * O; q += kFirThreads) ys[yidx(q)] = 0.f;
+    }
+    // y[ylo + i] = sum_j h[j + J] x[cut + ylo + i - j] = sum_k h[k] xs[i + 2J - k]
+    if (tid * U < it.nrows) {
+      float h[K];
+#pragma unroll
+      for (int k = 0; k < K; k++) h[k] = stage[Lay::XS + k];
+      float acc[U];
+#pragma unroll
+      for (int g = 0; g < U; g++) acc[g] = 0.f;
+      const float* xu = stage + tid * U;
+#pragma unroll
+      for (int ep = 0; ep < U + 2 * J; ep++) {
+        const float v = xu[ep];
+#pragma unroll
+        for (int g = 0; g < U; g++) {
+          const int k = g + 2 * J - ep;
+          if (k >= 0 && k < K) acc[g] = fmaf(h[k], v, acc[g]);
+        }
+      }
+      const int t0 = yoff + tid * U;
+      const int nv = it.nrows - tid * U;
+#pragma unroll
+      for (int g = 0; g < U; g++)
+        if (g < nv) ys[yidx(t0 + g)] = acc[g];
+    }
+    __syncthreads();
+    // blocks whose last row lies in [s0, s0 + S) (the last segment: >= s0)
+    const int row0 = (int)fa.row0, nb = (int)fa.nb;
+    auto first_block_ending_at_or_after = [&](int r) -> int {  // min b with row0 + b*O + 4O - 1 >= r
+      const int num = r - 4 * O + 1 - row0;
+      const int b = num <= 0 ? 0 : (num + O - 1) / O;
+      return min(b, nb);
+    };
+    const int b0 = it.first ? 0 : first_block_ending_at_or_after(it.s0);
+    const int b1 = it.last ? nb : first_block_ending_at_or_after(it.s0 + S);
+    const float4* wt = reinterpret_cast<const float4*>(stage + Lay::XS + Lay::TAPS + Lay::ST);
+    float* wout = fa.W + (int64_t)it.in * fa.nb * ((int64_t)O * P) + (int64_t)it.n * GW;
+    for (int b = b0 + tid; b < b1; b += kFirThreads) {
+      const int rfirst = row0 + b * O;
+      float* wb = wout + (int64_t)b * ((int64_t)O * P);
+      if (rfirst >= it.s1) {  // entirely past the end of the stream
+#pragma unroll
+        for (int p = 0; p < O; p += 4)
+          *reinterpret_cast<float4*>(wb + (int64_t)(p / GW) * P * GW + (p % GW)) = make_float4(0.f, 0.f, 0.f, 0.f);
+        continue;
+      }
+      const int q0 = 4 * O - it.s0 + rfirst;   // y row of the block's first row (= phi mod O)
+      const float* yb = ys + yidx(q0);          // rows q0 + c at yb[c + c/O]
+      float2 a[NC];
+#pragma unroll
+      for (int m = 0; m < NC; m++) {
+        float zz[2];
+#pragma unroll
+        for (int e = 0; e < 2; e++) {
+          const int tp = 2 * m + e;
+          const float4 w4 = wt[tp];
+          zz[e] = fmaf(w4.x, yb[tp], fmaf(w4.y, yb[tp + (O + 1)],
+                                          fmaf(w4.z, yb[tp + 2 * (O + 1)], w4.w * yb[tp + 3 * (O + 1)])));
+        }
+        a[m] = make_float2(zz[0], zz[1]);
+      }
+      reg_fft_dif<NC>(a);
+      // untangle the real input: W_k = (Z_k + conj Z_{NC-k})/2 + w^k (Z_k - conj Z_{NC-k})/(2i);
+      // packed floats p = 2k, 2k+1 ((W_0, W_{O/2}) at p = 0, 1), stored 4 at a time
+#pragma unroll
+      for (int p = 0; p < O; p += 4) {
+        float2 o[2];
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+          const int k = p / 2 + h;
+          if (k == 0) {
+            o[h] = make_float2(a[0].x + a[0].y, a[0].x - a[0].y);
+          } else {
+            const float2 z = a[bitrev(k, LOGNC)], c = cconj(a[bitrev(NC - k, LOGNC)]);
+            const float2 E = cscale(cadd(z, c), 0.5f);
+            const float2 D = csub(z, c);
+            const float2 Od = make_float2(0.5f * D.y, -0.5f * D.x);
+            o[h] = cadd(E, cmul(c_fir_tw[k * (64 / O)], Od));
+          }
+        }
+        *reinterpret_cast<float4*>(wb + (int64_t)(p / GW) * P * GW + (p % GW)) = make_float4(o[0].x, o[0].y, o[1].x, o[1].y);
+      }
+    }
+    if (it.last) {
+      float* st = state_out + ((int64_t)it.in * P + it.n) * (4 * O);
+      for (int i = tid; i < 4 * O; i += kFirThreads) st[i] = ys[yidx(4 * O - it.s0 + (acclen - 4 * O + i))];
+    }
+    __syncthreads();  // ys and this staging buffer are reused next
+  }
 }
 
 template <int J, int U, int G>
 static int launch_fir_t(const FirArgs& a, const FoldArgs& fa, cudaStream_t s) {
-  constexpr int O = 2 * G, R = U * kFirThreads;
-  const int S = R - 4 * O;
+  constexpr int O = 2 * G;
+  using Lay = FirLayout<J, U, O>;
+  const int S = Lay::R - 4 * O;
   const int nseg = std::max(1, (a.acclen + S - 1) / S);
-  const size_t smem = fir_smem_bytes<J, U>(O);
+  const int64_t nitems = (int64_t)nseg * a.P * a.ninputs;
+  AB_CHECK_ARG(nitems < (1LL << 31), "FIR time stage: too many work items");
+  AB_CHECK_ARG(((uintptr_t)fa.W & 15) == 0 && (a.P % 4) == 0, "FIR time stage: W must be 16-byte aligned");
+  const size_t smem = Lay::bytes();
   AB_CUDA(cudaFuncSetAttribute(fir_fold_kernel<J, U, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  dim3 grid((unsigned)nseg, (unsigned)a.P, (unsigned)a.ninputs);
-  fir_fold_kernel<J, U, G><<<grid, kFirThreads, smem, s>>>(a.data, a.ld, a.P, a.nslice, a.cut, a.acclen, S, a.taps,
-                                                           fa, a.state_in, a.state_out, a.tw64);
+  const int per_sm = J <= 32 ? 2 : 1;
+  const int64_t grid = std::min<int64_t>(nitems, (int64_t)per_sm * std::max(a.num_sms, 1));
+  fir_fold_kernel<J, U, G><<<(unsigned)grid, kFirThreads, smem, s>>>(a.data, a.ld, a.P, a.nslice, a.cut, a.acclen, S,
+                                                                     nseg, (int)nitems, a.taps, fa, a.state_in,
+                                                                     a.state_out);
   AB_LAUNCH_CHECK();
   return AB_OK;
 }
@@ -347,9 +528,12 @@ int launch_fir_fold(const FirArgs& a, const FoldArgs& fa, cudaStream_t s) {
   AB_CHECK_ARG(fa.ntap == 4, "FIR time stage: needs ntap = 4");
   AB_CHECK_ARG(a.P <= 65535 && a.ninputs <= 65535, "FIR time stage: grid too large");
   AB_CHECK_ARG(a.row_tile == 16 || a.row_tile == 32, "FIR time stage: row tile must be 16 or 32");
+  AB_CHECK_ARG(a.num_sms > 0, "FIR time stage: SM count unknown");
   AB_CHECK_ARG(a.row_tile * kFirThreads > 4 * fa.O, "FIR time stage: row tile too small for osamp %d", fa.O);
-  if (a.J == 32) return a.row_tile == 32 ? launch_fir_o<32, 32>(a, fa, s) : launch_fir_o<32, 16>(a, fa, s);
-  if (a.J == 64) return a.row_tile == 32 ? launch_fir_o<64, 32>(a, fa, s) : launch_fir_o<64, 16>(a, fa, s);
+  // odd row tiles (33, 17 rows per thread) keep the FIR's shared loads
+  // conflict-free without padding
+  if (a.J == 32) return a.row_tile == 32 ? launch_fir_o<32, 33>(a, fa, s) : launch_fir_o<32, 17>(a, fa, s);
+  if (a.J == 64) return a.row_tile == 32 ? launch_fir_o<64, 33>(a, fa, s) : launch_fir_o<64, 17>(a, fa, s);
   set_error("FIR time stage: J = %d not supported", a.J);
   return AB_ERR_UNSUPPORTED;
 }

@@ -85,7 +85,10 @@ struct FirArgs {
   const float* state_in;  // previous chunk's last 4*O rows (ninputs, P, 4*O)
   float* state_out;       // this chunk's last 4*O rows (the other buffer)
   const float2* tw64;
+  int num_sms;            // persistent grid: CTAs per SM x num_sms
 };
+// Per-device constants of the FIR time stage (call once per device).
+int fir_init_device();
 // Time stage by FIR over the kept rows, fused with the PFB fold (fa: O, ntap
 // = 4, row0, nb, win, W; fa.cut/acclen/state unused).
 int launch_fir_fold(const FirArgs& a, const FoldArgs& fa, cudaStream_t s);

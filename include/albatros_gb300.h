@@ -55,8 +55,8 @@ int ab_ctx_set_fft_plan(ab_ctx *ctx, int64_t n, const int32_t *radices, int64_t 
  * from the FP64 filter at the same nslice bins), usable when the dropped tail
  * is below 1e-7 of the filter norm and the PFB fold is fused (osamp >= 4,
  * ntap = 4); it runs any nslice.  The FFT form needs nslice/2 to factor into
- * 2,3,5,7.  mode 0: FIR where usable, else FFT; mode 1: FFT only; mode 2
- * (default): FFT where it runs, else FIR.
+ * 2,3,5,7.  mode 0 (default): FIR where usable, else FFT; mode 1: FFT only;
+ * mode 2: FFT where it runs, else FIR.
  * row_tile: kept rows per thread of the FIR stage (16 or 32; 0 keeps the
  * current value), taken by streams created after the call.  No reference counterpart: the reference
  * always filters with cuFFT (albatros_analysis/src/utils/pfb_gpu_utils.py:56-91). */
