@@ -53,6 +53,7 @@ SIGNATURES = {
     "ab_stream_kernel_launches": (I64, [P]),
     "ab_stream_workspace_bytes": (I64, [P]),
     "ab_stream_fir_taps": (I64, [P]),
+    "ab_stream_time_filter": (I32, [P, P, P]),
     "ab_stream_set_workspace": (I32, [P, P, I64]),
 }
 

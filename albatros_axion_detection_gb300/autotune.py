@@ -1,9 +1,9 @@
 """Autotuner for the chain's time stage: FIR row tile, or FFT radix order.
 
-The IPFB time-axis deconvolution has two forms in the library.  The FIR form
-(the default wherever the reference's Wiener filter decays fast enough) has one
-tunable tile: the kept rows per thread (16 or 32), which sets the rows a CTA
-filters and how many CTAs share an SM.  The FFT form runs one real FFT of
+The IPFB time-axis deconvolution has three forms in the library.  The IIR and
+FIR forms (the default wherever the reference's Wiener filter decays fast
+enough) have one tunable tile: the kept rows per thread (16 or 32), which sets
+the rows a CTA filters and how many CTAs share an SM.  The FFT form runs one real FFT of
 nslice = acclen + 2*cut points per coarse sample phase (a complex FFT of
 n = nslice/2 points) and its inverse; two lengths have compile-time plans
 (n = 16464 for acclen 2^15, cut 80, and n = 16384), every other length runs
@@ -133,9 +133,9 @@ def set_time_filter(mode: int = DEFAULT_MODE, row_tile: int = 0, device: Optiona
 
 
 def _time_chain(acclen: int, cut: int, osamp: int, nchunks: int = 2, reps: int = 2, mode: int = 0,
-                row_tile: int = 32) -> Tuple[float, int]:
-    """(ms per launch of the chain's time stage for one antenna, FIR J) with
-    the given time-filter setting; the previous setting is restored."""
+                row_tile: int = 32) -> Tuple[float, Tuple[str, int]]:
+    """(ms per launch of the chain's time stage for one antenna, the form that
+    ran) with the given time-filter setting; the previous setting is restored."""
     from .stream import StreamCorrelator
     prev = dict(_filter_setting)
     set_time_filter(mode, row_tile)
@@ -145,7 +145,7 @@ def _time_chain(acclen: int, cut: int, osamp: int, nchunks: int = 2, reps: int =
         set_time_filter(prev["mode"], prev["row_tile"])
 
 
-def _time_chain_now(acclen: int, cut: int, osamp: int, nchunks: int, reps: int) -> Tuple[float, int]:
+def _time_chain_now(acclen: int, cut: int, osamp: int, nchunks: int, reps: int) -> Tuple[float, Tuple[str, int]]:
     from .stream import StreamCorrelator
     dev = torch.device("cuda", torch.cuda.current_device())
     nch = 8
@@ -167,7 +167,7 @@ def _time_chain_now(acclen: int, cut: int, osamp: int, nchunks: int, reps: int) 
             ms, nl = sc.stage_times()["time_deconv"]
             sc.profile(False)
             best = min(best, ms / max(nl, 1))
-        return best, sc.fir_taps()
+        return best, sc.time_filter()
     finally:
         sc.close()
 
@@ -217,10 +217,10 @@ def tune_time_fft(acclen: int, cut: int, osamp: int = 64, *, use_cache: bool = T
 
 def tune_time_stage(acclen: int, cut: int, osamp: int = 64, *, use_cache: bool = True, limit: int = 24,
                     verbose: bool = False) -> Dict[str, object]:
-    """Choose the time stage for (acclen, cut, osamp): the FIR form with the
-    faster row tile, or the FFT form with its tuned radix order, whichever is
-    faster on this device.  Returns {"mode", "row_tile", "radices", "ms",
-    "fir_J"}; ``apply`` installs it."""
+    """Choose the time stage for (acclen, cut, osamp): the IIR or FIR form with
+    either row tile, or the FFT form with its tuned radix order, whichever is
+    fastest on this device.  Returns {"mode", "row_tile", "radices", "ms",
+    "form"}; ``apply`` installs it."""
     _lib.require_cuda()
     key = f"{torch.cuda.get_device_name()}|time_stage|{acclen}|{cut}|{osamp}"
     with _lock:
@@ -229,18 +229,19 @@ def tune_time_stage(acclen: int, cut: int, osamp: int = 64, *, use_cache: bool =
         apply(hit)
         return hit
     cands = []
-    for tile in (32, 16):
-        ms, J = _time_chain(acclen, cut, osamp, mode=0, row_tile=tile)
-        if J == 0:
-            break  # the FIR form does not apply to this filter
-        cands.append({"mode": 0, "row_tile": tile, "radices": None, "ms": ms, "fir_J": J})
-        if verbose:
-            print(f"acclen={acclen} cut={cut} osamp={osamp} FIR J={J} tile={tile}: {ms:.3f} ms", flush=True)
+    for mode, kind in ((0, "iir"), (3, "fir")):
+        for tile in (32, 16):
+            ms, form = _time_chain(acclen, cut, osamp, mode=mode, row_tile=tile)
+            if form[0] != kind:
+                break  # this form does not apply to the filter
+            cands.append({"mode": mode, "row_tile": tile, "radices": None, "ms": ms, "form": list(form)})
+            if verbose:
+                print(f"acclen={acclen} cut={cut} osamp={osamp} {form} tile={tile}: {ms:.3f} ms", flush=True)
     try:
         radices, ms = tune_time_fft(acclen, cut, osamp, use_cache=use_cache, limit=limit if not cands else 0,
                                     verbose=verbose)
         cands.append({"mode": 1, "row_tile": _filter_setting["row_tile"],
-                      "radices": radices if radices == BUILTIN else list(radices), "ms": ms, "fir_J": 0})
+                      "radices": radices if radices == BUILTIN else list(radices), "ms": ms, "form": ["fft", 0]})
     except (ValueError, _lib.AlbatrosError):
         pass
     if not cands:

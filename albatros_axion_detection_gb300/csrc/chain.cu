@@ -48,6 +48,7 @@ struct ab_stream {
   bool fused = false;        // PFB fold fused into the time stage (osamp >= 4)
   float* state = nullptr;    // fused: last 4*osamp timestream rows per column (x2 for the FIR path)
   int fir_J = 0;             // > 0: time stage as a (2J+1)-tap FIR (fir.cu)
+  int iir_W = 0;             // > 0: time stage as the IIR factorisation, warm-up iir_W (fir.cu)
   int fir_row_tile = 32;     // kept rows per thread of the FIR stage
   const float* fir_taps = nullptr;
   float* W = nullptr;
@@ -157,32 +158,36 @@ extern "C" int ab_stream_create(ab_ctx* ctx, int64_t nant, int64_t nchan_raw, in
   FftPlan pm{};
   const bool fft_ok = st->nslice % 2 == 0 && ctx_plan(ctx, (int)(st->nslice / 2), &pm) &&
                       (size_t)(st->nslice / 2) * sizeof(float2) <= ctx->smem_optin;
-  if (st->fused && (mode == 0 || (mode == 2 && !fft_ok)) && st->nslice <= (int64_t)1 << 30) {
-    int rc = get_fir_taps(ctx, P, (int)st->nslice, (int)ntap, (float)thresh, &st->fir_J, &st->fir_taps);
+  if (st->fused && (mode == 0 || mode == 3 || (mode == 2 && !fft_ok)) && st->nslice <= (int64_t)1 << 30) {
+    int rc = AB_OK;
+    if (mode != 3) rc = get_iir_coeffs(ctx, P, (int)ntap, (float)thresh, &st->iir_W, &st->fir_taps);
+    if (rc == AB_OK && st->iir_W == 0)
+      rc = get_fir_taps(ctx, P, (int)st->nslice, (int)ntap, (float)thresh, &st->fir_J, &st->fir_taps);
     if (rc != AB_OK) {
       delete st;
       return rc;
     }
   }
+  const bool fir_path = st->fir_J > 0 || st->iir_W > 0;
   if (!ctx_plan(ctx, P, &st->planP)) {
     set_error("ab_stream_create: no FFT plan for lblock %d", P);
     delete st;
     return AB_ERR_UNSUPPORTED;
   }
-  if (st->fir_J == 0 && (st->nslice % 2 || !ctx_plan(ctx, (int)(st->nslice / 2), &st->planM))) {
+  if (!fir_path && (st->nslice % 2 || !ctx_plan(ctx, (int)(st->nslice / 2), &st->planM))) {
     set_error("ab_stream_create: nslice = acclen + 2*cut = %lld must be even with nslice/2 factoring into 2,3,5,7",
               (long long)st->nslice);
     delete st;
     return AB_ERR_UNSUPPORTED;
   }
-  if (st->fir_J == 0 && (size_t)(st->nslice / 2) * sizeof(float2) > ctx->smem_optin) {
+  if (!fir_path && (size_t)(st->nslice / 2) * sizeof(float2) > ctx->smem_optin) {
     set_error("ab_stream_create: nslice %lld exceeds the shared-memory column limit", (long long)st->nslice);
     delete st;
     return AB_ERR_UNSUPPORTED;
   }
   int rc;
   if ((rc = get_twiddles(ctx, P, &st->twP)) != AB_OK ||
-      (st->fir_J == 0 && (rc = get_twiddles(ctx, st->nslice, &st->twN)) != AB_OK) ||
+      (!fir_path && (rc = get_twiddles(ctx, st->nslice, &st->twN)) != AB_OK) ||
       (rc = get_twiddles(ctx, (int64_t)P * osamp, &st->twL)) != AB_OK) {
     delete st;
     return rc;
@@ -319,6 +324,12 @@ extern "C" int ab_stream_set_workspace(ab_stream* st, void* ws, int64_t bytes) {
 extern "C" const float* ab_stream_vis(const ab_stream* st) { return st ? (const float*)st->vis : nullptr; }
 extern "C" int64_t ab_stream_kernel_launches(const ab_stream* st) { return st ? st->launches : -1; }
 extern "C" int64_t ab_stream_fir_taps(const ab_stream* st) { return st ? st->fir_J : -1; }
+extern "C" int ab_stream_time_filter(const ab_stream* st, int32_t* kind, int32_t* param) {
+  AB_CHECK_ARG(st && kind && param, "ab_stream_time_filter: NULL pointer");
+  *kind = st->iir_W > 0 ? 2 : st->fir_J > 0 ? 1 : 0;
+  *param = st->iir_W > 0 ? st->iir_W : st->fir_J;
+  return AB_OK;
+}
 
 // Stage timing (profiling mode only): events around one stage, synchronised
 // immediately, so this mode serialises the host with the device.
@@ -375,12 +386,12 @@ static int stream_push(ab_stream* st, const uint8_t* raw, int64_t ant_stride, co
     t.done(1);
   }
   // 2. time stage (with the PFB fold fused in when osamp >= 4)
-  if (st->fir_J > 0) {
+  if (st->fir_J > 0 || st->iir_W > 0) {
     StageTimer t(st, s, 1);
     const size_t half = (size_t)M * P * 4 * O;
     FirArgs fa_fir{cur, nslice, P, M, (int)nslice, (int)cut, (int)acclen, st->fir_taps, st->fir_J,
                    st->fir_row_tile, st->state + (chunk & 1) * half, st->state + ((chunk + 1) & 1) * half,
-                   st->ctx->tw64, st->ctx->num_sms};
+                   st->ctx->tw64, st->ctx->num_sms, st->iir_W};
     FoldArgs fa{O, st->ntap, (int)cut, (int)acclen, row0_all, nb_all, st->d_win, st->W, nullptr};
     AB_TRY(launch_fir_fold(fa_fir, fa, s));
     t.done(1);

@@ -76,8 +76,8 @@ struct ab_ctx {
   // FIR taps of the time stage keyed by (P, nslice, ntap, thresh bits):
   // (J, device (P, 2J+1) floats or null when J = 0)
   std::map<std::vector<int64_t>, std::pair<int, const float*>> fir_taps;
-  // 0: FIR where accurate, else FFT (default); 1: always FFT; 2: FFT where
-  // it runs, else FIR
+  // 0: IIR, else FIR, else FFT, the first that is accurate (default);
+  // 1: always FFT; 2: FFT where it runs, else IIR/FIR; 3: FIR, else FFT
   int time_filter_mode = 0;
   int fir_row_tile = 32;     // kept rows per thread of the FIR time stage
   // grow-only scratch buffers keyed by slot

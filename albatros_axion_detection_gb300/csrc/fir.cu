@@ -218,6 +218,154 @@ int get_fir_taps(ab_ctx* ctx, int P, int N, int ntap, float thresh, int* J_out, 
 }
 
 // ---------------------------------------------------------------------------
+// IIR form of the same filter.  With W(z) = sum_{k<4} w_k z^-k (the column's
+// window taps, m = W(exp(2 pi i f / nslice))), the reference's filter is
+//   H(z) = W(z) (1 + t^2) / D(z),  D(z) = t^2 + W(z) W(1/z),
+// and D, positive on the unit circle, factors as D(z) = B(z) B(1/z) with
+// B(z) = b_0 + b_1 z^-1 + b_2 z^-2 + b_3 z^-3 minimum-phase (Wilson's
+// iteration: Newton's method on B(z)B(1/z) = D(z), started from a constant).
+// So y = g W(z) / (A(z) A(1/z)) x with A = B / b_0 and g = (1 + t^2) / b_0^2:
+// a 4-tap FIR, a causal 3-pole recursion and an anti-causal 3-pole recursion,
+// 11 FMAs per sample.  Applied to the periodic column it reproduces the
+// circular convolution; each thread starts both recursions IW samples before
+// its rows from zero state, which drops a tail of the size of 1/A's impulse
+// response after IW samples (chosen below 1e-10 of its peak).
+static bool iir_factor(const double* w, double t, double coef[8], int* warm) {
+  const int m = 3;
+  double d[4];
+  for (int k = 0; k <= m; k++) {
+    d[k] = 0.0;
+    for (int i = 0; i + k <= m; i++) d[k] += w[i] * w[i + k];
+  }
+  d[0] += t * t;
+  if (!(d[0] > 0.0)) return false;
+  double b[4] = {std::sqrt(d[0]), 0.0, 0.0, 0.0};
+  for (int it = 0; it < 200; it++) {
+    // B X* + X B* = D + B B*, lags 0..m
+    double M[4][5];
+    for (int k = 0; k <= m; k++) {
+      double rhs = d[k];
+      for (int j = 0; j + k <= m; j++) rhs += b[j] * b[j + k];
+      for (int i = 0; i <= m; i++) M[k][i] = (i >= k ? b[i - k] : 0.0) + (i + k <= m ? b[i + k] : 0.0);
+      M[k][4] = rhs;
+    }
+    for (int c = 0; c <= m; c++) {  // Gaussian elimination with partial pivoting
+      int pv = c;
+      for (int r = c + 1; r <= m; r++)
+        if (std::fabs(M[r][c]) > std::fabs(M[pv][c])) pv = r;
+      if (std::fabs(M[pv][c]) < 1e-300) return false;
+      if (pv != c)
+        for (int q = 0; q < 5; q++) std::swap(M[c][q], M[pv][q]);
+      for (int r = 0; r <= m; r++) {
+        if (r == c) continue;
+        const double f = M[r][c] / M[c][c];
+        for (int q = c; q < 5; q++) M[r][q] -= f * M[c][q];
+      }
+    }
+    double delta = 0.0, norm = 0.0;
+    for (int i = 0; i <= m; i++) {
+      const double x = M[i][4] / M[i][i];
+      delta = std::max(delta, std::fabs(x - b[i]));
+      norm = std::max(norm, std::fabs(x));
+      b[i] = x;
+    }
+    if (!std::isfinite(norm)) return false;
+    if (delta <= 1e-15 * norm) break;
+  }
+  // check B(z) B(1/z) = D(z) on the unit circle
+  for (int q = 0; q < 64; q++) {
+    const double om = M_PI * q / 63.0;
+    double br = 0, bi = 0;
+    for (int k = 0; k <= m; k++) {
+      br += b[k] * std::cos(om * k);
+      bi -= b[k] * std::sin(om * k);
+    }
+    double dd = d[0];
+    for (int k = 1; k <= m; k++) dd += 2.0 * d[k] * std::cos(om * k);
+    if (std::fabs(br * br + bi * bi - dd) > 1e-11 * dd) return false;
+  }
+  const double a1 = b[1] / b[0], a2 = b[2] / b[0], a3 = b[3] / b[0];
+  // decay of 1/A: warm-up length
+  double h[600] = {1.0};
+  double peak = 1.0;
+  int last = 0;
+  for (int k = 1; k < 600; k++) {
+    h[k] = -(a1 * h[k - 1] + (k >= 2 ? a2 * h[k - 2] : 0.0) + (k >= 3 ? a3 * h[k - 3] : 0.0));
+    peak = std::max(peak, std::fabs(h[k]));
+    if (std::fabs(h[k]) > 1e-10 * peak) last = k;
+  }
+  if (last >= 590 || peak > 1e6) return false;
+  *warm = last + 1;
+  const double g = (1.0 + t * t) / (b[0] * b[0]);  // folded into the FIR taps
+  coef[0] = g * w[0];
+  coef[1] = g * w[1];
+  coef[2] = g * w[2];
+  coef[3] = g * w[3];
+  coef[4] = a1;
+  coef[5] = a2;
+  coef[6] = a3;
+  coef[7] = 0.0;
+  return true;
+}
+
+// Per-column IIR coefficients (g w0..g w3, a1..a3, 0) as float (P, 8) and the
+// warm-up IW in {40, 80} (0 when no factorisation or a longer warm-up is
+// needed), cached in the context per (P, ntap, thresh).
+int get_iir_coeffs(ab_ctx* ctx, int P, int ntap, float thresh, int* W_out, const float** coef_out) {
+  *W_out = 0;
+  *coef_out = nullptr;
+  if (ntap != 4) return AB_OK;
+  uint32_t tb;
+  memcpy(&tb, &thresh, sizeof(tb));
+  std::vector<int64_t> key = {-1, P, ntap, (int64_t)tb};
+  {
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    auto it = ctx->fir_taps.find(key);
+    if (it != ctx->fir_taps.end()) {
+      *W_out = it->second.first;
+      *coef_out = it->second.second;
+      return AB_OK;
+    }
+  }
+  std::vector<double> w;
+  sinc_hamming_host(ntap, P, w);
+  std::vector<float> cf((size_t)P * 8);
+  int warm = 0;
+  bool ok = thresh > 0.f;
+  for (int n = 0; n < P && ok; n++) {
+    double wn[4], c[8];
+    for (int k = 0; k < 4; k++) wn[k] = w[(size_t)k * P + n];
+    int wm = 0;
+    ok = iir_factor(wn, (double)thresh, c, &wm);
+    warm = std::max(warm, wm);
+    for (int k = 0; k < 8; k++) cf[(size_t)n * 8 + k] = (float)c[k];
+  }
+  const int IW = !ok ? 0 : warm <= 40 ? 40 : warm <= 80 ? 80 : 0;
+  float* dc = nullptr;
+  if (IW > 0) {
+    if (cudaMalloc(&dc, sizeof(float) * cf.size()) != cudaSuccess) {
+      set_error("IIR coefficients: device allocation failed");
+      return AB_ERR_NOMEM;
+    }
+    if (cudaMemcpy(dc, cf.data(), sizeof(float) * cf.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+      cudaFree(dc);
+      set_error("IIR coefficients: upload failed");
+      return AB_ERR_CUDA;
+    }
+  }
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  auto it = ctx->fir_taps.find(key);
+  if (it != ctx->fir_taps.end()) {
+    cudaFree(dc);
+  } else {
+    it = ctx->fir_taps.emplace(key, std::make_pair(IW, (const float*)dc)).first;
+  }
+  *W_out = it->second.first;
+  *coef_out = it->second.second;
+  return AB_OK;
+}
+
+// ---------------------------------------------------------------------------
 // FIR + fold.  U kept rows per thread (U odd, so that lanes reading rows U
 // apart hit distinct shared-memory banks), kFirThreads threads: a work item
 // (segment seg of column n of input in) computes up to R = U*kFirThreads rows,
@@ -244,11 +392,15 @@ int fir_init_device() {
   return AB_OK;
 }
 
-template <int J, int U, int O>
+// IW = 0: FIR with 2J+1 taps (halo J each side); IW > 0: IIR with warm-up IW
+// (halo IW + 3 before, IW after; 8 coefficients per column).
+template <int J, int U, int O, int IW>
 struct FirLayout {
   static constexpr int R = U * kFirThreads;
-  static constexpr int K = 2 * J + 1;
-  static constexpr int XS = (R + 2 * J + U + 3) & ~3;  // x window (floats, unpadded)
+  static constexpr int HL = IW > 0 ? IW + 3 : J;
+  static constexpr int HR = IW > 0 ? IW : J;
+  static constexpr int K = IW > 0 ? 8 : 2 * J + 1;
+  static constexpr int XS = (R + HL + HR + U + 3) & ~3;  // x window (floats, unpadded)
   static constexpr int TAPS = (K + 3) & ~3;
   static constexpr int ST = 4 * O;                      // tail rows of the previous chunk
   static constexpr int WT = 4 * O;                      // window coefficients, float4 per t'
@@ -325,14 +477,14 @@ __device__ __forceinline__ FirItem fir_item(int item, int nseg, int P, int S, in
   return it;
 }
 
-template <int J, int U, int G>
-__global__ void __launch_bounds__(kFirThreads, J <= 32 ? 2 : 1)
+template <int J, int U, int G, int IW>
+__global__ void __launch_bounds__(kFirThreads, (IW > 0 && IW <= 40) || (IW == 0 && J <= 32) ? 2 : 1)
     fir_fold_kernel(const float* __restrict__ data, int64_t ld, int P, int nslice, int cut, int acclen, int S,
                     int nseg, int nitems, const float* __restrict__ taps, FoldArgs fa,
                     const float* __restrict__ state_in, float* __restrict__ state_out) {
   constexpr int O = 2 * G, NC = O / 2, LOGNC = ilog2(NC);
   constexpr int GW = O < 8 ? O : 8;
-  using Lay = FirLayout<J, U, O>;
+  using Lay = FirLayout<J, U, O, IW>;
   constexpr int K = Lay::K;
   extern __shared__ float4 smem4[];
   float* stage0 = reinterpret_cast<float*>(smem4);
@@ -342,9 +494,9 @@ __global__ void __launch_bounds__(kFirThreads, J <= 32 ? 2 : 1)
   auto prefetch = [&](int item, float* stage) {
     const FirItem it = fir_item(item, nseg, P, S, acclen, O);
     const float* col = data + ((int64_t)it.in * P + it.n) * ld;
-    // x window: stage[e] = x[(cut + ylo - J + e) mod nslice], e < nrows + 2J
-    const int xbase = cut + it.ylo - J;
-    const int nx = it.nrows + 2 * J;
+    // x window: stage[e] = x[(cut + ylo - HL + e) mod nslice], e < nrows + HL + HR
+    const int xbase = cut + it.ylo - Lay::HL;
+    const int nx = it.nrows + Lay::HL + Lay::HR;
     const float* src = col + xbase;
     if (xbase >= 0 && xbase + nx <= nslice && (((uintptr_t)src) & 15) == 0) {
       const int n4 = nx >> 2;
@@ -400,6 +552,39 @@ __global__ void __launch_bounds__(kFirThreads, J <= 32 ? 2 : 1)
     if (it.last) {  // zeros past the end of the stream (zero-padded final blocks)
       for (int q = yoff + it.nrows + tid; q < yoff + it.nrows + 4 * O; q += kFirThreads) ys[yidx(q)] = 0.f;
     }
+    if constexpr (IW > 0) {
+      // IIR: rows r0 + [0, U), r0 = tid*U; x of row offset tt (from r0) at
+      // xu[IW + 3 + tt].  Causal u = W x, v = u / A over tt in [-IW, U + IW),
+      // keeping v for tt >= 0; then y = g v / A(1/z) backwards from U + IW - 1.
+      if (tid * U < it.nrows) {
+        const float* cf = stage + Lay::XS;
+        const float w0 = cf[0], w1 = cf[1], w2 = cf[2], w3 = cf[3];
+        const float a1 = cf[4], a2 = cf[5], a3 = cf[6];
+        const float* xu = stage + tid * U;
+        float v[U + IW];
+        float s1 = 0.f, s2 = 0.f, s3 = 0.f;
+#pragma unroll
+        for (int mm = 0; mm < U + 2 * IW; mm++) {
+          const float u = fmaf(w0, xu[mm + 3], fmaf(w1, xu[mm + 2], fmaf(w2, xu[mm + 1], w3 * xu[mm])));
+          const float vt = fmaf(-a1, s1, fmaf(-a2, s2, fmaf(-a3, s3, u)));
+          s3 = s2;
+          s2 = s1;
+          s1 = vt;
+          if (mm >= IW) v[mm - IW] = vt;
+        }
+        const int t0 = yoff + tid * U;
+        const int nv = it.nrows - tid * U;
+        float q1 = 0.f, q2 = 0.f, q3 = 0.f;
+#pragma unroll
+        for (int mm = U + IW - 1; mm >= 0; mm--) {
+          const float yt = fmaf(-a1, q1, fmaf(-a2, q2, fmaf(-a3, q3, v[mm])));
+          q3 = q2;
+          q2 = q1;
+          q1 = yt;
+          if (mm < U) ys[mm < nv ? yidx(t0 + mm) : Lay::YS - 1] = yt;  // rows past nrows go to a spare slot
+        }
+      }
+    } else
     // y[ylo + i] = sum_j h[j + J] x[cut + ylo + i - j] = sum_k h[k] xs[i + 2J - k]
     if (tid * U < it.nrows) {
       float h[K];
@@ -421,8 +606,7 @@ __global__ void __launch_bounds__(kFirThreads, J <= 32 ? 2 : 1)
       const int t0 = yoff + tid * U;
       const int nv = it.nrows - tid * U;
 #pragma unroll
-      for (int g = 0; g < U; g++)
-        if (g < nv) ys[yidx(t0 + g)] = acc[g];
+      for (int g = 0; g < U; g++) ys[g < nv ? yidx(t0 + g) : Lay::YS - 1] = acc[g];  // spare slot past nrows
     }
     __syncthreads();
     // blocks whose last row lies in [s0, s0 + S) (the last segment: >= s0)
@@ -490,34 +674,34 @@ __global__ void __launch_bounds__(kFirThreads, J <= 32 ? 2 : 1)
   }
 }
 
-template <int J, int U, int G>
+template <int J, int U, int G, int IW>
 static int launch_fir_t(const FirArgs& a, const FoldArgs& fa, cudaStream_t s) {
   constexpr int O = 2 * G;
-  using Lay = FirLayout<J, U, O>;
+  using Lay = FirLayout<J, U, O, IW>;
   const int S = Lay::R - 4 * O;
   const int nseg = std::max(1, (a.acclen + S - 1) / S);
   const int64_t nitems = (int64_t)nseg * a.P * a.ninputs;
   AB_CHECK_ARG(nitems < (1LL << 31), "FIR time stage: too many work items");
   AB_CHECK_ARG(((uintptr_t)fa.W & 15) == 0 && (a.P % 4) == 0, "FIR time stage: W must be 16-byte aligned");
   const size_t smem = Lay::bytes();
-  AB_CUDA(cudaFuncSetAttribute(fir_fold_kernel<J, U, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  const int per_sm = J <= 32 ? 2 : 1;
+  AB_CUDA(cudaFuncSetAttribute(fir_fold_kernel<J, U, G, IW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const int per_sm = (IW > 0 && IW <= 40) || (IW == 0 && J <= 32) ? 2 : 1;
   const int64_t grid = std::min<int64_t>(nitems, (int64_t)per_sm * std::max(a.num_sms, 1));
-  fir_fold_kernel<J, U, G><<<(unsigned)grid, kFirThreads, smem, s>>>(a.data, a.ld, a.P, a.nslice, a.cut, a.acclen, S,
+  fir_fold_kernel<J, U, G, IW><<<(unsigned)grid, kFirThreads, smem, s>>>(a.data, a.ld, a.P, a.nslice, a.cut, a.acclen, S,
                                                                      nseg, (int)nitems, a.taps, fa, a.state_in,
                                                                      a.state_out);
   AB_LAUNCH_CHECK();
   return AB_OK;
 }
 
-template <int J, int U>
+template <int J, int U, int IW>
 static int launch_fir_o(const FirArgs& a, const FoldArgs& fa, cudaStream_t s) {
   switch (fa.O) {
-    case 4: return launch_fir_t<J, U, 2>(a, fa, s);
-    case 8: return launch_fir_t<J, U, 4>(a, fa, s);
-    case 16: return launch_fir_t<J, U, 8>(a, fa, s);
-    case 32: return launch_fir_t<J, U, 16>(a, fa, s);
-    case 64: return launch_fir_t<J, U, 32>(a, fa, s);
+    case 4: return launch_fir_t<J, U, 2, IW>(a, fa, s);
+    case 8: return launch_fir_t<J, U, 4, IW>(a, fa, s);
+    case 16: return launch_fir_t<J, U, 8, IW>(a, fa, s);
+    case 32: return launch_fir_t<J, U, 16, IW>(a, fa, s);
+    case 64: return launch_fir_t<J, U, 32, IW>(a, fa, s);
     default:
       set_error("FIR time stage: osamp %d not supported (4..64)", fa.O);
       return AB_ERR_UNSUPPORTED;
@@ -530,11 +714,13 @@ int launch_fir_fold(const FirArgs& a, const FoldArgs& fa, cudaStream_t s) {
   AB_CHECK_ARG(a.row_tile == 16 || a.row_tile == 32, "FIR time stage: row tile must be 16 or 32");
   AB_CHECK_ARG(a.num_sms > 0, "FIR time stage: SM count unknown");
   AB_CHECK_ARG(a.row_tile * kFirThreads > 4 * fa.O, "FIR time stage: row tile too small for osamp %d", fa.O);
-  // odd row tiles (33, 17 rows per thread) keep the FIR's shared loads
-  // conflict-free without padding
-  if (a.J == 32) return a.row_tile == 32 ? launch_fir_o<32, 33>(a, fa, s) : launch_fir_o<32, 17>(a, fa, s);
-  if (a.J == 64) return a.row_tile == 32 ? launch_fir_o<64, 33>(a, fa, s) : launch_fir_o<64, 17>(a, fa, s);
-  set_error("FIR time stage: J = %d not supported", a.J);
+  // odd row tiles (33, 17 rows per thread) keep the shared loads conflict-free
+  // without padding
+  if (a.iir_w == 40) return a.row_tile == 32 ? launch_fir_o<0, 33, 40>(a, fa, s) : launch_fir_o<0, 17, 40>(a, fa, s);
+  if (a.iir_w == 80) return launch_fir_o<0, 17, 80>(a, fa, s);
+  if (a.J == 32) return a.row_tile == 32 ? launch_fir_o<32, 33, 0>(a, fa, s) : launch_fir_o<32, 17, 0>(a, fa, s);
+  if (a.J == 64) return a.row_tile == 32 ? launch_fir_o<64, 33, 0>(a, fa, s) : launch_fir_o<64, 17, 0>(a, fa, s);
+  set_error("FIR time stage: J = %d / IW = %d not supported", a.J, a.iir_w);
   return AB_ERR_UNSUPPORTED;
 }
 

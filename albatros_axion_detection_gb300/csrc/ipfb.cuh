@@ -75,17 +75,23 @@ int launch_time_fold(ab_ctx* ctx, float* buf, int64_t ld, int ninputs, int P, in
 // time stage must run).  Cached in ctx per (P, nslice, ntap, thresh).
 int get_fir_taps(ab_ctx* ctx, int P, int N, int ntap, float thresh, int* J, const float** taps);
 
+// IIR form (fir.cu): per-column (w0..w3, a1..a3, g), (P, 8) float, and the
+// warm-up IW (40 or 80; 0 when the factorisation or warm-up fails).  Cached
+// in ctx per (P, ntap, thresh); ntap must be 4.
+int get_iir_coeffs(ab_ctx* ctx, int P, int ntap, float thresh, int* IW, const float** coef);
+
 struct FirArgs {
   const float* data;      // [n][t] window columns, column stride ld
   int64_t ld;
   int P, ninputs, nslice, cut, acclen;
-  const float* taps;
-  int J;                  // 32 or 64
+  const float* taps;      // FIR taps (P, 2J+1) or IIR coefficients (P, 8)
+  int J;                  // FIR: 32 or 64 (ignored when iir_w > 0)
   int row_tile;           // kept rows per thread: 16 or 32
   const float* state_in;  // previous chunk's last 4*O rows (ninputs, P, 4*O)
   float* state_out;       // this chunk's last 4*O rows (the other buffer)
   const float2* tw64;
   int num_sms;            // persistent grid: CTAs per SM x num_sms
+  int iir_w;              // > 0: IIR form with this warm-up
 };
 // Per-device constants of the FIR time stage (call once per device).
 int fir_init_device();

@@ -346,6 +346,90 @@ __global__ void __launch_bounds__(kBSThreads, 2)
   }
 }
 
+// Stage B for a band [u0, u1) of coarse channels (P = 4096, O >= 2): one CTA
+// per (slot c, block, input), one transform per slot for c >= 1.  With
+// z[n] = W_c[n] w_L^{c n} (w_L = exp(-2 pi i / L)), the input of the fine
+// offset O - c is conj(W_c[n]) w_L^{(O-c) n} = conj(z[n]) w_P^{n}, whose DFT is
+// conj(Z[P - 1 - u]): so Y[O u + c] = Z[u] and Y[O u + O - c] = conj(Z[P-1-u]),
+// the band and its mirror image taken from the same transform (the spectrum
+// of the real PFB block is Hermitian).  Slot 0 carries the real W_0 and
+// W_{O/2} and takes two transforms.  Only the needed outputs of the last
+// radix-16 pass are formed: X[u] = sum_m buf[g(u) + m] w16^(m (u / 256)) with
+// g(u) = (u % 16) * 256 + ((u / 16) % 16) * 16 (that pass has no twiddles),
+// 16 lanes per channel summed by shuffles.
+constexpr int kBandThreads = 256;
+__host__ __device__ inline size_t stage_band_smem() {
+  return sizeof(float2) * ((size_t)padded_len(4096) + 1024 + 16);
+}
+
+__device__ __forceinline__ void band_outputs(const float2* buf, const float2* w16, int u0, int nu, bool mirror, int s,
+                                             int O, float2* __restrict__ ob, int tid) {
+  constexpr int P = 4096;
+  const int l16 = tid & 15, grp = tid >> 4;  // 16 groups of 16 lanes
+  const int nu16 = (nu + 15) & ~15;
+  for (int i = grp; i < nu16; i += kBandThreads / 16) {
+    const int ub = u0 + min(i, nu - 1);
+    const int u = mirror ? P - 1 - ub : ub;
+    const int g = (u & 15) * 256 + ((u >> 4) & 15) * 16;
+    float2 p = cmul(buf[pidx(g) + l16], w16[(l16 * (u >> 8)) & 15]);
+#pragma unroll
+    for (int off = 8; off >= 1; off >>= 1) {
+      p.x += __shfl_xor_sync(0xffffffffu, p.x, off);
+      p.y += __shfl_xor_sync(0xffffffffu, p.y, off);
+    }
+    if (l16 == 0 && i < nu) ob[(int64_t)i * O + s] = mirror ? cconj(p) : p;
+  }
+}
+
+__global__ void __launch_bounds__(kBandThreads, 3)
+    pfb_stage_band_kernel(const float* __restrict__ W, int O, int64_t nb, const float2* __restrict__ twL,
+                          const float2* __restrict__ tws, int u0, int u1, float2* __restrict__ out) {
+  constexpr int P = 4096, PER = P / kBandThreads;
+  extern __shared__ float2 sm2[];
+  float2* buf = sm2;
+  float2* vtw = buf + padded_len(P);  // hi[512], lo[512]: exp(-2 pi i e / L)
+  float2* w16 = vtw + 1024;           // exp(-2 pi i m / 16)
+  const int GW = O < 8 ? O : 8, NG = O / GW;
+  const int c = blockIdx.x;
+  const int64_t b = blockIdx.y;
+  const int in = blockIdx.z;
+  const int L = P * O;
+  const int tid = threadIdx.x;
+  const int nhi = (L + 511) / 512;
+  for (int i = tid; i < nhi; i += kBandThreads) vtw[i] = __ldg(&twL[(int64_t)i * 512]);
+  for (int i = tid; i < 512; i += kBandThreads) vtw[512 + i] = i < L ? __ldg(&twL[i]) : make_float2(1.f, 0.f);
+  if (tid < 16) w16[tid] = __ldg(&twL[(int64_t)tid * (L / 16)]);
+  // W_c of sample phase n at src + n * GW
+  const int g = (2 * c) / GW, e = (2 * c) % GW;
+  const float* src = W + ((((int64_t)in * nb + b) * NG + g) * P) * GW + e;
+  const int nu = u1 - u0;
+  float2* ob = out + ((int64_t)in * nb + b) * ((int64_t)nu * O);
+  __syncthreads();
+  const int ntr = (c == 0) ? 2 : 1;
+  for (int h = 0; h < ntr; h++) {
+    const int s = (c == 0) ? (h ? O / 2 : 0) : c;
+#pragma unroll 4
+    for (int q = 0; q < PER; q++) {
+      const int n = tid + q * kBandThreads;
+      const float2 wq = __ldg(reinterpret_cast<const float2*>(src + (size_t)n * GW));
+      float2 x = (c == 0) ? make_float2(h ? wq.y : wq.x, 0.f) : wq;
+      if (s) {
+        const int ex = s * n;
+        x = cmul(x, cmul(vtw[ex >> 9], vtw[512 + (ex & 511)]));
+      }
+      buf[pidx(n)] = x;
+    }
+    __syncthreads();
+    spass<16, 256, 4096, kBandThreads, false>(buf, tws + Plan4096::tw_off(0), tid);
+    __syncthreads();
+    spass<16, 16, 4096, kBandThreads, false>(buf, tws + Plan4096::tw_off(1), tid);
+    __syncthreads();
+    band_outputs(buf, w16, u0, nu, false, s, O, ob, tid);
+    if (c != 0) band_outputs(buf, w16, u0, nu, true, O - c, O, ob, tid);
+    __syncthreads();
+  }
+}
+
 int launch_pfb_stage_a(const TsSrc& src, int ninputs, int P, int O, int ntap, int64_t row0, int64_t nb,
                        const float* win, float* W, const float2* tw64, cudaStream_t s) {
   AB_CHECK_ARG(P % kFoldCols == 0, "pfb: lblock/osamp %d must be a multiple of %d", P, kFoldCols);
@@ -388,7 +472,14 @@ int launch_pfb_stage_b(ab_ctx* ctx, const float* W, int ninputs, int P, int O, i
   size_t smem = sizeof(float) * (size_t)P * GW + sizeof(float2) * ((size_t)padded_len(P) + smem_tw_len(P * O));
   AB_CHECK_ARG(smem <= 220 * 1024, "pfb: stage B needs %zu bytes of shared memory", smem);
   dim3 grid((unsigned)nb, (unsigned)(O / GW), (unsigned)ninputs);
-  if (P == Plan4096::N && O >= 2 && nb <= 65535) {
+  if (P == Plan4096::N && O >= 2 && nb <= 65535 && u1 >= 0) {
+    const float2* tws;
+    AB_TRY(get_twiddle_stream(ctx, P, {16, 16, 16}, &tws));
+    size_t sm = stage_band_smem();
+    AB_CUDA(cudaFuncSetAttribute(pfb_stage_band_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    dim3 g2((unsigned)(O / 2), (unsigned)nb, (unsigned)ninputs);
+    pfb_stage_band_kernel<<<g2, kBandThreads, sm, s>>>(W, O, nb, twL, tws, u0, u1, out);
+  } else if (P == Plan4096::N && O >= 2 && nb <= 65535) {
     const float2* tws;
     AB_TRY(get_twiddle_stream(ctx, P, {16, 16, 16}, &tws));
     size_t sm = stage_bslot_smem();

@@ -142,6 +142,13 @@ class StreamCorrelator:
         """Half-length J of the FIR time stage (0: the FFT time stage runs)."""
         return int(_lib.load().ab_stream_fir_taps(self._h))
 
+    def time_filter(self):
+        """("fft", 0), ("fir", J) or ("iir", warm-up samples): the form of the
+        IPFB time stage this stream runs."""
+        kind, param = ctypes.c_int32(), ctypes.c_int32()
+        _lib.call("ab_stream_time_filter", self._h, ctypes.byref(kind), ctypes.byref(param))
+        return ("fft", "fir", "iir")[kind.value], int(param.value)
+
     def workspace_bytes(self) -> int:
         """Bytes of per-push scratch this stream can take from a shared
         workspace (-1: it keeps state there and cannot share)."""

@@ -121,10 +121,10 @@ def stage_bytes(sc):
     M, nslice, nq = 2 * NANT, ACCLEN + 2 * CUT, sc.nq
     nb = ACCLEN // OSAMP
     L = P * OSAMP
-    J = sc.fir_taps()
+    kind, par = sc.time_filter()
     # rows of each IPFB column the time stage must read: all nslice for the
-    # FFT form, the kept rows plus the FIR half-lengths for the FIR form
-    rows_in = nslice if J == 0 else ACCLEN + 2 * J
+    # FFT form, the kept rows plus the filter's halo for the FIR/IIR forms
+    rows_in = {"fft": nslice, "fir": ACCLEN + 2 * par, "iir": ACCLEN + 2 * par + 3}[kind]
     return {
         "row_ifft": NANT * nslice * 2 * NCHAN_RAW + M * P * nslice * 4,      # packets in, f32 rows out
         # time-axis deconvolution with the PFB fold fused in: IPFB column in,
@@ -173,7 +173,7 @@ def run_ours(args):
     raw = synth_raw(torch, dev)
     if args.time_filter != "default":
         from albatros_axion_detection_gb300 import autotune
-        autotune.set_time_filter({"fir": 0, "fft": 1}[args.time_filter], args.row_tile)
+        autotune.set_time_filter({"iir": 0, "fir": 3, "fft": 1}[args.time_filter], args.row_tile)
     sc = stream.StreamCorrelator(NANT, channels, 0, NCHAN_RAW, ACCLEN, NSPEC // ACCLEN, NBLOCK, OSAMP, CUT, THRESH,
                                  NTAP, nchan_raw=NCHAN_RAW)
     nchunks = NSPEC // ACCLEN
@@ -264,7 +264,7 @@ def run_ours(args):
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded Gaussian 4-bit packets)",
             "config": {"workload": WORKLOAD, "spectra_per_step": spectra_per_step, "chunks_per_step": nchunks,
-                       "time_stage": f"FIR J={sc.fir_taps()}" if sc.fir_taps() else "FFT",
+                       "time_stage": "%s %d" % sc.time_filter(),
                        "parallelism": f"replicas x{world}",
                        "l2": "inputs larger than L2 (256 MiB packets, 2 x 4.3 GB IPFB intermediates per step)"},
             "e2e": {"value": world * spectra_per_step / (ms_e2e / 1e3), "unit": "spectra/s",
@@ -423,7 +423,7 @@ def main():
     ap.add_argument("--workload", default="stream", choices=["stream", "uneven-batch"],
                     help="stream: the 2-antenna 2^20-spectrum chain (default); uneven-batch: 24 mixed files")
     ap.add_argument("--lanes", type=int, default=4, help="uneven-batch: concurrent CUDA streams")
-    ap.add_argument("--time-filter", default="default", choices=["default", "fir", "fft"],
+    ap.add_argument("--time-filter", default="default", choices=["default", "iir", "fir", "fft"],
                     help="stream: IPFB time stage form (default: the library's choice)")
     ap.add_argument("--row-tile", type=int, default=0, help="stream: FIR rows per thread (16 or 32)")
     ap.add_argument("--check", action="store_true", help="uneven-batch: job-0 error of every file vs the FP64 oracle")

@@ -50,13 +50,18 @@ int ab_ctx_destroy(ab_ctx *ctx);
  * length.  No reference counterpart: the reference delegates FFT planning to
  * cuFFT (albatros_analysis/src/utils/pycufft.cu:201-303). */
 int ab_ctx_set_fft_plan(ab_ctx *ctx, int64_t n, const int32_t *radices, int64_t npass);
-/* Time-axis deconvolution of streams created after this call.  The FIR form
- * is a (2J+1)-tap FIR of the reference's Wiener filter (J = 32 or 64, taps
- * from the FP64 filter at the same nslice bins), usable when the dropped tail
- * is below 1e-7 of the filter norm and the PFB fold is fused (osamp >= 4,
- * ntap = 4); it runs any nslice.  The FFT form needs nslice/2 to factor into
- * 2,3,5,7.  mode 0 (default): FIR where usable, else FFT; mode 1: FFT only;
- * mode 2: FFT where it runs, else FIR.
+/* Time-axis deconvolution of streams created after this call.  Three forms
+ * compute the reference's circular Wiener deconvolution:
+ *  - IIR: the filter W(z)(1+t^2)/D(z) factored (FP64, Wilson's spectral
+ *    factorisation) into a 4-tap FIR and causal + anti-causal 3-pole
+ *    recursions, warmed up over 40 or 80 samples; usable when the
+ *    factorisation converges and the poles decay fast enough;
+ *  - FIR: a (2J+1)-tap FIR (J = 32 or 64, taps of the FP64 filter at the same
+ *    nslice bins), usable when the dropped tail is below 1e-7 of the norm;
+ *  - FFT: nslice-point transforms (nslice/2 must factor into 2,3,5,7).
+ * IIR and FIR need the fused PFB fold (osamp >= 4, ntap = 4) and run any
+ * nslice.  mode 0 (default): IIR, else FIR, else FFT; mode 1: FFT only;
+ * mode 2: FFT where it runs, else IIR/FIR; mode 3: FIR, else FFT.
  * row_tile: kept rows per thread of the FIR stage (16 or 32; 0 keeps the
  * current value), taken by streams created after the call.  No reference counterpart: the reference
  * always filters with cuFFT (albatros_analysis/src/utils/pfb_gpu_utils.py:56-91). */
@@ -253,9 +258,11 @@ int64_t ab_stream_kernel_launches(const ab_stream *st);
  * stream's own scratch (after a device synchronise) and uses ws (device,
  * 256-byte aligned, caller-owned, alive until the stream is destroyed).
  * Pushes of streams sharing a workspace must not overlap in time. */
-/* Half-length J of the FIR time stage this stream runs (0: the FFT time
- * stage). */
+/* Half-length J of the FIR time stage this stream runs (0: another form). */
 int64_t ab_stream_fir_taps(const ab_stream *st);
+/* Time stage form of this stream: kind 0 = FFT, 1 = FIR (param = J),
+ * 2 = IIR (param = warm-up samples). */
+int ab_stream_time_filter(const ab_stream *st, int32_t *kind, int32_t *param);
 int64_t ab_stream_workspace_bytes(const ab_stream *st);
 int ab_stream_set_workspace(ab_stream *st, void *ws, int64_t bytes);
 

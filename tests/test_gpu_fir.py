@@ -1,9 +1,9 @@
-"""GPU tests of the FIR form of the IPFB time stage (csrc/fir.cu): it is
-chosen for the default Wiener threshold, agrees with the FFT form and the FP64
-oracle, reproduces the reference's circular wrap when cut is below the FIR
-half-length (including the reference's default cut = 10, whose nslice has no
-fast FFT), and gives way to the FFT form for thresholds whose filter decays
-too slowly."""
+"""GPU tests of the IIR and FIR forms of the IPFB time stage (csrc/fir.cu):
+the IIR form is chosen for the default Wiener threshold, the FIR form when
+asked for; both agree with the FFT form and the FP64 oracle, reproduce the
+reference's circular wrap when cut is below the filter's reach (including the
+reference's default cut = 10, whose nslice has no fast FFT), and give way to
+the FFT form for thresholds whose filter decays too slowly."""
 import numpy as np
 import pytest
 import torch
@@ -15,7 +15,10 @@ from tests.test_gpu_stream import check
 pytestmark = pytest.mark.gpu
 
 
-def stream_vis(raw_np, channels, mode=0, row_tile=32, thresh=0.45, bits=4, **kw):
+FIR, IIR, FFT = 3, 0, 1  # time-filter modes
+
+
+def stream_vis(raw_np, channels, mode=FIR, row_tile=32, thresh=0.45, bits=4, **kw):
     from albatros_axion_detection_gb300 import autotune, stream
     autotune.set_time_filter(mode, row_tile)
     try:
@@ -28,7 +31,7 @@ def stream_vis(raw_np, channels, mode=0, row_tile=32, thresh=0.45, bits=4, **kw)
         raw = torch.from_numpy(raw_np).cuda()
         for j in range(kw["nchunks"]):
             sc.push(raw, j, final=(j == kw["nchunks"] - 1))
-        return sc.vis_device().permute(1, 2, 3, 0).cpu().numpy(), sc.fir_taps()
+        return sc.vis_device().permute(1, 2, 3, 0).cpu().numpy(), sc.time_filter()
     finally:
         sc.close()
 
@@ -40,29 +43,38 @@ def test_fir_chosen_and_matches_fft_and_oracle():
     raw = gen.raw_4bit(seed=21, nspec=3 * 1024, nchan=8, nant=2)
     ch = np.arange(600, 608)
     ref, _ = po.repfb_xcorr_avg(raw, ch, **CFG)
-    v_fir, J = stream_vis(raw, ch, mode=0, **CFG)
-    v_fft, J0 = stream_vis(raw, ch, mode=1, **CFG)
-    assert J == 32 and J0 == 0
-    check(v_fir, ref)
-    check(v_fft, ref)
+    v_fir, tf = stream_vis(raw, ch, mode=FIR, **CFG)
+    v_iir, ti = stream_vis(raw, ch, mode=IIR, **CFG)
+    v_fft, t0 = stream_vis(raw, ch, mode=FFT, **CFG)
+    assert tf == ("fir", 32) and ti == ("iir", 40) and t0 == ("fft", 0)
+    for v in (v_fir, v_iir, v_fft):
+        check(v, ref)
     assert np.linalg.norm(v_fir - v_fft) / np.linalg.norm(v_fft) < 2e-6
+    assert np.linalg.norm(v_iir - v_fft) / np.linalg.norm(v_fft) < 2e-6
 
 
-def test_fir_row_tiles_agree_bitwise():
+@pytest.mark.parametrize("mode", [FIR, IIR])
+def test_row_tiles_agree(mode):
+    """Row tiles 33 and 17: the FIR sums are identical term by term (bitwise);
+    the IIR warm-up starts at different rows, so equal to rounding."""
     raw = gen.raw_4bit(seed=22, nspec=3 * 1024, nchan=8, nant=1)
     ch = np.arange(100, 108)
     cfg = dict(CFG, osamp=64, nblock=16)
-    a, _ = stream_vis(raw, ch, row_tile=32, **cfg)
-    b, _ = stream_vis(raw, ch, row_tile=16, **cfg)
-    assert np.array_equal(a, b)
+    a, _ = stream_vis(raw, ch, mode=mode, row_tile=32, **cfg)
+    b, _ = stream_vis(raw, ch, mode=mode, row_tile=16, **cfg)
+    if mode == FIR:
+        assert np.array_equal(a, b)
+    else:
+        assert np.linalg.norm(a - b) / np.linalg.norm(a) < 1e-6
 
 
+@pytest.mark.parametrize("mode", [FIR, IIR])
 @pytest.mark.parametrize("acclen,cut,osamp,nchunks,bits", [
-    (1024, 10, 16, 3, 4),   # the reference's default cut: nslice 1044 = 4*9*29, FIR only; wrap inside kept rows
-    (512, 8, 4, 4, 4),      # cut < J with 4*osamp = 16
+    (1024, 10, 16, 3, 4),   # the reference's default cut: nslice 1044 = 4*9*29, no FFT form; wrap inside kept rows
+    (512, 8, 4, 4, 4),      # cut below the filter's reach with 4*osamp = 16
     (1024, 10, 64, 3, 1),   # 1-bit packets, osamp 64
 ])
-def test_fir_circular_wrap_small_cut(acclen, cut, osamp, nchunks, bits):
+def test_circular_wrap_small_cut(acclen, cut, osamp, nchunks, bits, mode):
     nch = 8
     if bits == 4:
         raw = gen.raw_4bit(seed=acclen + cut, nspec=nchunks * acclen, nchan=nch, nant=2)
@@ -73,17 +85,18 @@ def test_fir_circular_wrap_small_cut(acclen, cut, osamp, nchunks, bits):
     kw = dict(acclen=acclen, nchunks=nchunks, nblock=max(acclen // osamp, 1), chanstart=0, chanend=nch,
               osamp=osamp, cut=cut)
     ref, _ = po.repfb_xcorr_avg(raw, ch, bits=bits, **kw)
-    v, J = stream_vis(raw, ch, bits=bits, **kw)
-    assert J == 32
+    v, tf = stream_vis(raw, ch, mode=mode, bits=bits, **kw)
+    assert tf == (("fir", 32) if mode == FIR else ("iir", 40))
     check(v, ref)
 
 
-def test_threshold_02_uses_long_fir():
+@pytest.mark.parametrize("mode,expect", [(FIR, ("fir", 64)), (IIR, ("iir", 80))])
+def test_threshold_02_uses_longer_filters(mode, expect):
     raw = gen.raw_4bit(seed=24, nspec=3 * 1024, nchan=8, nant=1)
     ch = np.arange(310, 318)
     ref, _ = po.repfb_xcorr_avg(raw, ch, filt_thresh=0.2, **CFG)
-    v, J = stream_vis(raw, ch, thresh=0.2, **CFG)
-    assert J == 64  # 0.2 needs 64 taps a side
+    v, tf = stream_vis(raw, ch, mode=mode, thresh=0.2, **CFG)
+    assert tf == expect  # 0.2: 64 taps a side, or an 80-sample warm-up
     check(v, ref)
 
 
@@ -91,9 +104,10 @@ def test_small_threshold_uses_fft_stage():
     raw = gen.raw_4bit(seed=23, nspec=3 * 1024, nchan=8, nant=1)
     ch = np.arange(300, 308)
     ref, _ = po.repfb_xcorr_avg(raw, ch, filt_thresh=0.1, **CFG)
-    v, J = stream_vis(raw, ch, thresh=0.1, **CFG)
-    assert J == 0  # the thresh 0.1 filter needs more than 64 taps a side
-    check(v, ref)
+    for mode in (FIR, IIR):
+        v, tf = stream_vis(raw, ch, mode=mode, thresh=0.1, **CFG)
+        assert tf == ("fft", 0)  # the thresh 0.1 filter decays too slowly for either
+        check(v, ref)
 
 
 def test_time_stage_tuner(tmp_path, monkeypatch):
@@ -110,8 +124,9 @@ def test_time_stage_tuner(tmp_path, monkeypatch):
         autotune.set_plan(576, None)
 
 
+@pytest.mark.parametrize("mode", [FIR, IIR])
 @pytest.mark.parametrize("osamp,row_tile", [(64, 16), (64, 32), (4, 16)])
-def test_fir_multi_segment_columns(osamp, row_tile):
+def test_multi_segment_columns(osamp, row_tile, mode):
     """acclen 8192 spans 2-3 segments per column (a segment holds
     row_tile*256 - 4*osamp new rows): blocks across segment edges and the
     tail state handed between chunks must match the oracle."""
@@ -121,6 +136,6 @@ def test_fir_multi_segment_columns(osamp, row_tile):
     kw = dict(acclen=acclen, nchunks=nchunks, nblock=acclen // osamp // 2, chanstart=0, chanend=4, osamp=osamp,
               cut=64)
     ref, _ = po.repfb_xcorr_avg(raw, ch, **kw)
-    v, J = stream_vis(raw, ch, row_tile=row_tile, **kw)
-    assert J == 32
+    v, tf = stream_vis(raw, ch, mode=mode, row_tile=row_tile, **kw)
+    assert tf[0] == ("fir" if mode == FIR else "iir")
     check(v, ref)

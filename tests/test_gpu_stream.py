@@ -89,7 +89,7 @@ def test_stream_rejects_bad_config():
     from albatros_axion_detection_gb300._lib import AlbatrosError
     # nslice/2 = 261 = 9*29: only the FIR time stage can run it
     sc = stream.StreamCorrelator(1, np.arange(8), 0, 8, acclen=500, nchunks=2, nblock=4, osamp=4, cut=11)
-    assert sc.fir_taps() == 32
+    assert sc.time_filter() == ("iir", 40)
     sc.close()
     autotune.set_time_filter(1)
     try:
