@@ -25,6 +25,7 @@ SIGNATURES = {
     "ab_ctx_destroy": (I32, [P]),
     "ab_ctx_set_fft_plan": (I32, [P, I64, P, I64]),
     "ab_ctx_set_time_filter": (I32, [P, I32, I32]),
+    "ab_ctx_set_option": (I32, [P, I32, I32]),
     "ab_unpack_4bit": (I32, [P, P, P, I64, I64, P, I64, I64, P]),
     "ab_unpack_4bit_range": (I32, [P, P, P, I64, I64, I64, I64, I64, P]),
     "ab_unpack_1bit": (I32, [P, P, P, I64, I64, P, I64, I64, P]),

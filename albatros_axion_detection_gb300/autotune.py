@@ -132,6 +132,14 @@ def set_time_filter(mode: int = DEFAULT_MODE, row_tile: int = 0, device: Optiona
         _filter_setting["row_tile"] = int(row_tile)
 
 
+OPT_ROW_FFTS_PER_CTA = 1
+
+
+def set_row_ffts_per_cta(n: int, device: Optional[int] = None) -> None:
+    """Spectra per CTA of the streaming row stage (4 or 2)."""
+    _lib.call("ab_ctx_set_option", _lib.ctx(device), OPT_ROW_FFTS_PER_CTA, int(n))
+
+
 def _time_chain(acclen: int, cut: int, osamp: int, nchunks: int = 2, reps: int = 2, mode: int = 0,
                 row_tile: int = 32) -> Tuple[float, Tuple[str, int]]:
     """(ms per launch of the chain's time stage for one antenna, the form that

@@ -290,6 +290,20 @@ int ab_ctx_set_time_filter(ab_ctx* ctx, int32_t mode, int32_t row_tile) {
   return AB_OK;
 }
 
+int ab_ctx_set_option(ab_ctx* ctx, int32_t option, int32_t value) {
+  AB_CHECK_ARG(ctx, "ab_ctx_set_option: NULL context");
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  switch (option) {
+    case AB_OPT_ROW_FFTS_PER_CTA:
+      AB_CHECK_ARG(value == 2 || value == 4, "ab_ctx_set_option: row FFTs per CTA must be 2 or 4");
+      ctx->row_ffts_per_cta = value;
+      return AB_OK;
+    default:
+      ab::set_error("ab_ctx_set_option: unknown option %d", option);
+      return AB_ERR_ARG;
+  }
+}
+
 int ab_ctx_destroy(ab_ctx* ctx) {
   if (!ctx) return AB_OK;
   cudaSetDevice(ctx->device);

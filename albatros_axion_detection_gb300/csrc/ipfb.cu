@@ -81,8 +81,8 @@ constexpr int kRowThreadsPerFft = 256;
 
 // shared memory of a row-stage CTA: kRowFftsPerCta padded P-point buffers,
 // then the twiddle tables of T = P
-__host__ __device__ inline size_t row_smem_bytes(int P) {
-  return sizeof(float2) * ((size_t)padded_len(P) * kRowFftsPerCta + smem_tw_len(P));
+__host__ __device__ inline size_t row_smem_bytes(int P, int fpc = kRowFftsPerCta) {
+  return sizeof(float2) * ((size_t)padded_len(P) * fpc + smem_tw_len(P));
 }
 
 __device__ __forceinline__ float dec4f(unsigned v) { return (float)((int)((v + 7u) & 15u) - 7); }
@@ -120,23 +120,25 @@ __device__ __forceinline__ void put_pair_t(float2* buf, const FftPlan& p, int P,
   }
 }
 
-// grid: (ceil(nrows / kRowFftsPerCta), nant); one FFT per spectrum row, both pols.
-template <class PL>
-__global__ void __launch_bounds__(kRowFftsPerCta* kRowThreadsPerFft)
+// grid: (ceil(nrows / FPC), nant); one FFT per spectrum row, both pols, FPC
+// spectra per CTA (4: one 1024-thread CTA per SM; 2: two or three CTAs per SM
+// whose phases interleave, with 8-byte instead of 16-byte column stores).
+template <class PL, int FPC>
+__global__ void __launch_bounds__(FPC* kRowThreadsPerFft, FPC == 4 ? 1 : 2)
     row_stage_packed4_kernel(Packed4Src src, int nrows, FftPlan plan, const float2* __restrict__ tw,
                              const float2* __restrict__ tws, float* __restrict__ out, int64_t ld) {
   extern __shared__ float2 smem[];
   const int P = plan.n, PL_ = padded_len(P);
   const int a = blockIdx.y;
   const int sub = threadIdx.x / kRowThreadsPerFft, ltid = threadIdx.x % kRowThreadsPerFft;
-  const int t = blockIdx.x * kRowFftsPerCta + sub;
+  const int t = blockIdx.x * FPC + sub;
   float2* buf = smem + (size_t)sub * PL_;
   SmemTw tws_s{nullptr, nullptr};
   if constexpr (std::is_same<PL, NoPlan>::value)
-    tws_s = load_smem_tw(smem + (size_t)kRowFftsPerCta * PL_, tw, P, threadIdx.x, blockDim.x);
+    tws_s = load_smem_tw(smem + (size_t)FPC * PL_, tw, P, threadIdx.x, blockDim.x);
   {
     float4* b4 = reinterpret_cast<float4*>(smem);  // zero all buffers (PL_ * FFTS float2, even count)
-    const int n4 = (kRowFftsPerCta * PL_) / 2;
+    const int n4 = (FPC * PL_) / 2;
     for (int i = threadIdx.x; i < n4; i += blockDim.x) b4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
   }
   __syncthreads();
@@ -168,9 +170,9 @@ __global__ void __launch_bounds__(kRowFftsPerCta* kRowThreadsPerFft)
   // write: column n of input (2a+p) at rows t0..t0+3 (one 16-byte store per
   // column and pol when the rows are 16-byte aligned)
   const float inv = 1.0f / (float)P;
-  const int nthr = kRowFftsPerCta * kRowThreadsPerFft;
-  const int64_t t0 = (int64_t)blockIdx.x * kRowFftsPerCta;
-  if (kRowFftsPerCta == 4 && ld % 4 == 0 && t0 + 4 <= nrows && ((uintptr_t)out & 15) == 0) {
+  const int nthr = FPC * kRowThreadsPerFft;
+  const int64_t t0 = (int64_t)blockIdx.x * FPC;
+  if (FPC == 4 && ld % 4 == 0 && t0 + 4 <= nrows && ((uintptr_t)out & 15) == 0) {
     for (int n = threadIdx.x; n < P; n += nthr) {
       float2 z0 = smem[pidx(n)], z1 = smem[(size_t)PL_ + pidx(n)];
       float2 z2 = smem[(size_t)2 * PL_ + pidx(n)], z3 = smem[(size_t)3 * PL_ + pidx(n)];
@@ -179,9 +181,16 @@ __global__ void __launch_bounds__(kRowFftsPerCta* kRowThreadsPerFft)
       *reinterpret_cast<float4*>(out + ((int64_t)(2 * a + 1) * P + n) * ld + t0) =
           make_float4(z0.y * inv, z1.y * inv, z2.y * inv, z3.y * inv);
     }
+  } else if (FPC == 2 && ld % 2 == 0 && t0 + 2 <= nrows && ((uintptr_t)out & 7) == 0) {
+    for (int n = threadIdx.x; n < P; n += nthr) {
+      float2 z0 = smem[pidx(n)], z1 = smem[(size_t)PL_ + pidx(n)];
+      *reinterpret_cast<float2*>(out + ((int64_t)(2 * a) * P + n) * ld + t0) = make_float2(z0.x * inv, z1.x * inv);
+      *reinterpret_cast<float2*>(out + ((int64_t)(2 * a + 1) * P + n) * ld + t0) =
+          make_float2(z0.y * inv, z1.y * inv);
+    }
   } else {
-    for (int i = threadIdx.x; i < kRowFftsPerCta * P; i += nthr) {
-      int n = i / kRowFftsPerCta, f = i - n * kRowFftsPerCta;
+    for (int i = threadIdx.x; i < FPC * P; i += nthr) {
+      int n = i / FPC, f = i - n * FPC;
       int64_t tt = t0 + f;
       if (tt >= nrows) continue;
       float2 z = smem[(size_t)f * PL_ + pidx(n)];
@@ -362,26 +371,33 @@ static int set_smem_attr(K kernel, size_t bytes) {
   return AB_OK;
 }
 
-int launch_row_stage_packed4(ab_ctx* ctx, const Packed4Src& src, int nant, int nrows, int P, const FftPlan& plan,
-                             const float2* twP, float* out, int64_t ld, cudaStream_t s) {
-  size_t smem = row_smem_bytes(P);
+template <int FPC>
+static int launch_row_packed4_t(ab_ctx* ctx, const Packed4Src& src, int nant, int nrows, int P, const FftPlan& plan,
+                                const float2* twP, float* out, int64_t ld, cudaStream_t s) {
+  size_t smem = row_smem_bytes(P, FPC);
   AB_CHECK_ARG(smem <= ctx->smem_optin, "row stage: lblock %d too large", P);
-  dim3 grid((unsigned)((nrows + kRowFftsPerCta - 1) / kRowFftsPerCta), (unsigned)nant);
+  dim3 grid((unsigned)((nrows + FPC - 1) / FPC), (unsigned)nant);
   bool tuned = false;
   { FftPlan tmp; ctx_plan(ctx, P, &tmp, &tuned); }
   if (P == Plan4096::N && !tuned) {
     const float2* tws;
     AB_TRY(get_twiddle_stream(ctx, P, {16, 16, 16}, &tws));
-    AB_TRY(set_smem_attr(row_stage_packed4_kernel<Plan4096>, smem));
-    row_stage_packed4_kernel<Plan4096><<<grid, kRowFftsPerCta * kRowThreadsPerFft, smem, s>>>(src, nrows, plan, twP,
-                                                                                               tws, out, ld);
+    AB_TRY(set_smem_attr(row_stage_packed4_kernel<Plan4096, FPC>, smem));
+    row_stage_packed4_kernel<Plan4096, FPC><<<grid, FPC * kRowThreadsPerFft, smem, s>>>(src, nrows, plan, twP, tws,
+                                                                                         out, ld);
   } else {
-    AB_TRY(set_smem_attr(row_stage_packed4_kernel<NoPlan>, smem));
-    row_stage_packed4_kernel<NoPlan><<<grid, kRowFftsPerCta * kRowThreadsPerFft, smem, s>>>(src, nrows, plan, twP,
-                                                                                             nullptr, out, ld);
+    AB_TRY(set_smem_attr(row_stage_packed4_kernel<NoPlan, FPC>, smem));
+    row_stage_packed4_kernel<NoPlan, FPC><<<grid, FPC * kRowThreadsPerFft, smem, s>>>(src, nrows, plan, twP, nullptr,
+                                                                                       out, ld);
   }
   AB_LAUNCH_CHECK();
   return AB_OK;
+}
+
+int launch_row_stage_packed4(ab_ctx* ctx, const Packed4Src& src, int nant, int nrows, int P, const FftPlan& plan,
+                             const float2* twP, float* out, int64_t ld, cudaStream_t s) {
+  if (ctx->row_ffts_per_cta == 2) return launch_row_packed4_t<2>(ctx, src, nant, nrows, P, plan, twP, out, ld, s);
+  return launch_row_packed4_t<4>(ctx, src, nant, nrows, P, plan, twP, out, ld, s);
 }
 
 int launch_row_stage_c64(ab_ctx* ctx, const float2* dat, int64_t nslice, int P, const FftPlan& plan,

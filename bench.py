@@ -171,6 +171,9 @@ def run_ours(args):
 
     channels = np.arange(CHAN0, CHAN0 + NCHAN_RAW)
     raw = synth_raw(torch, dev)
+    if args.row_ffts:
+        from albatros_axion_detection_gb300 import autotune
+        autotune.set_row_ffts_per_cta(args.row_ffts)
     if args.time_filter != "default":
         from albatros_axion_detection_gb300 import autotune
         autotune.set_time_filter({"iir": 0, "fir": 3, "fft": 1}[args.time_filter], args.row_tile)
@@ -426,6 +429,7 @@ def main():
     ap.add_argument("--time-filter", default="default", choices=["default", "iir", "fir", "fft"],
                     help="stream: IPFB time stage form (default: the library's choice)")
     ap.add_argument("--row-tile", type=int, default=0, help="stream: FIR rows per thread (16 or 32)")
+    ap.add_argument("--row-ffts", type=int, default=0, help="stream: spectra per row-stage CTA (2 or 4)")
     ap.add_argument("--check", action="store_true", help="uneven-batch: job-0 error of every file vs the FP64 oracle")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -66,6 +66,12 @@ int ab_ctx_set_fft_plan(ab_ctx *ctx, int64_t n, const int32_t *radices, int64_t 
  * current value), taken by streams created after the call.  No reference counterpart: the reference
  * always filters with cuFFT (albatros_analysis/src/utils/pfb_gpu_utils.py:56-91). */
 int ab_ctx_set_time_filter(ab_ctx *ctx, int32_t mode, int32_t row_tile);
+/* Launch-shape options of this context (no reference counterpart; set by the
+ * autotuner, albatros_axion_detection_gb300/autotune.py).
+ * AB_OPT_ROW_FFTS_PER_CTA: spectra per CTA of the streaming row stage, 4
+ * (default) or 2, read at each push. */
+#define AB_OPT_ROW_FFTS_PER_CTA 1
+int ab_ctx_set_option(ab_ctx *ctx, int32_t option, int32_t value);
 
 /* ---- unpacking ----------------------------------------------------------
  * ab_unpack_4bit: replaces unpack_4bit / _unpack_4bit_float_gpu

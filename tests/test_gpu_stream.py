@@ -102,3 +102,21 @@ def test_stream_rejects_bad_config():
         kw.update(bad)
         with pytest.raises((AlbatrosError, ValueError)):
             stream.StreamCorrelator(1, np.arange(8), 0, 8, **kw)
+
+
+@pytest.mark.parametrize("nrows_extra", [0, 1])
+def test_stream_two_spectra_per_row_cta(nrows_extra):
+    """The row stage with 2 spectra per CTA (8-byte column stores, and the
+    scalar tail when nslice is odd) gives the oracle's visibilities."""
+    from albatros_axion_detection_gb300 import autotune
+    acclen, cut = 512 + nrows_extra, 32
+    raw = gen.raw_4bit(seed=77 + nrows_extra, nspec=3 * acclen, nchan=8, nant=2)
+    channels = np.arange(520, 528)
+    kw = dict(acclen=acclen, nchunks=3, nblock=32, chanstart=0, chanend=8, osamp=16, cut=cut)
+    ref, _ = po.repfb_xcorr_avg(raw, channels, **kw)
+    autotune.set_row_ffts_per_cta(2)
+    try:
+        vis, _ = run(raw, channels, **kw)
+    finally:
+        autotune.set_row_ffts_per_cta(4)
+    check(vis, ref)
