@@ -136,7 +136,8 @@ OPT_ROW_FFTS_PER_CTA = 1
 
 
 def set_row_ffts_per_cta(n: int, device: Optional[int] = None) -> None:
-    """Spectra per CTA of the streaming row stage (4 or 2)."""
+    """Spectra per CTA of the streaming row stage: 8 (time-paired, the
+    default), 4 or 2 (pol-paired)."""
     _lib.call("ab_ctx_set_option", _lib.ctx(device), OPT_ROW_FFTS_PER_CTA, int(n))
 
 

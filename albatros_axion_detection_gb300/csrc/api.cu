@@ -295,7 +295,8 @@ int ab_ctx_set_option(ab_ctx* ctx, int32_t option, int32_t value) {
   std::lock_guard<std::mutex> lk(ctx->mu);
   switch (option) {
     case AB_OPT_ROW_FFTS_PER_CTA:
-      AB_CHECK_ARG(value == 2 || value == 4, "ab_ctx_set_option: row FFTs per CTA must be 2 or 4");
+      AB_CHECK_ARG(value == 2 || value == 4 || value == 8,
+                   "ab_ctx_set_option: row stage spectra per CTA must be 8 (time-paired), 4 or 2 (pol-paired)");
       ctx->row_ffts_per_cta = value;
       return AB_OK;
     default:

@@ -80,7 +80,8 @@ struct ab_ctx {
   // 1: always FFT; 2: FFT where it runs, else IIR/FIR; 3: FIR, else FFT
   int time_filter_mode = 0;
   int fir_row_tile = 32;     // kept rows per thread of the FIR time stage
-  int row_ffts_per_cta = 4;  // spectra per CTA of the packed row stage (2 or 4)
+  int row_ffts_per_cta = 8;  // row stage: 8 = time-paired spectra of one input per CTA;
+                             // 4 or 2 = pol-paired spectra of one antenna per CTA
   // grow-only scratch buffers keyed by slot
   std::map<int, std::pair<void*, size_t>> scratch;
   float2* tw64 = nullptr;  // exp(-2 pi i e / 64)

@@ -371,6 +371,100 @@ static int set_smem_attr(K kernel, size_t bytes) {
   return AB_OK;
 }
 
+// Time-paired form: a CTA takes 8 consecutive spectra of ONE input (antenna
+// a, pol p = blockIdx.y % 2) and transforms spectra (t, t+1) together as
+// Z = A_t + i A_{t+1}.  Each column then receives 8 consecutive rows (32 bytes,
+// one full sector), written by two lanes with 16-byte stores, so a warp store
+// covers 16 whole sectors.  (Pairing the two pols of one spectrum instead
+// leaves 16 bytes per column and input, half a sector per lane.)
+template <class PL>
+__global__ void __launch_bounds__(4 * kRowThreadsPerFft)
+    row_stage_tpair_kernel(Packed4Src src, int nrows, FftPlan plan, const float2* __restrict__ tw,
+                           const float2* __restrict__ tws, float* __restrict__ out, int64_t ld) {
+  constexpr int FFTS = 4, ROWS = 2 * FFTS;
+  extern __shared__ float2 smem[];
+  const int P = plan.n, PL_ = padded_len(P);
+  const int in = blockIdx.y, a = in >> 1, pol = in & 1;
+  const int sub = threadIdx.x / kRowThreadsPerFft, ltid = threadIdx.x % kRowThreadsPerFft;
+  const int64_t t0 = (int64_t)blockIdx.x * ROWS;
+  float2* buf = smem + (size_t)sub * PL_;
+  SmemTw tws_s{nullptr, nullptr};
+  if constexpr (std::is_same<PL, NoPlan>::value)
+    tws_s = load_smem_tw(smem + (size_t)FFTS * PL_, tw, P, threadIdx.x, blockDim.x);
+  {
+    float4* b4 = reinterpret_cast<float4*>(smem);  // zero all buffers (PL_ * FFTS float2, even count)
+    const int n4 = (FFTS * PL_) / 2;
+    for (int i = threadIdx.x; i < n4; i += blockDim.x) b4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  __syncthreads();
+  // raw rows of the two spectra of this FFT
+  int64_t rawrow[2] = {-1, -1};
+#pragma unroll
+  for (int e = 0; e < 2; e++) {
+    const int64_t t = t0 + 2 * sub + e;
+    if (t < nrows) {
+      const int64_t g = src.g0 + t;
+      if (g >= 0) rawrow[e] = src.spec_map ? (int64_t)src.spec_map[(int64_t)a * src.map_stride + g] : g;
+    }
+  }
+  if (rawrow[0] >= 0 || rawrow[1] >= 0) {
+    const uint8_t* base = src.raw + (int64_t)a * src.ant_stride;
+    for (int k = ltid; k < src.nsel; k += kRowThreadsPerFft) {
+      const int c = __ldg(&src.chan_cols[k]);
+      float2 v[2];
+#pragma unroll
+      for (int e = 0; e < 2; e++) {
+        v[e] = make_float2(0.f, 0.f);
+        if (rawrow[e] < 0) continue;
+        const uint8_t* row = base + rawrow[e] * src.row_bytes;
+        if (src.bits == 4) {
+          const unsigned b = row[2 * c + pol];
+          v[e] = make_float2(dec4f(b >> 4), dec4f(b & 15u));
+        } else {
+          // 1-bit (unpacking.c:207-246): r0 i0 r1 i1 per channel, set bit = +1
+          const unsigned q = (row[c >> 1] >> ((c & 1) ? 0 : 4)) & 15u;
+          const unsigned sh = pol ? 0u : 2u;
+          v[e] = make_float2((float)(((q >> (sh + 1)) & 1u) * 2) - 1.f, (float)(((q >> sh) & 1u) * 2) - 1.f);
+        }
+      }
+      put_pair_t<PL>(buf, plan, P, __ldg(&src.chan_abs[k]), v[0], v[1]);
+    }
+  }
+  __syncthreads();
+  fft_inv<PL, kRowThreadsPerFft>(buf, plan, tws_s, P, tws, ltid);
+  // write: column n of this input gets rows t0 .. t0+7; lane pair (2j, 2j+1)
+  // writes the two 16-byte halves of one column's 32 bytes
+  const float inv = 1.0f / (float)P;
+  const int nthr = FFTS * kRowThreadsPerFft;
+  float* ocol = out + (int64_t)in * P * ld + t0;
+  if (ld % 4 == 0 && t0 + ROWS <= nrows && ((uintptr_t)out & 15) == 0) {
+    for (int i = threadIdx.x; i < 2 * P; i += nthr) {
+      const int n = i >> 1, h = i & 1;
+      const float2 za = smem[(size_t)(2 * h) * PL_ + pidx(n)], zb = smem[(size_t)(2 * h + 1) * PL_ + pidx(n)];
+      *reinterpret_cast<float4*>(ocol + (int64_t)n * ld + 4 * h) =
+          make_float4(za.x * inv, za.y * inv, zb.x * inv, zb.y * inv);
+    }
+  } else {
+    for (int i = threadIdx.x; i < ROWS * P; i += nthr) {
+      const int n = i / ROWS, r = i - n * ROWS;
+      if (t0 + r >= nrows) continue;
+      const float2 z = smem[(size_t)(r >> 1) * PL_ + pidx(n)];
+      ocol[(int64_t)n * ld + r] = ((r & 1) ? z.y : z.x) * inv;
+    }
+  }
+}
+
+template <class PL>
+static int launch_row_tpair_t(ab_ctx* ctx, const Packed4Src& src, int nant, int nrows, int P, const FftPlan& plan,
+                              const float2* twP, const float2* tws, float* out, int64_t ld, cudaStream_t s) {
+  const size_t smem = row_smem_bytes(P, 4);
+  AB_TRY(set_smem_attr(row_stage_tpair_kernel<PL>, smem));
+  dim3 grid((unsigned)((nrows + 7) / 8), (unsigned)(2 * nant));
+  row_stage_tpair_kernel<PL><<<grid, 4 * kRowThreadsPerFft, smem, s>>>(src, nrows, plan, twP, tws, out, ld);
+  AB_LAUNCH_CHECK();
+  return AB_OK;
+}
+
 template <int FPC>
 static int launch_row_packed4_t(ab_ctx* ctx, const Packed4Src& src, int nant, int nrows, int P, const FftPlan& plan,
                                 const float2* twP, float* out, int64_t ld, cudaStream_t s) {
@@ -397,7 +491,17 @@ static int launch_row_packed4_t(ab_ctx* ctx, const Packed4Src& src, int nant, in
 int launch_row_stage_packed4(ab_ctx* ctx, const Packed4Src& src, int nant, int nrows, int P, const FftPlan& plan,
                              const float2* twP, float* out, int64_t ld, cudaStream_t s) {
   if (ctx->row_ffts_per_cta == 2) return launch_row_packed4_t<2>(ctx, src, nant, nrows, P, plan, twP, out, ld, s);
-  return launch_row_packed4_t<4>(ctx, src, nant, nrows, P, plan, twP, out, ld, s);
+  if (ctx->row_ffts_per_cta == 4) return launch_row_packed4_t<4>(ctx, src, nant, nrows, P, plan, twP, out, ld, s);
+  // default: time-paired spectra
+  AB_CHECK_ARG(row_smem_bytes(P, 4) <= ctx->smem_optin, "row stage: lblock %d too large", P);
+  bool tuned = false;
+  { FftPlan tmp; ctx_plan(ctx, P, &tmp, &tuned); }
+  if (P == Plan4096::N && !tuned) {
+    const float2* tws;
+    AB_TRY(get_twiddle_stream(ctx, P, {16, 16, 16}, &tws));
+    return launch_row_tpair_t<Plan4096>(ctx, src, nant, nrows, P, plan, twP, tws, out, ld, s);
+  }
+  return launch_row_tpair_t<NoPlan>(ctx, src, nant, nrows, P, plan, twP, nullptr, out, ld, s);
 }
 
 int launch_row_stage_c64(ab_ctx* ctx, const float2* dat, int64_t nslice, int P, const FftPlan& plan,

@@ -68,8 +68,10 @@ int ab_ctx_set_fft_plan(ab_ctx *ctx, int64_t n, const int32_t *radices, int64_t 
 int ab_ctx_set_time_filter(ab_ctx *ctx, int32_t mode, int32_t row_tile);
 /* Launch-shape options of this context (no reference counterpart; set by the
  * autotuner, albatros_axion_detection_gb300/autotune.py).
- * AB_OPT_ROW_FFTS_PER_CTA: spectra per CTA of the streaming row stage, 4
- * (default) or 2, read at each push. */
+ * AB_OPT_ROW_FFTS_PER_CTA: spectra per CTA of the streaming row stage, read
+ * at each push: 8 (default; 8 consecutive spectra of one input, transformed
+ * in time pairs, 32-byte column stores), or 4 / 2 (both pols of 4 / 2
+ * spectra, 16 / 8-byte column stores). */
 #define AB_OPT_ROW_FFTS_PER_CTA 1
 int ab_ctx_set_option(ab_ctx *ctx, int32_t option, int32_t value);
 

@@ -104,19 +104,26 @@ def test_stream_rejects_bad_config():
             stream.StreamCorrelator(1, np.arange(8), 0, 8, **kw)
 
 
-@pytest.mark.parametrize("nrows_extra", [0, 1])
-def test_stream_two_spectra_per_row_cta(nrows_extra):
-    """The row stage with 2 spectra per CTA (8-byte column stores, and the
-    scalar tail when nslice is odd) gives the oracle's visibilities."""
+@pytest.mark.parametrize("per_cta", [2, 4, 8])
+@pytest.mark.parametrize("nrows_extra", [0, 1, 3])
+def test_stream_row_stage_shapes(per_cta, nrows_extra):
+    """Each row-stage shape (2 or 4 pol-paired spectra, 8 time-paired spectra
+    per CTA; with the scalar tail when nslice is not a multiple of the
+    spectra per CTA) gives the oracle's visibilities, with and without
+    missing spectra."""
     from albatros_axion_detection_gb300 import autotune
     acclen, cut = 512 + nrows_extra, 32
     raw = gen.raw_4bit(seed=77 + nrows_extra, nspec=3 * acclen, nchan=8, nant=2)
     channels = np.arange(520, 528)
     kw = dict(acclen=acclen, nchunks=3, nblock=32, chanstart=0, chanend=8, osamp=16, cut=cut)
-    ref, _ = po.repfb_xcorr_avg(raw, channels, **kw)
-    autotune.set_row_ffts_per_cta(2)
+    present = np.ones((2, 3 * acclen), bool)
+    present[0, 100:131] = False
+    present[1, 700:705] = False
+    spec_map = np.where(present, np.arange(3 * acclen)[None, :], -1).astype(np.int32)
+    ref, _ = po.repfb_xcorr_avg(raw, channels, spec_present=present, **kw)
+    autotune.set_row_ffts_per_cta(per_cta)
     try:
-        vis, _ = run(raw, channels, **kw)
+        vis, _ = run(raw, channels, spec_map=spec_map, **kw)
     finally:
-        autotune.set_row_ffts_per_cta(4)
+        autotune.set_row_ffts_per_cta(8)
     check(vis, ref)
