@@ -625,8 +625,11 @@ __global__ void __launch_bounds__(kFirThreads, (IW > 0 && IW <= 40) || (IW == 0 
       float* wb = wout + (int64_t)b * ((int64_t)O * P);
       if (rfirst >= it.s1) {  // entirely past the end of the stream
 #pragma unroll
-        for (int p = 0; p < O; p += 4)
-          *reinterpret_cast<float4*>(wb + (int64_t)(p / GW) * P * GW + (p % GW)) = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int p = 0; p < O; p += GW) {
+          float* dst = wb + (int64_t)(p / GW) * P * GW;
+          if constexpr (GW == 8) st_global_v8(dst, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f);
+          else *reinterpret_cast<float4*>(dst) = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
         continue;
       }
       const int q0 = 4 * O - it.s0 + rfirst;   // y row of the block's first row (= phi mod O)
@@ -646,12 +649,13 @@ __global__ void __launch_bounds__(kFirThreads, (IW > 0 && IW <= 40) || (IW == 0 
       }
       reg_fft_dif<NC>(a);
       // untangle the real input: W_k = (Z_k + conj Z_{NC-k})/2 + w^k (Z_k - conj Z_{NC-k})/(2i);
-      // packed floats p = 2k, 2k+1 ((W_0, W_{O/2}) at p = 0, 1), stored 4 at a time
+      // packed floats p = 2k, 2k+1 ((W_0, W_{O/2}) at p = 0, 1), one group of
+      // GW floats per store (a whole 32-byte sector when GW = 8)
 #pragma unroll
-      for (int p = 0; p < O; p += 4) {
-        float2 o[2];
+      for (int p = 0; p < O; p += GW) {
+        float2 o[GW / 2];
 #pragma unroll
-        for (int h = 0; h < 2; h++) {
+        for (int h = 0; h < GW / 2; h++) {
           const int k = p / 2 + h;
           if (k == 0) {
             o[h] = make_float2(a[0].x + a[0].y, a[0].x - a[0].y);
@@ -663,7 +667,9 @@ __global__ void __launch_bounds__(kFirThreads, (IW > 0 && IW <= 40) || (IW == 0 
             o[h] = cadd(E, cmul(c_fir_tw[k * (64 / O)], Od));
           }
         }
-        *reinterpret_cast<float4*>(wb + (int64_t)(p / GW) * P * GW + (p % GW)) = make_float4(o[0].x, o[0].y, o[1].x, o[1].y);
+        float* dst = wb + (int64_t)(p / GW) * P * GW;
+        if constexpr (GW == 8) st_global_v8(dst, o[0].x, o[0].y, o[1].x, o[1].y, o[2].x, o[2].y, o[3].x, o[3].y);
+        else *reinterpret_cast<float4*>(dst) = make_float4(o[0].x, o[0].y, o[1].x, o[1].y);
       }
     }
     if (it.last) {
@@ -682,7 +688,7 @@ static int launch_fir_t(const FirArgs& a, const FoldArgs& fa, cudaStream_t s) {
   const int nseg = std::max(1, (a.acclen + S - 1) / S);
   const int64_t nitems = (int64_t)nseg * a.P * a.ninputs;
   AB_CHECK_ARG(nitems < (1LL << 31), "FIR time stage: too many work items");
-  AB_CHECK_ARG(((uintptr_t)fa.W & 15) == 0 && (a.P % 4) == 0, "FIR time stage: W must be 16-byte aligned");
+  AB_CHECK_ARG(((uintptr_t)fa.W & 31) == 0 && (a.P % 4) == 0, "FIR time stage: W must be 32-byte aligned");
   const size_t smem = Lay::bytes();
   AB_CUDA(cudaFuncSetAttribute(fir_fold_kernel<J, U, G, IW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const int per_sm = (IW > 0 && IW <= 40) || (IW == 0 && J <= 32) ? 2 : 1;

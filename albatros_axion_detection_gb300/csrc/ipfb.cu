@@ -432,12 +432,20 @@ __global__ void __launch_bounds__(4 * kRowThreadsPerFft)
   }
   __syncthreads();
   fft_inv<PL, kRowThreadsPerFft>(buf, plan, tws_s, P, tws, ltid);
-  // write: column n of this input gets rows t0 .. t0+7; lane pair (2j, 2j+1)
-  // writes the two 16-byte halves of one column's 32 bytes
+  // write: column n of this input gets rows t0 .. t0+7, one 32-byte store
+  // (a whole sector) per column
   const float inv = 1.0f / (float)P;
   const int nthr = FFTS * kRowThreadsPerFft;
   float* ocol = out + (int64_t)in * P * ld + t0;
-  if (ld % 4 == 0 && t0 + ROWS <= nrows && ((uintptr_t)out & 15) == 0) {
+  if (ld % 8 == 0 && t0 + ROWS <= nrows && ((uintptr_t)out & 31) == 0) {
+    for (int n = threadIdx.x; n < P; n += nthr) {
+      const float2 z0 = smem[pidx(n)], z1 = smem[(size_t)PL_ + pidx(n)];
+      const float2 z2 = smem[(size_t)2 * PL_ + pidx(n)], z3 = smem[(size_t)3 * PL_ + pidx(n)];
+      st_global_v8(ocol + (int64_t)n * ld, z0.x * inv, z0.y * inv, z1.x * inv, z1.y * inv, z2.x * inv, z2.y * inv,
+                   z3.x * inv, z3.y * inv);
+    }
+  } else if (ld % 4 == 0 && t0 + ROWS <= nrows && ((uintptr_t)out & 15) == 0) {
+    // lane pair (2j, 2j+1) writes the two 16-byte halves of one column's 32 bytes
     for (int i = threadIdx.x; i < 2 * P; i += nthr) {
       const int n = i >> 1, h = i & 1;
       const float2 za = smem[(size_t)(2 * h) * PL_ + pidx(n)], zb = smem[(size_t)(2 * h + 1) * PL_ + pidx(n)];
