@@ -115,7 +115,7 @@ def test_time_stage_tuner(tmp_path, monkeypatch):
     monkeypatch.setenv("ALBATROS_GB300_TUNE_CACHE", str(tmp_path / "t.json"))
     try:
         best = autotune.tune_time_stage(1024, 64, 16, limit=2)
-        assert best["mode"] in (0, 1) and best["ms"] > 0
+        assert best["mode"] in (0, 1, 3) and best["ms"] > 0
         assert len(best["candidates"]) >= 2
         again = autotune.tune_time_stage(1024, 64, 16, limit=2)
         assert again["ms"] == best["ms"]
