@@ -135,6 +135,15 @@ def set_time_filter(mode: int = DEFAULT_MODE, row_tile: int = 0, device: Optiona
 OPT_ROW_FFTS_PER_CTA = 1
 
 
+OPT_COARSE_MMA_BITS = 3
+
+
+def set_coarse_mma_bits(bits: int, device: Optional[int] = None) -> None:
+    """Operand type of the coarse correlator's tensor-core MMA: 16 (fp16,
+    exact, the default) or 8 (int8)."""
+    _lib.call("ab_ctx_set_option", _lib.ctx(device), OPT_COARSE_MMA_BITS, int(bits))
+
+
 def set_row_ffts_per_cta(n: int, device: Optional[int] = None) -> None:
     """Spectra per CTA of the streaming row stage: 8 (time-paired, the
     default), 4 or 2 (pol-paired)."""

@@ -80,6 +80,7 @@ struct ab_ctx {
   // 1: always FFT; 2: FFT where it runs, else IIR/FIR; 3: FIR, else FFT
   int time_filter_mode = 0;
   int fir_row_tile = 32;     // kept rows per thread of the FIR time stage
+  bool coarse_f16 = true;    // coarse correlator on fp16 (exact) instead of int8 tensor-core MMA
   int row_ffts_per_cta = 8;  // row stage: 8 = time-paired spectra of one input per CTA;
                              // 4 or 2 = pol-paired spectra of one antenna per CTA
   // grow-only scratch buffers keyed by slot

@@ -10,6 +10,8 @@
 //    the FP32 accumulator, the s8 mma is exact by construction;
 //  * pairwise 4-bit / 1-bit correlators on sortpols'd bytes
 //    (albatros_analysis/src/correlations/correlations_cpu.c:128-638).
+#include <cuda_fp16.h>
+
 #include "common.cuh"
 
 namespace ab {
@@ -284,6 +286,106 @@ __global__ void __launch_bounds__(kCcThreads)
   }
 }
 
+// FP16 form of the same Gram matrix.  The decoded values are integers in
+// [-8, 7], exact in fp16; mma.sync m16n8k16 multiplies them exactly and
+// accumulates in fp32, which stays exact while |sum| < 2^24: a CTA slice of
+// at most 4096 samples sums at most 4096 * 64 = 2^18.  The fp32 partials are
+// converted to int64 exactly and flushed with int64 atomics, as in the int8
+// form.  (The fp16 tensor path has a much higher rate than the int8 one on
+// this part.)
+__device__ __forceinline__ void mma_f16(float (&c)[4], const unsigned (&a)[4], unsigned b0, unsigned b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+constexpr int kCcPitchH = kCcKT + 8;  // halves per A row in smem (conflict-free fragment loads)
+
+template <int NT>
+__global__ void __launch_bounds__(kCcThreads)
+    coarse_xcorr_f16_kernel(const uint8_t* __restrict__ raw, int64_t ant_stride, int64_t row_bytes, int nant,
+                            int64_t rowstart, int64_t nrows, const int32_t* __restrict__ rows,
+                            const int64_t* __restrict__ channels, int ncols, int64_t chunk_rows, int64_t slice,
+                            int64_t slices_per_chunk, long long* __restrict__ G) {
+  constexpr int Rp = NT * 8;
+  constexpr int MT = Rp / 16;
+  constexpr int FC = (8 / MT) > 0 ? 8 / MT : 1;
+  extern __shared__ __align__(16) unsigned short Ah[];  // fp16 bits, [FC][Rp][kCcPitchH]
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int g = lane >> 2, tig = lane & 3;
+  const int c0 = blockIdx.x * FC;
+  const int64_t chunk = blockIdx.y / slices_per_chunk;
+  const int64_t sl = blockIdx.y % slices_per_chunk;
+  const int64_t k_begin = chunk * chunk_rows + sl * slice;
+  int64_t k_end = k_begin + slice;
+  const int64_t chunk_end = min((chunk + 1) * chunk_rows, nrows);
+  if (k_end > chunk_end) k_end = chunk_end;
+  const int fc = warp / MT, mi = warp % MT;
+  const bool active = (warp < FC * MT) && (c0 + fc < ncols);
+  float acc[NT][4];
+#pragma unroll
+  for (int j = 0; j < NT; j++)
+#pragma unroll
+    for (int q = 0; q < 4; q++) acc[j][q] = 0.f;
+  for (int i = threadIdx.x; i < FC * Rp * kCcPitchH; i += blockDim.x) Ah[i] = 0;
+  __syncthreads();
+  auto h16 = [](int v) -> unsigned short { return __half_as_ushort(__int2half_rn(v)); };
+  for (int64_t kt = k_begin; kt < k_end; kt += kCcKT) {
+    const int total = FC * nant * kCcKT;
+    for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+      int t = idx % kCcKT;
+      int rest = idx / kCcKT;
+      int a = rest % nant, f = rest / nant;
+      int64_t k = kt + t;
+      unsigned b0 = 0u, b1 = 0u;
+      if (k < k_end && c0 + f < ncols) {
+        int64_t r = rows ? (int64_t)rows[(int64_t)a * nrows + k] : rowstart + k;
+        const uint8_t* p = raw + (int64_t)a * ant_stride + r * row_bytes + 2 * channels[c0 + f];
+        uchar2 bb = *reinterpret_cast<const uchar2*>(p);
+        b0 = bb.x;
+        b1 = bb.y;
+      }
+      unsigned short* base = Ah + ((size_t)f * Rp + 4 * a) * kCcPitchH + t;
+      base[0] = h16(dec4i(b0 >> 4));
+      base[kCcPitchH] = h16(dec4i(b0 & 15u));
+      base[2 * kCcPitchH] = h16(dec4i(b1 >> 4));
+      base[3 * kCcPitchH] = h16(dec4i(b1 & 15u));
+    }
+    __syncthreads();
+    if (active) {
+      const unsigned short* Af = Ah + (size_t)fc * Rp * kCcPitchH;
+#pragma unroll
+      for (int ks = 0; ks < kCcKT; ks += 16) {
+        unsigned a[4];
+        const unsigned short* ra = Af + (size_t)(mi * 16 + g) * kCcPitchH + ks + tig * 2;
+        a[0] = *reinterpret_cast<const unsigned*>(ra);
+        a[1] = *reinterpret_cast<const unsigned*>(ra + 8 * kCcPitchH);
+        a[2] = *reinterpret_cast<const unsigned*>(ra + 8);
+        a[3] = *reinterpret_cast<const unsigned*>(ra + 8 * kCcPitchH + 8);
+#pragma unroll
+        for (int j = 0; j < NT; j++) {
+          const unsigned short* rb = Af + (size_t)(j * 8 + g) * kCcPitchH + ks + tig * 2;
+          mma_f16(acc[j], a, *reinterpret_cast<const unsigned*>(rb), *reinterpret_cast<const unsigned*>(rb + 8));
+        }
+      }
+    }
+    __syncthreads();
+  }
+  if (!active) return;
+  long long* Gc = G + (((int64_t)chunk * ncols + c0 + fc) * Rp) * Rp;
+#pragma unroll
+  for (int j = 0; j < NT; j++) {
+    int row = mi * 16 + g, col = j * 8 + tig * 2;
+    atomicAdd((unsigned long long*)&Gc[(int64_t)row * Rp + col], (unsigned long long)__float2ll_rn(acc[j][0]));
+    atomicAdd((unsigned long long*)&Gc[(int64_t)row * Rp + col + 1], (unsigned long long)__float2ll_rn(acc[j][1]));
+    atomicAdd((unsigned long long*)&Gc[(int64_t)(row + 8) * Rp + col], (unsigned long long)__float2ll_rn(acc[j][2]));
+    atomicAdd((unsigned long long*)&Gc[(int64_t)(row + 8) * Rp + col + 1],
+              (unsigned long long)__float2ll_rn(acc[j][3]));
+  }
+}
+
 __global__ void coarse_finalize_kernel(const long long* __restrict__ G, int Rp, int M, int ncols, int64_t nchunks,
                                        int64_t* __restrict__ re, int64_t* __restrict__ im) {
   int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -387,13 +489,23 @@ int coarse_xcorr_run(ab_ctx* ctx, const uint8_t* raw, int64_t ant_stride, int64_
   AB_CHECK_ARG(nchunks * spc <= 0x7fffffff, "coarse xcorr: too many slices");
   dim3 grid((unsigned)((ncols + FC - 1) / FC), (unsigned)(nchunks * spc));
   AB_CHECK_ARG(grid.y <= 65535, "coarse xcorr: %u time slices exceed the grid limit; use larger chunks", grid.y);
-#define AB_CC(NTV)                                                                                         \
-  case NTV:                                                                                                \
-    AB_CUDA(cudaFuncSetAttribute(coarse_xcorr_kernel<NTV>, cudaFuncAttributeMaxDynamicSharedMemorySize,     \
-                                 (int)smem));                                                              \
-    coarse_xcorr_kernel<NTV><<<grid, kCcThreads, smem, s>>>(raw, ant_stride, 2 * nchan, (int)nant, rowstart, \
-                                                            nrows, rows, channels, (int)ncols, chunk_rows,  \
-                                                            slice, spc, G);                                 \
+  const bool f16 = !ctx || ctx->coarse_f16;
+  const size_t smem16 = sizeof(unsigned short) * (size_t)FC * Rp * kCcPitchH;
+#define AB_CC(NTV)                                                                                           \
+  case NTV:                                                                                                  \
+    if (f16) {                                                                                               \
+      AB_CUDA(cudaFuncSetAttribute(coarse_xcorr_f16_kernel<NTV>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                                   (int)smem16));                                                            \
+      coarse_xcorr_f16_kernel<NTV><<<grid, kCcThreads, smem16, s>>>(raw, ant_stride, 2 * nchan, (int)nant,     \
+                                                                    rowstart, nrows, rows, channels,          \
+                                                                    (int)ncols, chunk_rows, slice, spc, G);   \
+    } else {                                                                                                 \
+      AB_CUDA(cudaFuncSetAttribute(coarse_xcorr_kernel<NTV>, cudaFuncAttributeMaxDynamicSharedMemorySize,     \
+                                   (int)smem));                                                              \
+      coarse_xcorr_kernel<NTV><<<grid, kCcThreads, smem, s>>>(raw, ant_stride, 2 * nchan, (int)nant, rowstart, \
+                                                              nrows, rows, channels, (int)ncols, chunk_rows,  \
+                                                              slice, spc, G);                                 \
+    }                                                                                                        \
     break;
   switch (NT) {
     AB_CC(2)

@@ -370,6 +370,114 @@ def run_batch(args):
     print(json.dumps(out), flush=True)
 
 
+def _timed(torch, fn, steps, warmup, local):
+    """ms per call of fn() (CUDA events on the current stream, after warm-up)."""
+    s = torch.cuda.current_stream()
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        e0.record(s)
+        for _ in range(steps):
+            fn()
+        e1.record(s)
+        torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps, clk.summary()
+
+
+def _line(metric, value, unit, ms, args, workload, extra):
+    out = {"metric": metric, "value": value, "unit": unit, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "data": "synthetic (seeded)", "config": {"workload": workload}}
+    out.update(extra)
+    print(json.dumps(out), flush=True)
+
+
+def run_coarse(args, nant, nchan, nspec, chunk, workload):
+    """Exact all-baseline coarse correlation of 4-bit packets (int8 tensor
+    cores, int64 sums): configurations 'plain unpack + xcorr' and 'many-antenna
+    coarse correlator'."""
+    import torch
+    from albatros_axion_detection_gb300 import correlations
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    g = torch.Generator(device=dev)
+    g.manual_seed(4321)
+    shape = (nant, nspec, nchan, 2)
+
+    def nib():
+        v = torch.randn(shape, generator=g, device=dev, dtype=torch.float32) * 2.5
+        return torch.clamp(torch.round(v), -7, 7).to(torch.int16) & 15
+    re, im = nib(), nib()
+    raw = ((re << 4) | im).to(torch.uint8).reshape(nant, nspec, 2 * nchan).contiguous()
+    del re, im
+    channels = np.arange(nchan)
+    if args.mma_bits:
+        from albatros_axion_detection_gb300 import autotune
+        autotune.set_coarse_mma_bits(args.mma_bits)
+    fn = lambda: correlations.xcorr_coarse_4bit(raw, 0, nspec, channels, nchan, chunk=chunk, average=False)
+    ms, clk = _timed(torch, fn, args.steps, args.warmup, local)
+    host = torch.empty(raw.shape, dtype=torch.uint8, pin_memory=True)
+    host.copy_(raw)
+    dev_in = torch.empty_like(raw)
+
+    def e2e():
+        dev_in.copy_(host, non_blocking=True)
+        re_, im_ = correlations.xcorr_coarse_4bit(dev_in, 0, nspec, channels, nchan, chunk=chunk, average=False)
+        return re_.cpu(), im_.cpu()
+    out_re, out_im = e2e()
+    ms_e2e, _ = _timed(torch, e2e, args.steps, 1, local)
+    spectra = nant * nspec
+    bytes_in = raw.numel()
+    peak, peak_kind = peaks()
+    achieved = bytes_in / (ms / 1e3) / 1e9
+    M = 2 * nant
+    macs = spectra // nant * nchan * (M * (M + 1) // 2) * 4  # real int MACs, unique pairs
+    _line("input spectra/s, exact all-baseline coarse correlation (int8 tensor cores, int64 sums)",
+          spectra / (ms / 1e3), "spectra/s", ms, args, workload,
+          {"dtype": ("int8" if args.mma_bits == 8 else "fp16 (exact small integers)") + " -> int64", "clocks": clk,
+           "e2e": {"value": spectra / (ms_e2e / 1e3), "unit": "spectra/s", "ms_per_step": ms_e2e,
+                   "h2d_bytes_per_step": int(bytes_in), "d2h_bytes_per_step": int(out_re.numel() * 16)},
+           "roofline": {"bound": "hbm", "kernel": "coarse_xcorr_kernel", "achieved": achieved, "peak": peak,
+                        "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+                        "int_macs_per_s_unique_pairs": macs / (ms / 1e3)},
+           "gpu_launches": None})
+
+
+def run_ipfb_pfb(args):
+    """IPFB + PFB rechannelisation of one input: 4096 rows of 2049 channels
+    -> IPFB (threshold 0.45) -> PFB osamp 64 on 64 selected coarse channels."""
+    import torch
+    from albatros_axion_detection_gb300 import pfb_gpu_utils as pg
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    nslice, nchan, osamp, c0 = 4096, 2049, 64, 640
+    g = torch.Generator(device=dev)
+    g.manual_seed(99)
+    dat = torch.complex(torch.randn(nslice, nchan, generator=g, device=dev),
+                        torch.randn(nslice, nchan, generator=g, device=dev)).to(torch.complex64)
+    filt = pg.calculate_filter(pg.get_matft(nslice, nchan, 4), 0.45)
+    lblock = 4096 * osamp
+    # fine PFB window (sinc-Hamming, ntap 4) built on the host in double
+    N = 4 * lblock
+    i = np.arange(N)
+    w = (0.54 - 0.46 * np.cos(2 * np.pi * i / (N - 1))) * np.sinc((i - N / 2) / lblock)
+    win = torch.from_numpy(w.astype(np.float32)).to(dev)
+    q0, q1 = c0 * osamp, (c0 + 64) * osamp
+
+    def fn():
+        ts = pg.cupy_ipfb(dat, filt)
+        return pg.cupy_pfb_band(ts.contiguous().reshape(-1), win, q0, q1, nchan=lblock // 2 + 1)
+    ms, clk = _timed(torch, fn, args.steps, args.warmup, local)
+    _line("input spectra/s, IPFB (lblock 4096) + PFB osamp 64 band of 64 coarse channels, one input",
+          nslice / (ms / 1e3), "spectra/s", ms, args,
+          "IPFB 4096 rows x 2049 channels (threshold 0.45) + PFB osamp 64 on 64 channels",
+          {"dtype": "f32", "clocks": clk, "gpu_launches": None})
+
+
 def cpu_baseline_sample(raw_np, sc=None, reps=1):
     """The CPU chain over one 2^15-spectrum chunk of both antennas."""
     from oracle import cpu_chain
@@ -423,14 +531,18 @@ def main():
                     help="stream only this many 2^15-spectrum chunks (smaller case for profiling; "
                          "every launch keeps its full size)")
     ap.add_argument("--nant", type=int, default=None, help="antennas (profiling case; default 2)")
-    ap.add_argument("--workload", default="stream", choices=["stream", "uneven-batch"],
-                    help="stream: the 2-antenna 2^20-spectrum chain (default); uneven-batch: 24 mixed files")
+    ap.add_argument("--workload", default="stream",
+                    choices=["stream", "uneven-batch", "unpack-xcorr", "coarse-xcorr", "ipfb-pfb"],
+                    help="stream: the 2-antenna 2^20-spectrum chain (default); uneven-batch: 24 mixed files; "
+                         "unpack-xcorr: 2 ant x 64 ch x 2^17 spectra, 2^14-spectrum averages; coarse-xcorr: "
+                         "16 ant x 256 ch x 2^18 spectra all baselines; ipfb-pfb: one-input rechannelisation")
     ap.add_argument("--lanes", type=int, default=4, help="uneven-batch: concurrent CUDA streams")
     ap.add_argument("--time-filter", default="default", choices=["default", "iir", "fir", "fft"],
                     help="stream: IPFB time stage form (default: the library's choice)")
     ap.add_argument("--row-tile", type=int, default=0, help="stream: FIR rows per thread (16 or 32)")
     ap.add_argument("--row-ffts", type=int, default=0, help="stream: spectra per row-stage CTA (2 or 4)")
     ap.add_argument("--check", action="store_true", help="uneven-batch: job-0 error of every file vs the FP64 oracle")
+    ap.add_argument("--mma-bits", type=int, default=0, help="coarse workloads: tensor-core operand bits (16 or 8)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -438,6 +550,16 @@ def main():
         run_reference(args)
     elif args.workload == "uneven-batch":
         run_batch(args)
+    elif args.workload == "unpack-xcorr":
+        run_coarse(args, 2, 64, 1 << 17, 1 << 14,
+                   "plain unpack + xcorr: 2 ant x 2 pol 4-bit, 64 ch, 2^17 spectra, averages over 2^14 spectra")
+        run_coarse(args, 2, 64, 1 << 24, 1 << 14,
+                   "plain unpack + xcorr, bandwidth sweep size: 2 ant x 2 pol 4-bit, 64 ch, 2^24 spectra")
+    elif args.workload == "coarse-xcorr":
+        run_coarse(args, 16, 256, 1 << 18, None,
+                   "many-antenna coarse correlator: 16 ant x 2 pol 4-bit, 256 ch, 2^18 spectra, all 528 pairs")
+    elif args.workload == "ipfb-pfb":
+        run_ipfb_pfb(args)
     else:
         run_ours(args)
 

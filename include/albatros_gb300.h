@@ -73,6 +73,10 @@ int ab_ctx_set_time_filter(ab_ctx *ctx, int32_t mode, int32_t row_tile);
  * in time pairs, 32-byte column stores), or 4 / 2 (both pols of 4 / 2
  * spectra, 16 / 8-byte column stores). */
 #define AB_OPT_ROW_FFTS_PER_CTA 1
+/* AB_OPT_COARSE_MMA_BITS: input type of the coarse correlator's tensor-core
+ * MMA, 16 (default: fp16 operands, fp32 partial sums, exact) or 8 (int8
+ * operands, int32 partial sums). */
+#define AB_OPT_COARSE_MMA_BITS 3
 int ab_ctx_set_option(ab_ctx *ctx, int32_t option, int32_t value);
 
 /* ---- unpacking ----------------------------------------------------------

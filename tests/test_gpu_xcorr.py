@@ -56,9 +56,18 @@ def test_all_ant_errors():
         avg_xcorr_all_ant_gpu(x, 2, 1, 10, 3, out=torch.zeros((2, 2, 3), dtype=torch.complex64, device="cuda"))
 
 
+@pytest.fixture(params=[16, 8], ids=["fp16-mma", "int8-mma"])
+def mma_bits(request):
+    """Run a coarse-correlator test with each tensor-core operand type."""
+    from albatros_axion_detection_gb300 import autotune
+    autotune.set_coarse_mma_bits(request.param)
+    yield request.param
+    autotune.set_coarse_mma_bits(16)
+
+
 @pytest.mark.parametrize("nant,nspec,nchan,chunk", [(2, 2 ** 14, 64, 2 ** 12), (16, 2048, 256, None),
                                                      (1, 333, 5, 100), (3, 1000, 16, 64)])
-def test_coarse_xcorr_bit_exact(nant, nspec, nchan, chunk):
+def test_coarse_xcorr_bit_exact(nant, nspec, nchan, chunk, mma_bits):
     from albatros_axion_detection_gb300.correlations import xcorr_coarse_4bit
     raw = gen.raw_4bit_uniform(seed=nant * nchan, nspec=nspec, nchan=nchan, nant=nant)
     ch = np.arange(nchan) if nchan < 64 else np.arange(0, nchan, 3)
@@ -72,15 +81,16 @@ def test_coarse_xcorr_bit_exact(nant, nspec, nchan, chunk):
         np.testing.assert_array_equal(im[k], ei)
 
 
-def test_coarse_xcorr_worst_case_magnitudes():
-    """All nibbles 0x8 (+8): the largest products, exact in int32 partials."""
+def test_coarse_xcorr_worst_case_magnitudes(mma_bits):
+    """All nibbles 0x8 (+8): the largest products, exact in the int32 / fp32
+    partial sums (4096 samples x 64 per CTA slice)."""
     from albatros_axion_detection_gb300.correlations import xcorr_coarse_4bit
     raw = np.full((2, 8192, 8), 0x88, np.uint8)
     re, im = xcorr_coarse_4bit(cu(raw), 0, 8192, np.arange(4), 4, average=False)
     assert np.all(re.cpu().numpy() == 8192 * 128) and np.all(im.cpu().numpy() == 0)
 
 
-def test_coarse_xcorr_row_lists():
+def test_coarse_xcorr_row_lists(mma_bits):
     from albatros_axion_detection_gb300.correlations import xcorr_coarse_4bit
     raw = gen.raw_4bit(seed=3, nspec=700, nchan=32, nant=2)
     rows = np.stack([np.arange(0, 600), np.arange(100, 700)]).astype(np.int32)
