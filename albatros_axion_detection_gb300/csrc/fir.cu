@@ -227,10 +227,16 @@ int get_fir_taps(ab_ctx* ctx, int P, int N, int ntap, float thresh, int* J_out, 
 // So y = g W(z) / (A(z) A(1/z)) x with A = B / b_0 and g = (1 + t^2) / b_0^2:
 // a 4-tap FIR, a causal 3-pole recursion and an anti-causal 3-pole recursion,
 // 11 FMAs per sample.  Applied to the periodic column it reproduces the
-// circular convolution; each thread starts both recursions IW samples before
-// its rows from zero state, which drops a tail of the size of 1/A's impulse
-// response after IW samples (chosen below 1e-10 of its peak).
-static bool iir_factor(const double* w, double t, double coef[8], int* warm) {
+// circular convolution.  The threads of a CTA run the recursions over
+// consecutive row ranges and pass their end states on (iir_fold_kernel); a
+// state is carried over at least IW rows, after which 1/A's impulse response
+// is below 1e-10 of its peak, and the rest of its effect is dropped.
+// Per-column IIR coefficients: g w0..g w3, a1..a3, 0, then 1/A's impulse
+// response h[U-5..U-1] for the two row tiles' U (state advance over one
+// thread's rows), each padded to 8 floats.
+constexpr int kIirU32 = 41, kIirU16 = 21, kIirCoef = 24;
+
+static bool iir_factor(const double* w, double t, double coef[kIirCoef], int* warm) {
   const int m = 3;
   double d[4];
   for (int k = 0; k <= m; k++) {
@@ -304,11 +310,15 @@ static bool iir_factor(const double* w, double t, double coef[8], int* warm) {
   coef[4] = a1;
   coef[5] = a2;
   coef[6] = a3;
-  coef[7] = 0.0;
+  for (int k = 7; k < kIirCoef; k++) coef[k] = 0.0;
+  for (int i = 0; i < 5; i++) {
+    coef[8 + i] = h[kIirU32 - 5 + i];
+    coef[16 + i] = h[kIirU16 - 5 + i];
+  }
   return true;
 }
 
-// Per-column IIR coefficients (g w0..g w3, a1..a3, 0) as float (P, 8) and the
+// Per-column IIR coefficients as float (P, kIirCoef) and the
 // warm-up IW in {40, 80} (0 when no factorisation or a longer warm-up is
 // needed), cached in the context per (P, ntap, thresh).
 int get_iir_coeffs(ab_ctx* ctx, int P, int ntap, float thresh, int* W_out, const float** coef_out) {
@@ -329,16 +339,16 @@ int get_iir_coeffs(ab_ctx* ctx, int P, int ntap, float thresh, int* W_out, const
   }
   std::vector<double> w;
   sinc_hamming_host(ntap, P, w);
-  std::vector<float> cf((size_t)P * 8);
+  std::vector<float> cf((size_t)P * kIirCoef);
   int warm = 0;
   bool ok = thresh > 0.f;
   for (int n = 0; n < P && ok; n++) {
-    double wn[4], c[8];
+    double wn[4], c[kIirCoef];
     for (int k = 0; k < 4; k++) wn[k] = w[(size_t)k * P + n];
     int wm = 0;
     ok = iir_factor(wn, (double)thresh, c, &wm);
     warm = std::max(warm, wm);
-    for (int k = 0; k < 8; k++) cf[(size_t)n * 8 + k] = (float)c[k];
+    for (int k = 0; k < kIirCoef; k++) cf[(size_t)n * kIirCoef + k] = (float)c[k];
   }
   const int IW = !ok ? 0 : warm <= 40 ? 40 : warm <= 80 ? 80 : 0;
   float* dc = nullptr;
@@ -377,7 +387,7 @@ int get_iir_coeffs(ab_ctx* ctx, int P, int ntap, float thresh, int* W_out, const
 // The fold gives each fine block to one thread: it folds the 4 taps into O
 // samples and takes their real DFT in registers (compile-time radix-2 FFT of
 // O/2 points plus the real-input untangle), then writes the O packed floats
-// of W with 16-byte stores.
+// of W with 32-byte stores.
 constexpr int kFirThreads = 256;
 
 __constant__ float2 c_fir_tw[64];  // exp(-2 pi i k / 64)
@@ -392,14 +402,14 @@ int fir_init_device() {
   return AB_OK;
 }
 
-// IW = 0: FIR with 2J+1 taps (halo J each side); IW > 0: IIR with warm-up IW
-// (halo IW + 3 before, IW after; 8 coefficients per column).
-template <int J, int U, int O, int IW>
+// FIR layout: U rows per thread, R = U*kFirThreads computed rows per item,
+// halo J rows each side, y rows in their own buffer.
+template <int J, int U, int O>
 struct FirLayout {
   static constexpr int R = U * kFirThreads;
-  static constexpr int HL = IW > 0 ? IW + 3 : J;
-  static constexpr int HR = IW > 0 ? IW : J;
-  static constexpr int K = IW > 0 ? 8 : 2 * J + 1;
+  static constexpr int HL = J;
+  static constexpr int HR = J;
+  static constexpr int K = 2 * J + 1;
   static constexpr int XS = (R + HL + HR + U + 3) & ~3;  // x window (floats, unpadded)
   static constexpr int TAPS = (K + 3) & ~3;
   static constexpr int ST = 4 * O;                      // tail rows of the previous chunk
@@ -408,6 +418,25 @@ struct FirLayout {
   static constexpr int YROWS = R + 8 * O + U;           // y rows held (incl. zeros past the end)
   static constexpr int YS = YROWS + YROWS / O + 4;      // one pad float per O rows
   static constexpr size_t bytes() { return sizeof(float) * (2 * (size_t)STAGE + (size_t)YS); }
+};
+
+// IIR layout: thread k runs the recursions over window rows [k U, k U + U);
+// window row D*U is the item's first computed row, so threads 0..D-1 (and
+// the D threads after the last computed row) only run the recursions into
+// the computed rows.  R = (kFirThreads - 2D) U computed rows per item.  y
+// rows are written over the x window once it is dead (XS holds both), and
+// each thread's end-of-range states go to two exchange arrays.
+template <int U, int O, int D>
+struct IirLayout {
+  static constexpr int R = (kFirThreads - 2 * D) * U;
+  static constexpr int XW = kFirThreads * U + 6;  // all threads' rows, 3 before, up to 3 of alignment shift
+  static constexpr int YROWS = R + 8 * O;
+  static constexpr int YS = YROWS + YROWS / O + 4;
+  static constexpr int XS = ((XW > YS ? XW : YS) + 3) & ~3;
+  static constexpr int TAPS = kIirCoef;
+  static constexpr int STAGE = XS + TAPS + 4 * O + 4 * O;
+  static constexpr int XCH = 6 * kFirThreads;  // forward and backward states, 3 floats each
+  static constexpr size_t bytes() { return sizeof(float) * (2 * (size_t)STAGE + XCH); }
 };
 
 __device__ __forceinline__ void cp_async4(float* dst, const float* src) {
@@ -477,14 +506,163 @@ __device__ __forceinline__ FirItem fir_item(int item, int nseg, int P, int S, in
   return it;
 }
 
-template <int J, int U, int G, int IW>
-__global__ void __launch_bounds__(kFirThreads, (IW > 0 && IW <= 40) || (IW == 0 && J <= 32) ? 2 : 1)
+// Shift (0..3 floats) at which the x window lands in shared memory so that
+// it can be copied with 16-byte cp.async from the 16-byte boundary at or
+// below col + xbase; -1 when the window wraps around the column or that
+// boundary lies before the column (4-byte copies, no shift).
+__device__ __forceinline__ int window_shift(const float* col, int xbase, int nx, int nslice) {
+  const int xo = (int)((((uintptr_t)(col + xbase)) >> 2) & 3);
+  return (xbase - xo < 0 || xbase + nx > nslice) ? -1 : xo;
+}
+
+// stage[sh + e] = column[(xbase + e) mod nslice] for e < nx, sh = max(shift, 0);
+// an aligned shift also copies the shift floats before xbase into stage[0, sh).
+__device__ __forceinline__ void prefetch_window(float* stage, const float* col, int xbase, int nx, int nslice,
+                                                int shift, int tid) {
+  if (shift >= 0) {
+    const float* src = col + xbase - shift;
+    const int tot = shift + nx, n4 = tot >> 2;
+    for (int q = tid; q < n4; q += kFirThreads) cp_async16(stage + 4 * q, src + 4 * q);
+    for (int e = 4 * n4 + tid; e < tot; e += kFirThreads) cp_async4(stage + e, src + e);
+  } else {
+    for (int e = tid; e < nx; e += kFirThreads) {
+      int t = xbase + e;
+      if (t < 0 || t >= nslice) t = ((t % nslice) + nslice) % nslice;
+      cp_async4(stage + e, col + t);
+    }
+  }
+}
+
+// The item's other inputs, after its x window: the column's K taps or
+// coefficients (TAPS floats reserved), the previous chunk's last 4*O rows
+// (first segment only) and the 4*O fine-window coefficients of column n as
+// a float4 per t' ([t'][i] = win[(i*O + t')*P + n]).
+template <int O>
+__device__ __forceinline__ void prefetch_item_extras(float* st_taps, int K, int TAPS, const float* taps,
+                                                     const FirItem& it, int P, const float* win,
+                                                     const float* state_in, int tid) {
+  for (int k = tid; k < K; k += kFirThreads) cp_async4(st_taps + k, taps + (int64_t)it.n * K + k);
+  float* st_tail = st_taps + TAPS;
+  if (it.first) {
+    const float* st = state_in + ((int64_t)it.in * P + it.n) * (4 * O);
+    for (int q = tid; q < O; q += kFirThreads) cp_async16(st_tail + 4 * q, st + 4 * q);
+  }
+  float* st_win = st_tail + 4 * O;
+  for (int q = tid; q < 4 * O; q += kFirThreads) {
+    const int tp = q >> 2, i = q & 3;
+    cp_async4(st_win + q, win + (int64_t)(i * O + tp) * P + it.n);
+  }
+}
+
+// y rows are padded one float per O rows, with the pads at the fine blocks'
+// first rows (y row phi + k*O): a block's 4*O rows then sit at base + c + c/O
+// for compile-time c, and blocks O + 1 floats apart fall in distinct banks.
+template <int O>
+__device__ __forceinline__ int yidx(int q, int phi) {
+  return q + (q - phi + O) / O;
+}
+template <int O>
+__device__ __forceinline__ int y_phase(const FirItem& it, const FoldArgs& fa) {
+  return (((4 * O - it.s0 + (int)fa.row0) % O) + O) % O;
+}
+
+// Fold + real DFT of the fine blocks whose last row lies in [s0, s0 + S)
+// (the last segment: >= s0), from the item's y rows (y row q = kept row
+// q - 4*O + s0), one block per thread; then the last segment keeps the
+// chunk's last 4*O rows as the next chunk's tail.
+template <int O>
+__device__ __forceinline__ void fold_item_blocks(const float* ys, int phi, const float4* wt, const FirItem& it,
+                                                 const FoldArgs& fa, int P, int S, int acclen,
+                                                 float* __restrict__ state_out, int tid) {
+  constexpr int NC = O / 2, LOGNC = ilog2(NC);
+  constexpr int GW = O < 8 ? O : 8;
+  const int row0 = (int)fa.row0, nb = (int)fa.nb;
+  auto first_block_ending_at_or_after = [&](int r) -> int {  // min b with row0 + b*O + 4O - 1 >= r
+    const int num = r - 4 * O + 1 - row0;
+    const int b = num <= 0 ? 0 : (num + O - 1) / O;
+    return min(b, nb);
+  };
+  const int b0 = it.first ? 0 : first_block_ending_at_or_after(it.s0);
+  const int b1 = it.last ? nb : first_block_ending_at_or_after(it.s0 + S);
+  float* wout = fa.W + (int64_t)it.in * fa.nb * ((int64_t)O * P) + (int64_t)it.n * GW;
+  for (int b = b0 + tid; b < b1; b += kFirThreads) {
+    const int rfirst = row0 + b * O;
+    float* wb = wout + (int64_t)b * ((int64_t)O * P);
+    if (rfirst >= it.s1) {  // entirely past the end of the stream
+#pragma unroll
+      for (int p = 0; p < O; p += GW) {
+        float* dst = wb + (int64_t)(p / GW) * P * GW;
+        if constexpr (GW == 8) st_global_v8(dst, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f);
+        else *reinterpret_cast<float4*>(dst) = make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+      continue;
+    }
+    const int q0 = 4 * O - it.s0 + rfirst;  // y row of the block's first row (= phi mod O)
+    const float* yb = ys + yidx<O>(q0, phi);  // rows q0 + c at yb[c + c/O]
+    float2 a[NC];
+#pragma unroll
+    for (int m = 0; m < NC; m++) {
+      float zz[2];
+#pragma unroll
+      for (int e = 0; e < 2; e++) {
+        const int tp = 2 * m + e;
+        const float4 w4 = wt[tp];
+        zz[e] = fmaf(w4.x, yb[tp], fmaf(w4.y, yb[tp + (O + 1)],
+                                        fmaf(w4.z, yb[tp + 2 * (O + 1)], w4.w * yb[tp + 3 * (O + 1)])));
+      }
+      a[m] = make_float2(zz[0], zz[1]);
+    }
+    reg_fft_dif<NC>(a);
+    // untangle the real input: W_k = (Z_k + conj Z_{NC-k})/2 + w^k (Z_k - conj Z_{NC-k})/(2i);
+    // packed floats p = 2k, 2k+1 ((W_0, W_{O/2}) at p = 0, 1), one group of
+    // GW floats per store (a whole 32-byte sector when GW = 8)
+#pragma unroll
+    for (int p = 0; p < O; p += GW) {
+      float2 o[GW / 2];
+#pragma unroll
+      for (int h = 0; h < GW / 2; h++) {
+        const int k = p / 2 + h;
+        if (k == 0) {
+          o[h] = make_float2(a[0].x + a[0].y, a[0].x - a[0].y);
+        } else {
+          const float2 z = a[bitrev(k, LOGNC)], c = cconj(a[bitrev(NC - k, LOGNC)]);
+          const float2 E = cscale(cadd(z, c), 0.5f);
+          const float2 Dd = csub(z, c);
+          const float2 Od = make_float2(0.5f * Dd.y, -0.5f * Dd.x);
+          o[h] = cadd(E, cmul(c_fir_tw[k * (64 / O)], Od));
+        }
+      }
+      float* dst = wb + (int64_t)(p / GW) * P * GW;
+      if constexpr (GW == 8) st_global_v8(dst, o[0].x, o[0].y, o[1].x, o[1].y, o[2].x, o[2].y, o[3].x, o[3].y);
+      else *reinterpret_cast<float4*>(dst) = make_float4(o[0].x, o[0].y, o[1].x, o[1].y);
+    }
+  }
+  if (it.last) {
+    float* st = state_out + ((int64_t)it.in * P + it.n) * (4 * O);
+    for (int i = tid; i < 4 * O; i += kFirThreads) st[i] = ys[yidx<O>(4 * O - it.s0 + (acclen - 4 * O + i), phi)];
+  }
+}
+
+// y rows that do not come from the filter: the previous chunk's tail (first
+// segment, y rows [0, 4*O)) and zeros past the end of the stream (last
+// segment; zero-padded final blocks).
+template <int O>
+__device__ __forceinline__ void y_edges(float* ys, int phi, const float* tail, const FirItem& it, int yoff, int tid) {
+  if (it.first)
+    for (int i = tid; i < 4 * O; i += kFirThreads) ys[yidx<O>(i, phi)] = tail[i];
+  if (it.last)
+    for (int q = yoff + it.nrows + tid; q < yoff + it.nrows + 4 * O; q += kFirThreads) ys[yidx<O>(q, phi)] = 0.f;
+}
+
+// ---------------------------------------------------------------------------
+// FIR time stage + fold.
+template <int J, int U, int G>
+__global__ void __launch_bounds__(kFirThreads, J <= 32 ? 2 : 1)
     fir_fold_kernel(const float* __restrict__ data, int64_t ld, int P, int nslice, int cut, int acclen, int S,
                     int nseg, int nitems, const float* __restrict__ taps, FoldArgs fa,
                     const float* __restrict__ state_in, float* __restrict__ state_out) {
-  constexpr int O = 2 * G, NC = O / 2, LOGNC = ilog2(NC);
-  constexpr int GW = O < 8 ? O : 8;
-  using Lay = FirLayout<J, U, O, IW>;
+  constexpr int O = 2 * G;
+  using Lay = FirLayout<J, U, O>;
   constexpr int K = Lay::K;
   extern __shared__ float4 smem4[];
   float* stage0 = reinterpret_cast<float*>(smem4);
@@ -494,34 +672,11 @@ __global__ void __launch_bounds__(kFirThreads, (IW > 0 && IW <= 40) || (IW == 0 
   auto prefetch = [&](int item, float* stage) {
     const FirItem it = fir_item(item, nseg, P, S, acclen, O);
     const float* col = data + ((int64_t)it.in * P + it.n) * ld;
-    // x window: stage[e] = x[(cut + ylo - HL + e) mod nslice], e < nrows + HL + HR
-    const int xbase = cut + it.ylo - Lay::HL;
-    const int nx = it.nrows + Lay::HL + Lay::HR;
-    const float* src = col + xbase;
-    if (xbase >= 0 && xbase + nx <= nslice && (((uintptr_t)src) & 15) == 0) {
-      const int n4 = nx >> 2;
-      for (int q = tid; q < n4; q += kFirThreads) cp_async16(stage + 4 * q, src + 4 * q);
-      for (int e = 4 * n4 + tid; e < nx; e += kFirThreads) cp_async4(stage + e, src + e);
-    } else {
-      for (int e = tid; e < nx; e += kFirThreads) {
-        int t = xbase + e;
-        if (t < 0 || t >= nslice) t = ((t % nslice) + nslice) % nslice;
-        cp_async4(stage + e, col + t);
-      }
-    }
+    // x window: stage[e] = x[(cut + ylo - J + e) mod nslice], e < nrows + 2J
+    const int xbase = cut + it.ylo - J, nx = it.nrows + 2 * J;
+    prefetch_window(stage, col, xbase, nx, nslice, window_shift(col, xbase, nx, nslice) == 0 ? 0 : -1, tid);
     for (int e = nx + tid; e < nx + U; e += kFirThreads) stage[e] = 0.f;
-    float* st_taps = stage + Lay::XS;
-    for (int k = tid; k < K; k += kFirThreads) cp_async4(st_taps + k, taps + (int64_t)it.n * K + k);
-    float* st_tail = st_taps + Lay::TAPS;
-    if (it.first) {
-      const float* st = state_in + ((int64_t)it.in * P + it.n) * (4 * O);
-      for (int q = tid; q < O; q += kFirThreads) cp_async16(st_tail + 4 * q, st + 4 * q);
-    }
-    float* st_win = st_tail + Lay::ST;  // [t'][i] = win[(i*O + t')*P + n]
-    for (int q = tid; q < 4 * O; q += kFirThreads) {
-      const int tp = q >> 2, i = q & 3;
-      cp_async4(st_win + q, fa.win + (int64_t)(i * O + tp) * P + it.n);
-    }
+    prefetch_item_extras<O>(stage + Lay::XS, K, Lay::TAPS, taps, it, P, fa.win, state_in, tid);
     cp_async_commit();
   };
 
@@ -539,52 +694,8 @@ __global__ void __launch_bounds__(kFirThreads, (IW > 0 && IW <= 40) || (IW == 0 
     __syncthreads();
     const FirItem it = fir_item(item, nseg, P, S, acclen, O);
     const int yoff = it.ylo - it.s0 + 4 * O;  // y row of computed row ylo
-    // y rows are padded one float per O rows, with the pads at the fine
-    // blocks' first rows (y row phi + k*O): a block's 4*O rows then sit at
-    // base + c + c/O for compile-time c, and blocks O + 1 floats apart fall
-    // in distinct banks
-    const int phi = (((4 * O - it.s0 + (int)fa.row0) % O) + O) % O;
-    auto yidx = [phi](int q) { return q + (q - phi + O) / O; };
-    if (it.first) {
-      const float* st = stage + Lay::XS + Lay::TAPS;
-      for (int i = tid; i < 4 * O; i += kFirThreads) ys[yidx(i)] = st[i];
-    }
-    if (it.last) {  // zeros past the end of the stream (zero-padded final blocks)
-      for (int q = yoff + it.nrows + tid; q < yoff + it.nrows + 4 * O; q += kFirThreads) ys[yidx(q)] = 0.f;
-    }
-    if constexpr (IW > 0) {
-      // IIR: rows r0 + [0, U), r0 = tid*U; x of row offset tt (from r0) at
-      // xu[IW + 3 + tt].  Causal u = W x, v = u / A over tt in [-IW, U + IW),
-      // keeping v for tt >= 0; then y = g v / A(1/z) backwards from U + IW - 1.
-      if (tid * U < it.nrows) {
-        const float* cf = stage + Lay::XS;
-        const float w0 = cf[0], w1 = cf[1], w2 = cf[2], w3 = cf[3];
-        const float a1 = cf[4], a2 = cf[5], a3 = cf[6];
-        const float* xu = stage + tid * U;
-        float v[U + IW];
-        float s1 = 0.f, s2 = 0.f, s3 = 0.f;
-#pragma unroll
-        for (int mm = 0; mm < U + 2 * IW; mm++) {
-          const float u = fmaf(w0, xu[mm + 3], fmaf(w1, xu[mm + 2], fmaf(w2, xu[mm + 1], w3 * xu[mm])));
-          const float vt = fmaf(-a1, s1, fmaf(-a2, s2, fmaf(-a3, s3, u)));
-          s3 = s2;
-          s2 = s1;
-          s1 = vt;
-          if (mm >= IW) v[mm - IW] = vt;
-        }
-        const int t0 = yoff + tid * U;
-        const int nv = it.nrows - tid * U;
-        float q1 = 0.f, q2 = 0.f, q3 = 0.f;
-#pragma unroll
-        for (int mm = U + IW - 1; mm >= 0; mm--) {
-          const float yt = fmaf(-a1, q1, fmaf(-a2, q2, fmaf(-a3, q3, v[mm])));
-          q3 = q2;
-          q2 = q1;
-          q1 = yt;
-          if (mm < U) ys[mm < nv ? yidx(t0 + mm) : Lay::YS - 1] = yt;  // rows past nrows go to a spare slot
-        }
-      }
-    } else
+    const int phi = y_phase<O>(it, fa);
+    y_edges<O>(ys, phi, stage + Lay::XS + Lay::TAPS, it, yoff, tid);
     // y[ylo + i] = sum_j h[j + J] x[cut + ylo + i - j] = sum_k h[k] xs[i + 2J - k]
     if (tid * U < it.nrows) {
       float h[K];
@@ -606,110 +717,251 @@ __global__ void __launch_bounds__(kFirThreads, (IW > 0 && IW <= 40) || (IW == 0 
       const int t0 = yoff + tid * U;
       const int nv = it.nrows - tid * U;
 #pragma unroll
-      for (int g = 0; g < U; g++) ys[g < nv ? yidx(t0 + g) : Lay::YS - 1] = acc[g];  // spare slot past nrows
+      for (int g = 0; g < U; g++) ys[g < nv ? yidx<O>(t0 + g, phi) : Lay::YS - 1] = acc[g];  // spare slot past nrows
     }
     __syncthreads();
-    // blocks whose last row lies in [s0, s0 + S) (the last segment: >= s0)
-    const int row0 = (int)fa.row0, nb = (int)fa.nb;
-    auto first_block_ending_at_or_after = [&](int r) -> int {  // min b with row0 + b*O + 4O - 1 >= r
-      const int num = r - 4 * O + 1 - row0;
-      const int b = num <= 0 ? 0 : (num + O - 1) / O;
-      return min(b, nb);
-    };
-    const int b0 = it.first ? 0 : first_block_ending_at_or_after(it.s0);
-    const int b1 = it.last ? nb : first_block_ending_at_or_after(it.s0 + S);
-    const float4* wt = reinterpret_cast<const float4*>(stage + Lay::XS + Lay::TAPS + Lay::ST);
-    float* wout = fa.W + (int64_t)it.in * fa.nb * ((int64_t)O * P) + (int64_t)it.n * GW;
-    for (int b = b0 + tid; b < b1; b += kFirThreads) {
-      const int rfirst = row0 + b * O;
-      float* wb = wout + (int64_t)b * ((int64_t)O * P);
-      if (rfirst >= it.s1) {  // entirely past the end of the stream
-#pragma unroll
-        for (int p = 0; p < O; p += GW) {
-          float* dst = wb + (int64_t)(p / GW) * P * GW;
-          if constexpr (GW == 8) st_global_v8(dst, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f);
-          else *reinterpret_cast<float4*>(dst) = make_float4(0.f, 0.f, 0.f, 0.f);
-        }
-        continue;
-      }
-      const int q0 = 4 * O - it.s0 + rfirst;   // y row of the block's first row (= phi mod O)
-      const float* yb = ys + yidx(q0);          // rows q0 + c at yb[c + c/O]
-      float2 a[NC];
-#pragma unroll
-      for (int m = 0; m < NC; m++) {
-        float zz[2];
-#pragma unroll
-        for (int e = 0; e < 2; e++) {
-          const int tp = 2 * m + e;
-          const float4 w4 = wt[tp];
-          zz[e] = fmaf(w4.x, yb[tp], fmaf(w4.y, yb[tp + (O + 1)],
-                                          fmaf(w4.z, yb[tp + 2 * (O + 1)], w4.w * yb[tp + 3 * (O + 1)])));
-        }
-        a[m] = make_float2(zz[0], zz[1]);
-      }
-      reg_fft_dif<NC>(a);
-      // untangle the real input: W_k = (Z_k + conj Z_{NC-k})/2 + w^k (Z_k - conj Z_{NC-k})/(2i);
-      // packed floats p = 2k, 2k+1 ((W_0, W_{O/2}) at p = 0, 1), one group of
-      // GW floats per store (a whole 32-byte sector when GW = 8)
-#pragma unroll
-      for (int p = 0; p < O; p += GW) {
-        float2 o[GW / 2];
-#pragma unroll
-        for (int h = 0; h < GW / 2; h++) {
-          const int k = p / 2 + h;
-          if (k == 0) {
-            o[h] = make_float2(a[0].x + a[0].y, a[0].x - a[0].y);
-          } else {
-            const float2 z = a[bitrev(k, LOGNC)], c = cconj(a[bitrev(NC - k, LOGNC)]);
-            const float2 E = cscale(cadd(z, c), 0.5f);
-            const float2 D = csub(z, c);
-            const float2 Od = make_float2(0.5f * D.y, -0.5f * D.x);
-            o[h] = cadd(E, cmul(c_fir_tw[k * (64 / O)], Od));
-          }
-        }
-        float* dst = wb + (int64_t)(p / GW) * P * GW;
-        if constexpr (GW == 8) st_global_v8(dst, o[0].x, o[0].y, o[1].x, o[1].y, o[2].x, o[2].y, o[3].x, o[3].y);
-        else *reinterpret_cast<float4*>(dst) = make_float4(o[0].x, o[0].y, o[1].x, o[1].y);
-      }
-    }
-    if (it.last) {
-      float* st = state_out + ((int64_t)it.in * P + it.n) * (4 * O);
-      for (int i = tid; i < 4 * O; i += kFirThreads) st[i] = ys[yidx(4 * O - it.s0 + (acclen - 4 * O + i))];
-    }
+    fold_item_blocks<O>(ys, phi, reinterpret_cast<const float4*>(stage + Lay::XS + Lay::TAPS + Lay::ST), it, fa, P,
+                        S, acclen, state_out, tid);
     __syncthreads();  // ys and this staging buffer are reused next
   }
 }
 
-template <int J, int U, int G, int IW>
+// ---------------------------------------------------------------------------
+// IIR time stage + fold.  Per item each thread
+//  1. runs u = W x and the causal recursion v = u / A over its U rows from
+//     zero state, keeping u and the end state zf (v at its last 3 rows);
+//  2. takes the true state at its start, T(k-1) = zf(k-1) + Phi T(k-2),
+//     as the D-term sum zf(k-1) + Phi zf(k-2) + ... + Phi^(D-1) zf(k-D)
+//     (Phi: U rows of the homogeneous recursion; the dropped Phi^D term is
+//     1/A's impulse response after D*U >= IW rows, below 1e-10 of its peak),
+//     and re-runs v from it;
+//  3. the same for the anti-causal recursion y = v / A(1/z) from its top row
+//     (zero-state pass, states exchanged with the D threads above), writing
+//     the computed rows of y.
+// 16 FMAs per row against 7 (U + 2 IW) / U + 3 (U + IW) / U for per-thread
+// warm-ups of IW rows.
+
+struct Iir3 {
+  float p1, p2, p3;  // outputs at the nearest, second and third rows
+};
+
+// State after U more rows of the homogeneous recursion from s: the start
+// acts as the input u'_0 = -(a1 p1 + a2 p2 + a3 p3), u'_1 = -(a2 p1 + a3 p2),
+// u'_2 = -a3 p1 to the zero-state recursion, whose outputs at rows U-1, U-2,
+// U-3 are those inputs convolved with 1/A's impulse response, hh[i] = h[U-5+i].
+__device__ __forceinline__ Iir3 iir_advance(Iir3 s, float a1, float a2, float a3, const float* hh) {
+  const float u0 = -fmaf(a1, s.p1, fmaf(a2, s.p2, a3 * s.p3));
+  const float u1 = -fmaf(a2, s.p1, a3 * s.p2);
+  const float u2 = -a3 * s.p1;
+  Iir3 r;
+  r.p1 = fmaf(hh[4], u0, fmaf(hh[3], u1, hh[2] * u2));
+  r.p2 = fmaf(hh[3], u0, fmaf(hh[2], u1, hh[1] * u2));
+  r.p3 = fmaf(hh[2], u0, fmaf(hh[1], u1, hh[0] * u2));
+  return r;
+}
+
+// sum over d = 1..D of Phi^(d-1) z(k + dir*d), terms outside [0, nthr) omitted
+template <int D>
+__device__ __forceinline__ Iir3 iir_incoming(const float* z, int k, int dir, int nthr, float a1, float a2, float a3,
+                                             const float* hh) {
+  Iir3 s = {0.f, 0.f, 0.f};
+#pragma unroll
+  for (int d = D; d >= 1; d--) {
+    if (d < D) s = iir_advance(s, a1, a2, a3, hh);
+    const int j = k + dir * d;
+    if (j >= 0 && j < nthr) {
+      s.p1 += z[j];
+      s.p2 += z[kFirThreads + j];
+      s.p3 += z[2 * kFirThreads + j];
+    }
+  }
+  return s;
+}
+
+template <int U, int G, int D>
+__global__ void __launch_bounds__(kFirThreads, 2)
+    iir_fold_kernel(const float* __restrict__ data, int64_t ld, int P, int nslice, int cut, int acclen, int S,
+                    int nseg, int nitems, const float* __restrict__ coef, FoldArgs fa,
+                    const float* __restrict__ state_in, float* __restrict__ state_out) {
+  constexpr int O = 2 * G;
+  using Lay = IirLayout<U, O, D>;
+  static_assert(U >= 5, "the state advance needs U >= 5");
+  extern __shared__ float4 smem4[];
+  float* stage0 = reinterpret_cast<float*>(smem4);
+  float* zf = stage0 + 2 * Lay::STAGE;  // [3][kFirThreads] forward end states
+  float* zb = zf + 3 * kFirThreads;     // [3][kFirThreads] backward end states
+  const int tid = threadIdx.x;
+  // threads that run: up to D past the one holding the last computed row
+  auto threads_of = [](const FirItem& it) { return min(kFirThreads, (D * U + it.nrows - 1) / U + D + 1); };
+
+  auto prefetch = [&](int item, float* stage) {
+    const FirItem it = fir_item(item, nseg, P, S, acclen, O);
+    const float* col = data + ((int64_t)it.in * P + it.n) * ld;
+    const int xbase = cut + it.ylo - D * U - 3, nx = threads_of(it) * U + 3;
+    prefetch_window(stage, col, xbase, nx, nslice, window_shift(col, xbase, nx, nslice), tid);
+    prefetch_item_extras<O>(stage + Lay::XS, kIirCoef, Lay::TAPS, coef, it, P, fa.win, state_in, tid);
+    cp_async_commit();
+  };
+
+  int item = blockIdx.x, buf = 0;
+  if (item < nitems) prefetch(item, stage0);
+  for (; item < nitems; item += gridDim.x, buf ^= 1) {
+    float* stage = stage0 + buf * Lay::STAGE;
+    const int next = item + gridDim.x;
+    if (next < nitems) {
+      prefetch(next, stage0 + (buf ^ 1) * Lay::STAGE);
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
+    }
+    __syncthreads();
+    const FirItem it = fir_item(item, nseg, P, S, acclen, O);
+    const int nthr = threads_of(it);
+    const float* cf = stage + Lay::XS;
+    const float w0 = cf[0], w1 = cf[1], w2 = cf[2], w3 = cf[3];
+    const float a1 = cf[4], a2 = cf[5], a3 = cf[6];
+    const float* hh = cf + (U == kIirU32 ? 8 : 16);
+    float u[U];
+    Iir3 s = {0.f, 0.f, 0.f};
+    if (tid < nthr) {
+      const float* col = data + ((int64_t)it.in * P + it.n) * ld;
+      const int xbase = cut + it.ylo - D * U - 3;
+      const int sh = max(window_shift(col, xbase, nthr * U + 3, nslice), 0);
+      const float* xk = stage + sh + tid * U;  // x of window row tid*U + m at xk[m + 3]
+      float x0 = xk[0], x1 = xk[1], x2 = xk[2];
+#pragma unroll
+      for (int m = 0; m < U; m++) {
+        const float x3 = xk[m + 3];
+        const float ut = fmaf(w0, x3, fmaf(w1, x2, fmaf(w2, x1, w3 * x0)));
+        x0 = x1;
+        x1 = x2;
+        x2 = x3;
+        const float vt = fmaf(-a1, s.p1, fmaf(-a2, s.p2, fmaf(-a3, s.p3, ut)));
+        s.p3 = s.p2;
+        s.p2 = s.p1;
+        s.p1 = vt;
+        u[m] = ut;
+      }
+    }
+    zf[tid] = s.p1;
+    zf[kFirThreads + tid] = s.p2;
+    zf[2 * kFirThreads + tid] = s.p3;
+    __syncthreads();
+    // the x window is dead: y rows go over it
+    float* ys = stage;
+    const int yoff = it.ylo - it.s0 + 4 * O;  // y row of computed row ylo
+    const int phi = y_phase<O>(it, fa);
+    y_edges<O>(ys, phi, stage + Lay::XS + Lay::TAPS, it, yoff, tid);
+    Iir3 q = {0.f, 0.f, 0.f};
+    if (tid < nthr) {
+      s = iir_incoming<D>(zf, tid, -1, nthr, a1, a2, a3, hh);
+#pragma unroll
+      for (int m = 0; m < U; m++) {
+        const float vt = fmaf(-a1, s.p1, fmaf(-a2, s.p2, fmaf(-a3, s.p3, u[m])));
+        s.p3 = s.p2;
+        s.p2 = s.p1;
+        s.p1 = vt;
+        u[m] = vt;
+      }
+#pragma unroll
+      for (int m = U - 1; m >= 0; m--) {
+        const float yt = fmaf(-a1, q.p1, fmaf(-a2, q.p2, fmaf(-a3, q.p3, u[m])));
+        q.p3 = q.p2;
+        q.p2 = q.p1;
+        q.p1 = yt;
+      }
+    }
+    zb[tid] = q.p1;
+    zb[kFirThreads + tid] = q.p2;
+    zb[2 * kFirThreads + tid] = q.p3;
+    __syncthreads();
+    if (tid >= D && tid < nthr) {
+      q = iir_incoming<D>(zb, tid, 1, nthr, a1, a2, a3, hh);
+      const int r0 = (tid - D) * U;  // computed row of this thread's first row
+#pragma unroll
+      for (int m = U - 1; m >= 0; m--) {
+        const float yt = fmaf(-a1, q.p1, fmaf(-a2, q.p2, fmaf(-a3, q.p3, u[m])));
+        q.p3 = q.p2;
+        q.p2 = q.p1;
+        q.p1 = yt;
+        if (r0 + m < it.nrows) ys[yidx<O>(yoff + r0 + m, phi)] = yt;
+      }
+    }
+    __syncthreads();
+    fold_item_blocks<O>(ys, phi, reinterpret_cast<const float4*>(stage + Lay::XS + Lay::TAPS + 4 * O), it, fa, P, S,
+                        acclen, state_out, tid);
+    __syncthreads();  // this staging buffer is refilled next
+  }
+}
+
+template <int S_, int O>
+static int64_t fir_items(const FirArgs& a, int* nseg) {
+  *nseg = std::max(1, (a.acclen + S_ - 1) / S_);
+  return (int64_t)*nseg * a.P * a.ninputs;
+}
+
+template <int J, int U, int G>
 static int launch_fir_t(const FirArgs& a, const FoldArgs& fa, cudaStream_t s) {
   constexpr int O = 2 * G;
-  using Lay = FirLayout<J, U, O, IW>;
-  const int S = Lay::R - 4 * O;
-  const int nseg = std::max(1, (a.acclen + S - 1) / S);
-  const int64_t nitems = (int64_t)nseg * a.P * a.ninputs;
+  using Lay = FirLayout<J, U, O>;
+  constexpr int S = Lay::R - 4 * O;
+  int nseg;
+  const int64_t nitems = fir_items<S, O>(a, &nseg);
   AB_CHECK_ARG(nitems < (1LL << 31), "FIR time stage: too many work items");
-  AB_CHECK_ARG(((uintptr_t)fa.W & 31) == 0 && (a.P % 4) == 0, "FIR time stage: W must be 32-byte aligned");
   const size_t smem = Lay::bytes();
-  AB_CUDA(cudaFuncSetAttribute(fir_fold_kernel<J, U, G, IW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  const int per_sm = (IW > 0 && IW <= 40) || (IW == 0 && J <= 32) ? 2 : 1;
+  AB_CUDA(cudaFuncSetAttribute(fir_fold_kernel<J, U, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const int per_sm = J <= 32 ? 2 : 1;
   const int64_t grid = std::min<int64_t>(nitems, (int64_t)per_sm * std::max(a.num_sms, 1));
-  fir_fold_kernel<J, U, G, IW><<<(unsigned)grid, kFirThreads, smem, s>>>(a.data, a.ld, a.P, a.nslice, a.cut, a.acclen, S,
+  fir_fold_kernel<J, U, G><<<(unsigned)grid, kFirThreads, smem, s>>>(a.data, a.ld, a.P, a.nslice, a.cut, a.acclen, S,
                                                                      nseg, (int)nitems, a.taps, fa, a.state_in,
                                                                      a.state_out);
   AB_LAUNCH_CHECK();
   return AB_OK;
 }
 
-template <int J, int U, int IW>
+template <int U, int G, int D>
+static int launch_iir_t(const FirArgs& a, const FoldArgs& fa, cudaStream_t s) {
+  constexpr int O = 2 * G;
+  using Lay = IirLayout<U, O, D>;
+  constexpr int S = Lay::R - 4 * O;
+  static_assert(S > 0, "IIR tile too small for this osamp");
+  int nseg;
+  const int64_t nitems = fir_items<S, O>(a, &nseg);
+  AB_CHECK_ARG(nitems < (1LL << 31), "IIR time stage: too many work items");
+  const size_t smem = Lay::bytes();
+  AB_CUDA(cudaFuncSetAttribute(iir_fold_kernel<U, G, D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const int64_t grid = std::min<int64_t>(nitems, 2 * (int64_t)std::max(a.num_sms, 1));
+  iir_fold_kernel<U, G, D><<<(unsigned)grid, kFirThreads, smem, s>>>(a.data, a.ld, a.P, a.nslice, a.cut, a.acclen, S,
+                                                                     nseg, (int)nitems, a.taps, fa, a.state_in,
+                                                                     a.state_out);
+  AB_LAUNCH_CHECK();
+  return AB_OK;
+}
+
+template <int J, int U>
 static int launch_fir_o(const FirArgs& a, const FoldArgs& fa, cudaStream_t s) {
   switch (fa.O) {
-    case 4: return launch_fir_t<J, U, 2, IW>(a, fa, s);
-    case 8: return launch_fir_t<J, U, 4, IW>(a, fa, s);
-    case 16: return launch_fir_t<J, U, 8, IW>(a, fa, s);
-    case 32: return launch_fir_t<J, U, 16, IW>(a, fa, s);
-    case 64: return launch_fir_t<J, U, 32, IW>(a, fa, s);
+    case 4: return launch_fir_t<J, U, 2>(a, fa, s);
+    case 8: return launch_fir_t<J, U, 4>(a, fa, s);
+    case 16: return launch_fir_t<J, U, 8>(a, fa, s);
+    case 32: return launch_fir_t<J, U, 16>(a, fa, s);
+    case 64: return launch_fir_t<J, U, 32>(a, fa, s);
     default:
       set_error("FIR time stage: osamp %d not supported (4..64)", fa.O);
+      return AB_ERR_UNSUPPORTED;
+  }
+}
+
+template <int U, int D>
+static int launch_iir_o(const FirArgs& a, const FoldArgs& fa, cudaStream_t s) {
+  switch (fa.O) {
+    case 4: return launch_iir_t<U, 2, D>(a, fa, s);
+    case 8: return launch_iir_t<U, 4, D>(a, fa, s);
+    case 16: return launch_iir_t<U, 8, D>(a, fa, s);
+    case 32: return launch_iir_t<U, 16, D>(a, fa, s);
+    case 64: return launch_iir_t<U, 32, D>(a, fa, s);
+    default:
+      set_error("IIR time stage: osamp %d not supported (4..64)", fa.O);
       return AB_ERR_UNSUPPORTED;
   }
 }
@@ -720,12 +972,20 @@ int launch_fir_fold(const FirArgs& a, const FoldArgs& fa, cudaStream_t s) {
   AB_CHECK_ARG(a.row_tile == 16 || a.row_tile == 32, "FIR time stage: row tile must be 16 or 32");
   AB_CHECK_ARG(a.num_sms > 0, "FIR time stage: SM count unknown");
   AB_CHECK_ARG(a.row_tile * kFirThreads > 4 * fa.O, "FIR time stage: row tile too small for osamp %d", fa.O);
-  // odd row tiles (33, 17 rows per thread) keep the shared loads conflict-free
-  // without padding
-  if (a.iir_w == 40) return a.row_tile == 32 ? launch_fir_o<0, 33, 40>(a, fa, s) : launch_fir_o<0, 17, 40>(a, fa, s);
-  if (a.iir_w == 80) return launch_fir_o<0, 17, 80>(a, fa, s);
-  if (a.J == 32) return a.row_tile == 32 ? launch_fir_o<32, 33, 0>(a, fa, s) : launch_fir_o<32, 17, 0>(a, fa, s);
-  if (a.J == 64) return a.row_tile == 32 ? launch_fir_o<64, 33, 0>(a, fa, s) : launch_fir_o<64, 17, 0>(a, fa, s);
+  AB_CHECK_ARG(((uintptr_t)fa.W & 31) == 0 && (a.P % 4) == 0, "FIR time stage: W must be 32-byte aligned");
+  // odd rows per thread keep the shared loads of lanes U rows apart
+  // conflict-free without padding.  IIR: D = ceil(IW / U) exchanged states.
+  if (a.iir_w > 0) {
+    const int U = a.row_tile == 32 ? kIirU32 : kIirU16;
+    const int D = (a.iir_w + U - 1) / U;
+    if (U == kIirU32 && D == 1) return launch_iir_o<kIirU32, 1>(a, fa, s);
+    if (U == kIirU32 && D == 2) return launch_iir_o<kIirU32, 2>(a, fa, s);
+    if (U == kIirU16 && D == 2) return launch_iir_o<kIirU16, 2>(a, fa, s);
+    if (U == kIirU16 && D == 4) return launch_iir_o<kIirU16, 4>(a, fa, s);
+  } else {
+    if (a.J == 32) return a.row_tile == 32 ? launch_fir_o<32, 33>(a, fa, s) : launch_fir_o<32, 17>(a, fa, s);
+    if (a.J == 64) return a.row_tile == 32 ? launch_fir_o<64, 33>(a, fa, s) : launch_fir_o<64, 17>(a, fa, s);
+  }
   set_error("FIR time stage: J = %d / IW = %d not supported", a.J, a.iir_w);
   return AB_ERR_UNSUPPORTED;
 }

@@ -75,16 +75,17 @@ int launch_time_fold(ab_ctx* ctx, float* buf, int64_t ld, int ninputs, int P, in
 // time stage must run).  Cached in ctx per (P, nslice, ntap, thresh).
 int get_fir_taps(ab_ctx* ctx, int P, int N, int ntap, float thresh, int* J, const float** taps);
 
-// IIR form (fir.cu): per-column (w0..w3, a1..a3, g), (P, 8) float, and the
-// warm-up IW (40 or 80; 0 when the factorisation or warm-up fails).  Cached
-// in ctx per (P, ntap, thresh); ntap must be 4.
+// IIR form (fir.cu): per-column (g w0..g w3, a1..a3, 0, then 1/A's impulse
+// response at the row tiles' state-advance lags), (P, 24) float, and the
+// state-carry length IW (40 or 80; 0 when the factorisation fails or needs
+// longer).  Cached in ctx per (P, ntap, thresh); ntap must be 4.
 int get_iir_coeffs(ab_ctx* ctx, int P, int ntap, float thresh, int* IW, const float** coef);
 
 struct FirArgs {
   const float* data;      // [n][t] window columns, column stride ld
   int64_t ld;
   int P, ninputs, nslice, cut, acclen;
-  const float* taps;      // FIR taps (P, 2J+1) or IIR coefficients (P, 8)
+  const float* taps;      // FIR taps (P, 2J+1) or IIR coefficients (P, 24)
   int J;                  // FIR: 32 or 64 (ignored when iir_w > 0)
   int row_tile;           // kept rows per thread: 16 or 32
   const float* state_in;  // previous chunk's last 4*O rows (ninputs, P, 4*O)
