@@ -31,6 +31,11 @@ SIGNATURES = {
     "ab_unpack_1bit": (I32, [P, P, P, I64, I64, P, I64, I64, P]),
     "ab_sortpols": (I32, [P, P, P, I64, I64, I64, I64, I32, I64, I64, P]),
     "ab_make_continuous": (I32, [P, I64, I64, P, I64, P, I64, I64, P, P]),
+    "ab_hist": (I32, [P, P, I64, I64, I64, I32, I32, P]),
+    "ab_packets_to_rows": (I32, [P, I64, I64, P, P]),
+    "ab_spec_map_init": (I32, [P, I64, P]),
+    "ab_spec_map_add": (I32, [P, I64, I32, I64, I64, P, I64, P]),
+    "ab_spec_map_finish": (I32, [P, I64, P]),
     "ab_get_matft": (I32, [P, P, I64, I64, I64, P]),
     "ab_calculate_filter": (I32, [P, P, I64, D, P]),
     "ab_build_filter": (I32, [P, P, I64, I64, I64, D, P]),

@@ -4,6 +4,8 @@
 // 4-bit rule (albatros_analysis/src/correlations/unpacking.c:187-202): a
 // nibble v maps to v-16 when v > 8, else v, so 0x8 decodes to +8.  In integer
 // form that is ((v + 7) & 15) - 7, which the kernels use.
+#include <algorithm>
+
 #include "common.cuh"
 
 namespace ab {
@@ -113,6 +115,93 @@ __global__ void place_kernel(const float2* __restrict__ spec, int64_t nrows, int
   out[row * nchans + channels[k]] = spec[idx];
 }
 
+
+// ---------------------------------------------------------------------------
+// Quantisation histograms (hist_4bit / hist_1bit,
+// albatros_analysis/src/correlations/unpacking.c:7-153): hist[bin][c] counts
+// the real and imaginary levels of channel c (pol0, pol1 or both), a 4-bit
+// level at its raw nibble (bins 0..15), a 1-bit level at its bit (bins 0, 1).
+// One thread per (channel or byte column, row phase); CTAs cover a slab of
+// rows, so the reads of a warp are a contiguous piece of each row.
+constexpr int kHistTC = 128, kHistRY = 2;
+
+// 4-bit: per-CTA 32-bit counters in shared memory, [bin][column in tile]
+// (lanes on consecutive columns never share a bank), added into the 64-bit
+// global histogram once per CTA.
+__global__ void __launch_bounds__(kHistTC* kHistRY)
+    hist4_kernel(const uint8_t* __restrict__ data, int64_t row_bytes, int64_t rowstart, int64_t nrows, int nchan,
+                 int mode, int64_t rows_per_cta, unsigned long long* __restrict__ hist) {
+  __shared__ unsigned sh[16 * kHistTC];
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * kHistTC + tx;
+  for (int i = tid; i < 16 * kHistTC; i += kHistTC * kHistRY) sh[i] = 0u;
+  __syncthreads();
+  const int c = blockIdx.x * kHistTC + tx;
+  const int64_t r0 = (int64_t)blockIdx.y * rows_per_cta;
+  const int64_t r1 = min(nrows, r0 + rows_per_cta);
+  if (c < nchan) {
+    const uint8_t* p = data + (rowstart + r0 + ty) * row_bytes + 2 * c;
+#pragma unroll 4
+    for (int64_t r = r0 + ty; r < r1; r += kHistRY, p += kHistRY * row_bytes) {
+      const uchar2 b = *reinterpret_cast<const uchar2*>(p);  // pol0 byte, pol1 byte
+      if (mode != 1) {
+        atomicAdd(&sh[(b.x >> 4) * kHistTC + tx], 1u);
+        atomicAdd(&sh[(b.x & 15) * kHistTC + tx], 1u);
+      }
+      if (mode != 0) {
+        atomicAdd(&sh[(b.y >> 4) * kHistTC + tx], 1u);
+        atomicAdd(&sh[(b.y & 15) * kHistTC + tx], 1u);
+      }
+    }
+  }
+  __syncthreads();
+  if (c < nchan)
+    for (int bin = ty; bin < 16; bin += kHistRY) {
+      const unsigned v = sh[bin * kHistTC + tx];
+      if (v) atomicAdd(&hist[(int64_t)bin * nchan + c], (unsigned long long)v);
+    }
+}
+
+// 1-bit: byte j of a row holds channels 2j (bits 7..4: r pol0, i pol0,
+// r pol1, i pol1) and 2j+1 (bits 3..0, same order); each thread counts the
+// set bits of its column's two channels in registers.
+__global__ void __launch_bounds__(kHistTC* kHistRY)
+    hist1_kernel(const uint8_t* __restrict__ data, int64_t row_bytes, int64_t rowstart, int64_t nrows, int ncols,
+                 int mode, int64_t rows_per_cta, unsigned long long* __restrict__ hist) {
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int j = blockIdx.x * kHistTC + tx;
+  const int64_t r0 = (int64_t)blockIdx.y * rows_per_cta;
+  const int64_t r1 = min(nrows, r0 + rows_per_cta);
+  if (j >= ncols || r0 + ty >= r1) return;
+  const unsigned m0 = mode == 0 ? 0xC0u : mode == 1 ? 0x30u : 0xF0u;  // channel 2j's bits
+  const unsigned m1 = m0 >> 4;                                        // channel 2j+1's bits
+  unsigned ones0 = 0, ones1 = 0;
+  const uint8_t* p = data + (rowstart + r0 + ty) * row_bytes + j;
+  int64_t rows = 0;
+#pragma unroll 4
+  for (int64_t r = r0 + ty; r < r1; r += kHistRY, p += kHistRY * row_bytes) {
+    const unsigned b = *p;
+    ones0 += __popc(b & m0);
+    ones1 += __popc(b & m1);
+    rows++;
+  }
+  const unsigned long long levels = (unsigned long long)rows * (mode == -1 ? 4u : 2u);
+  const int nchan = 2 * ncols;
+  atomicAdd(&hist[nchan + 2 * j], (unsigned long long)ones0);
+  atomicAdd(&hist[nchan + 2 * j + 1], (unsigned long long)ones1);
+  atomicAdd(&hist[2 * j], levels - ones0);
+  atomicAdd(&hist[2 * j + 1], levels - ones1);
+}
+
+static int sm_count() {
+  static int n = 0;
+  if (n == 0) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        n <= 0)
+      n = 1;
+  }
+  return n;
+}
 }  // namespace ab
 
 using namespace ab;
@@ -199,5 +288,37 @@ extern "C" int ab_make_continuous(const float* spec, int64_t nrows, int64_t ncol
                                                                   (float2*)out);
     AB_LAUNCH_CHECK();
   }
+  return AB_OK;
+}
+
+extern "C" int ab_hist(const uint8_t* data, uint64_t* hist, int64_t rowstart, int64_t rowend, int64_t nchan,
+                       int bit_depth, int mode, void* stream) {
+  AB_CHECK_ARG(data && hist, "ab_hist: NULL pointer");
+  AB_CHECK_ARG(bit_depth == 1 || bit_depth == 4, "ab_hist: bit_depth must be 1 or 4");
+  AB_CHECK_ARG(mode == 0 || mode == 1 || mode == -1, "ab_hist: mode must be 0, 1 or -1");
+  AB_CHECK_ARG(nchan > 0 && nchan <= (1 << 30) && rowstart >= 0 && rowend >= rowstart, "ab_hist: bad sizes");
+  AB_CHECK_ARG(bit_depth == 4 || nchan % 2 == 0, "ab_hist: 1-bit data needs an even channel count");
+  AB_CHECK_ARG(bit_depth == 1 || ((uintptr_t)data & 1) == 0, "ab_hist: 4-bit data must be 2-byte aligned");
+  cudaStream_t s = as_stream(stream);
+  const int64_t nbins = bit_depth == 4 ? 15 : 1;
+  AB_CUDA(cudaMemsetAsync(hist, 0, sizeof(uint64_t) * (size_t)((nbins + 1) * nchan), s));
+  const int64_t nrows = rowend - rowstart;
+  if (nrows == 0) return AB_OK;
+  const int64_t cols = bit_depth == 4 ? nchan : nchan / 2;  // thread columns
+  const int64_t gx = (cols + kHistTC - 1) / kHistTC;
+  AB_CHECK_ARG(gx <= 65535, "ab_hist: too many channels");
+  // about 8 CTAs per SM, each at least 256 rows
+  const int64_t want = std::max<int64_t>(1, (8 * (int64_t)sm_count() + gx - 1) / gx);
+  const int64_t gy = std::min<int64_t>(std::min<int64_t>(want, (nrows + 255) / 256), 65535);
+  const int64_t rows_per = (nrows + gy - 1) / gy;
+  AB_CHECK_ARG(rows_per < (1LL << 29), "ab_hist: too many rows per CTA");
+  const dim3 grid((unsigned)gx, (unsigned)((nrows + rows_per - 1) / rows_per)), block(kHistTC, kHistRY);
+  if (bit_depth == 4)
+    hist4_kernel<<<grid, block, 0, s>>>(data, 2 * nchan, rowstart, nrows, (int)nchan, mode, rows_per,
+                                        reinterpret_cast<unsigned long long*>(hist));
+  else
+    hist1_kernel<<<grid, block, 0, s>>>(data, nchan / 2, rowstart, nrows, (int)(nchan / 2), mode, rows_per,
+                                        reinterpret_cast<unsigned long long*>(hist));
+  AB_LAUNCH_CHECK();
   return AB_OK;
 }

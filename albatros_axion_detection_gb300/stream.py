@@ -18,7 +18,7 @@ from typing import List, Optional, Tuple
 import numpy as np
 import torch
 
-from . import _lib
+from . import _lib, output
 from ._arrays import device_array, host_int64
 
 
@@ -188,7 +188,8 @@ def _device_view(addr: int, n: int) -> torch.Tensor:
 
 
 def repfb_xcorr_avg(raw, channels, acclen: int, nchunks: int, nblock: int, chanstart: int, chanend: int, osamp: int,
-                    cut: int = 10, filt_thresh: float = 0.45, ntap: int = 4, spec_map=None, bits: int = 4):
+                    cut: int = 10, filt_thresh: float = 0.45, ntap: int = 4, spec_map=None, bits: int = 4,
+                    with_missing: bool = False):
     """Streaming unpack -> IPFB -> PFB -> xcorr over device-resident packets.
 
     raw: (nant, nspec, 2*nchan_raw) uint8 device array of 4-bit packets, or
@@ -196,7 +197,9 @@ def repfb_xcorr_avg(raw, channels, acclen: int, nchunks: int, nblock: int, chans
     channel numbers of the raw columns; [chanstart, chanend) selects the
     coarse channels.  Returns (vis, freqs): vis (M, M, nchan, njobs) complex64
     F-ordered (numpy, NaNs masked as the reference does) and the fine
-    channel numbers."""
+    channel numbers; with_missing=True returns (vis, missing_fraction, freqs)
+    like the reference (helper_gpu_stream_clean.py:402), missing_fraction
+    (nant, njobs) the per-job missing-spectrum percentage of each antenna."""
     r = device_array(raw, torch.uint8, "raw")
     ch = host_int64(channels)
     nchan_raw = r.shape[2] // 2 if bits == 4 else r.shape[2] * 2
@@ -208,5 +211,9 @@ def repfb_xcorr_avg(raw, channels, acclen: int, nchunks: int, nblock: int, chans
         v = sc.vis_device().permute(1, 2, 3, 0).cpu().numpy()  # (M, M, nq, njobs)
     finally:
         sc.close()
-    vis = np.ma.masked_invalid(np.asfortranarray(v))
-    return vis, np.arange(sc.q0, sc.q1)
+    vis = output.mask_invalid(np.asfortranarray(v))
+    freqs = np.arange(sc.q0, sc.q1)
+    if not with_missing:
+        return vis, freqs
+    present = output.chunk_presence(spec_map, r.shape[0], nchunks, acclen)
+    return vis, output.missing_fraction(present, acclen, nblock, osamp, ntap), freqs

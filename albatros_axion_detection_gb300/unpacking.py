@@ -1,6 +1,6 @@
 """Packed-baseband unpacking on the GPU: the call surface of
 albatros_analysis/src/correlations/unpacking.py (unpack_4bit :193-245,
-unpack_1bit :248-302, sortpols :305-377), computed by the CUDA kernels of
+unpack_1bit :248-302, sortpols :305-377, hist :82-138), computed by the CUDA kernels of
 csrc/unpack.cu through the C-ABI."""
 from __future__ import annotations
 
@@ -112,3 +112,27 @@ def sortpols(data, length_channels, bit_mode, rowstart, rowend, chanstart, chane
         _lib.call("ab_sortpols", d.data_ptr(), pol0.data_ptr(), pol1.data_ptr(), rowstart, rowend, ncols,
                   length_channels, int(bit_mode), chanstart, chanend, _lib.stream_ptr(d))
     return pol0, pol1
+
+
+def hist(data, rowstart, rowend, length_channels, bit_depth, mode):
+    """Histogram of quantisation levels: device uint64 (2**bit_depth, length_channels).
+
+    hist[v, c] counts the real and imaginary levels of channel c in rows
+    [rowstart, rowend) equal to v (the raw nibble for 4-bit data, the bit for
+    1-bit data), over pol0 (mode 0), pol1 (mode 1) or both (mode -1).  The
+    reference asserts on a bad bit_depth or mode; here they raise ValueError."""
+    d = device_array(data, torch.uint8, "data")
+    rowstart, rowend, length_channels = int(rowstart), int(rowend), int(length_channels)
+    if bit_depth not in (1, 4):
+        raise ValueError(f"bit_depth set to {bit_depth}, only takes values 1 or 4")
+    if mode not in (0, 1, -1):
+        raise ValueError(f"mode set to {mode}, only takes values 0,1,-1")
+    if rowstart < 0 or rowend < rowstart:
+        raise ValueError(f"bad row range [{rowstart}, {rowend})")
+    if bit_depth == 1 and length_channels % 2:
+        raise ValueError("1-bit data needs an even number of channels")
+    _rows_view(d, 2 * length_channels if bit_depth == 4 else length_channels // 2, rowend)
+    out = torch.empty((2 ** bit_depth, length_channels), dtype=torch.uint64, device=d.device)
+    _lib.call("ab_hist", d.data_ptr(), out.data_ptr(), rowstart, rowend, length_channels, int(bit_depth), int(mode),
+              _lib.stream_ptr(d))
+    return out

@@ -109,6 +109,34 @@ int ab_sortpols(const uint8_t *data, uint8_t *pol0, uint8_t *pol1, int64_t rowst
                 int64_t ncols, int64_t nchan, int bit_depth, int64_t chanstart, int64_t chanend,
                 void *stream);
 
+/* ab_hist: replaces hist_4bit / hist_1bit
+ * (albatros_analysis/src/correlations/unpacking.c:7-153) behind hist
+ * (albatros_analysis/src/correlations/unpacking.py:82-138), on the device.
+ * data: (nspec, 2*nchan) bytes (bit_depth 4) or (nspec, nchan/2) (bit_depth
+ * 1, nchan even); hist: device uint64 (2^bit_depth, nchan), overwritten:
+ * hist[v][c] = number of real and imaginary levels of channel c in rows
+ * [rowstart, rowend) equal to v (the raw nibble for 4-bit, the bit for
+ * 1-bit), over pol0 (mode 0), pol1 (mode 1) or both (mode -1). */
+int ab_hist(const uint8_t *data, uint64_t *hist, int64_t rowstart, int64_t rowend, int64_t nchan,
+            int bit_depth, int mode, void *stream);
+
+/* Baseband file ingest on the device (replaces the per-chunk host loop of
+ * BasebandFileIterator.__next__, albatros_analysis/src/correlations/
+ * baseband_data_classes.py:614-715, with fill_arr :16-45 and
+ * get_rows_from_specnum :493-519).
+ * ab_packets_to_rows: body = npkt packets of bytes_per_packet bytes (a
+ *   big-endian uint32 spectrum number, then the spectra); rows = the
+ *   npkt*(bytes_per_packet-4) spectra bytes, packet after packet.
+ * ab_spec_map_init / _add / _finish: build spec_map (nmap int32) with
+ *   spec_map[g] = the lowest row holding spectrum number start + g, or -1;
+ *   _add is called once per file with its wrap-corrected per-packet
+ *   spectrum numbers (device int64, npkt) and the file's first row row0. */
+int ab_packets_to_rows(const uint8_t *body, int64_t npkt, int64_t bytes_per_packet, uint8_t *rows, void *stream);
+int ab_spec_map_init(int32_t *spec_map, int64_t nmap, void *stream);
+int ab_spec_map_add(const int64_t *specnum, int64_t npkt, int32_t spp, int64_t row0, int64_t start,
+                    int32_t *spec_map, int64_t nmap, void *stream);
+int ab_spec_map_finish(int32_t *spec_map, int64_t nmap, void *stream);
+
 /* ab_make_continuous: replaces make_continuous_gpu
  * (albatros_analysis/src/correlations/baseband_data_classes.py:48-73).
  * spec: c64 (nrows, ncols); specnum: device int64 (nrows); channels: device

@@ -116,3 +116,75 @@ def pack_1bit(r0, i0, r1, i1) -> np.ndarray:
 
 def fixture_1bit_packed() -> np.ndarray:
     return pack_1bit(*fixture_1bit_values()).reshape(1, -1)
+
+
+# ---------------------------------------------------------------------------
+# Baseband files.  Layout of the reference's file writer
+# (src/correlations/tests/generate_test_baseband.py:54-101): big-endian uint64
+# [80 + 8*len(chans), bytes_per_packet, len(chans), spectra_per_packet, bits,
+# have_trimble], the channel list (one entry per spectrum byte) as uint64,
+# [gps_week, gps_time] uint64, [lat, lon, elev] float64; then packets of a
+# big-endian uint32 spectrum number and the spectra bytes.
+
+def header_channels(chan0: int, nchan: int, bits: int) -> np.ndarray:
+    """Channel list of a contiguous band as the digitiser writes it: each
+    4-bit channel twice (pol0 and pol1 bytes), every other 1-bit channel."""
+    if bits == 4:
+        c = np.arange(chan0, chan0 + nchan)
+        return np.ravel(np.column_stack((c, c)))
+    return np.arange(chan0, chan0 + nchan, 2)
+
+
+def write_baseband(path: str, specnums, spp: int, chans, bits: int, payload: np.ndarray, gps_time: int = 1721800000):
+    """payload: (npkt, spp * len(chans)) uint8; specnums: per packet (taken mod 2^32)."""
+    chans = np.asarray(chans)
+    bpp = spp * len(chans) + 4
+    payload = np.asarray(payload, np.uint8).reshape(len(specnums), bpp - 4)
+    pk = np.zeros(len(specnums), dtype=[("spec_num", ">u4"), ("spectra", f"{bpp - 4}u1")])
+    pk["spec_num"] = np.asarray(specnums, dtype=np.int64) % (1 << 32)
+    pk["spectra"] = payload
+    with open(path, "wb") as f:
+        np.asarray([80 + 8 * len(chans), bpp, len(chans), spp, bits, 0], dtype=">u8").tofile(f)
+        np.asarray(chans, dtype=">u8").tofile(f)
+        np.asarray([0, gps_time], dtype=">u8").tofile(f)
+        np.asarray([0.0, 0.0, 0.0], dtype=">f8").tofile(f)
+        pk.tofile(f)
+
+
+def baseband_scenarios():
+    """name -> dict(files=[(specnums, spp, chan0, nchan, bits, seed)], acclen, nchunks, idxstart).
+    wrap: the reference's spectrum-number wrap trio (generate_test_baseband.py:
+    171-179: a wrap inside file 1 with a dropped packet, file 2 continuing
+    after it, a second wrap inside file 3); gaps4 / gaps1: dropped packets
+    inside files and gaps between them, 4-bit and 1-bit."""
+    rng = np.random.default_rng(2024)
+
+    def drop(sn, frac):
+        keep = rng.random(len(sn)) > frac
+        keep[0] = True
+        return np.asarray(sn)[keep]
+    s1 = (1 << 32) - 10 + 5 * np.arange(7)
+    wrap = dict(files=[(np.delete(s1, 2), 5, 452, 2, 4, 1), (25 + 5 * np.arange(3), 5, 452, 2, 4, 2),
+                       (np.array([40, 5, 10]), 5, 452, 2, 4, 3)], acclen=10, nchunks=6, idxstart=0)
+    a = 1000 + 7 * np.arange(60)
+    b = a[-1] + 7 * 9 + 7 * np.arange(50)
+    c = b[-1] + 7 * 3 + 7 * np.arange(70)
+    gaps4 = dict(files=[(drop(a, 0.15), 7, 100, 6, 4, 4), (drop(b, 0.1), 7, 100, 6, 4, 5),
+                        (drop(c, 0.2), 7, 100, 6, 4, 6)], acclen=50, nchunks=20, idxstart=13)
+    d = 77 + 4 * np.arange(45)
+    e = d[-1] + 4 * 5 + 4 * np.arange(40)
+    gaps1 = dict(files=[(drop(d, 0.1), 4, 200, 8, 1, 7), (drop(e, 0.2), 4, 200, 8, 1, 8)], acclen=24, nchunks=12,
+                 idxstart=3)
+    return {"wrap": wrap, "gaps4": gaps4, "gaps1": gaps1}
+
+
+def write_scenario(sc: dict, dirpath: str, name: str):
+    """Write a scenario's files; returns their paths."""
+    paths = []
+    for k, (sn, spp, chan0, nchan, bits, seed) in enumerate(sc["files"]):
+        chans = header_channels(chan0, nchan, bits)
+        pay = np.random.default_rng(seed).integers(0, 256, (len(sn), spp * len(chans)), dtype=np.uint8)
+        p = f"{dirpath}/{name}_{k}.raw"
+        write_baseband(p, sn, spp, chans, bits, pay)
+        paths.append(p)
+    return paths

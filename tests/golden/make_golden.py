@@ -46,6 +46,8 @@ def ref_c():
     up.unpack_4bit_float.argtypes = [P, P, P, I, I, P, I, I]
     up.unpack_1bit_float.argtypes = [P, P, P, I, I, I, I, I]
     up.sortpols.argtypes = [P, P, P, I, I, I, I, S, I, I]
+    up.hist_4bit.argtypes = [P, P, I, I, I, I, I]
+    up.hist_1bit.argtypes = [P, P, I, I, I, I, I]
     co.avg_xcorr_4bit.argtypes = [P, P, P, I, I]
     co.avg_xcorr_4bit_2ant.argtypes = [P, P, P, P, P, ctypes.c_int64, ctypes.c_int64, I, I, I]
     co.avg_xcorr_4bit_2ant.restype = I
@@ -110,6 +112,156 @@ def unpack_cases(up):
     return out
 
 
+def ref_hist(up, raw2d, r0, r1, nchan, bits, mode):
+    """The reference's hist_4bit / hist_1bit (unpacking.c:7-153).  Its final
+    merge loop runs k <= hist_len, one element past the histogram, so the
+    buffer gets one spare element, dropped here."""
+    nbins = 2 ** bits - 1
+    h = np.zeros((nbins + 1) * nchan + 1, dtype=np.uint64)
+    raw2d = np.ascontiguousarray(raw2d)
+    fn = up.hist_4bit if bits == 4 else up.hist_1bit
+    fn(raw2d.ctypes.data, h.ctypes.data, r0, r1, nchan, nbins, mode)
+    return h[:-1].reshape(nbins + 1, nchan)
+
+
+def hist_cases(up):
+    out = {}
+    packed, p1 = gen.fixture_4bit_packed(), gen.fixture_1bit_packed()
+    raw, raw1 = gen.raw_4bit(seed=11, nspec=300, nchan=64), gen.raw_1bit(seed=12, nspec=300, nchan=64)
+    for mode in (0, 1, -1):
+        m = "b" if mode == -1 else str(mode)
+        out[f"h4_fix_{m}"] = ref_hist(up, packed.reshape(-1, 20), 0, 2, 10, 4, mode)
+        out[f"h4_rand_{m}"] = ref_hist(up, raw, 7, 291, 64, 4, mode)
+        out[f"h1_fix_{m}"] = ref_hist(up, p1.reshape(-1, 4), 0, 2, 8, 1, mode)
+        out[f"h1_rand_{m}"] = ref_hist(up, raw1, 3, 299, 64, 1, mode)
+    return out
+
+
+def missing_cases():
+    """missing_fraction of the reference's streaming driver
+    (scripts/xcorr/helper_gpu_stream_clean.py): its own ProcessingConfig,
+    BufferSizes, BufferManager, MissingDataTracker, JobChunkPlanner and
+    _process_antenna_pol, taken from the source with ``cupy`` bound to NumPy,
+    driven by the job loop of its repfb_xcorr_avg (:355-372) with the IPFB
+    and make_continuous_gpu stubbed out (they do not touch the bookkeeping).
+    Chunks carry only their present spectrum numbers."""
+    import ast
+    from dataclasses import dataclass
+    from typing import List, Optional, Tuple
+    path = os.path.join(REF, "albatros_analysis", "scripts", "xcorr", "helper_gpu_stream_clean.py")
+    tree = ast.parse(open(path).read())
+    keep = {"ProcessingConfig", "BufferSizes", "BufferManager", "MissingDataTracker", "JobChunkPlanner",
+            "_process_antenna_pol"}
+    mod = ast.Module(body=[n for n in tree.body if getattr(n, "name", None) in keep], type_ignores=[])
+
+    class _Bdc:
+        @staticmethod
+        def make_continuous_gpu(pol, specnums, start, channels, nspec, nchans=2049):
+            return np.zeros((nspec, nchans), np.complex64)
+
+    ns = dict(np=np, cp=np, dataclass=dataclass, List=List, Tuple=Tuple, Optional=Optional, bdc=_Bdc)
+    exec(compile(mod, path, "exec"), ns)
+    out = {}
+    rng = np.random.default_rng(77)
+    for k, (nant, acclen, nblock, osamp, nchunks) in enumerate([(2, 64, 5, 4, 13), (3, 16, 8, 16, 20),
+                                                                (2, 32, 3, 64, 17), (1, 128, 40, 4, 9)]):
+        cfg = ns["ProcessingConfig"](acclen=acclen, pfb_size=0, nchunks=nchunks, nblock=nblock, chanstart=0,
+                                     chanend=4, osamp=osamp, cut=2)
+        sizes = ns["BufferSizes"].from_config(cfg)
+        present = rng.integers(acclen // 2, acclen + 1, (nant, nchunks))
+        present[:, rng.random(nchunks) < 0.3] = acclen  # some complete chunks
+        jobs = [tuple({"specnums": np.arange(present[a, c]), "pol0": None, "pol1": None} for a in range(nant))
+                for c in range(nchunks)]
+
+        class _Ipfb:
+            def process_chunk(self, chunk, pol_idx, start_specnum, cut_pol):
+                return np.zeros(sizes.lchunk, np.float32)
+
+        bm = ns["BufferManager"](cfg, sizes, nant)
+        plan = ns["JobChunkPlanner"].plan_chunks(nchunks, sizes.lchunk, nblock, sizes.lblock, cfg.ntap)
+        tracker = ns["MissingDataTracker"](nant, len(plan))
+        for job_idx, (c0, c1) in enumerate(plan):
+            bm.reset_overlap_region()
+            sub = jobs[c0:c1] if c1 is not None else jobs[c0:]
+            for a in range(nant):
+                for p in range(cfg.npol):
+                    ns["_process_antenna_pol"](a, p, sub, bm, _Ipfb(), tracker, job_idx, 0, np.arange(4), cfg,
+                                               sizes, False)
+        out[f"mf{k}_cfg"] = np.array([nant, acclen, nblock, osamp, nchunks])
+        out[f"mf{k}_present"] = present
+        out[f"mf{k}_out"] = tracker.missing_fraction
+    return out
+
+
+def ingest_cases():
+    """Baseband / BasebandFileIterator of the reference
+    (src/correlations/baseband_data_classes.py), taken from the source with
+    xp = NumPy and numba's njit / prange as identity / range, run on the
+    scenario files of gen.baseband_scenarios().  The iterator's float loader
+    unpacks nothing here: each chunk row it fills is tagged (row in file,
+    file index), so the fixture records which file row serves each present
+    spectrum, beside the chunk's spectrum numbers.  Also each file's header
+    fields and wrap-fixed per-packet spectrum numbers as Baseband reads them."""
+    import ast
+    import contextlib
+    import io as _io
+    import struct
+    import time
+    import types
+    path = os.path.join(REF, "albatros_analysis", "src", "correlations", "baseband_data_classes.py")
+    tree = ast.parse(open(path).read())
+    keep = {"fill_arr_cpu", "fill_arr", "add_constant_cpu", "add_constant", "get_rows_from_specnum", "Baseband",
+            "BasebandFloat", "BasebandFileIterator"}
+    mod = ast.Module(body=[n for n in tree.body if getattr(n, "name", None) in keep], type_ignores=[])
+    nb = types.SimpleNamespace(njit=lambda *a, **k: (lambda f: f), prange=range)
+    ns = dict(np=np, xp=np, nb=nb, os=os, struct=struct, time=time, unpk=None)
+    exec(compile(mod, path, "exec"), ns)
+    files_by_name = {}
+
+    class TaggedFloat(ns["BasebandFloat"]):
+        def __init__(self, file_name, *a, **k):
+            super().__init__(file_name, *a, **k)
+            self._fid = files_by_name[file_name]
+
+        def _unpack(self, rowstart, rowend):
+            rows = np.arange(rowstart, rowend, dtype=np.float32)[:, None] + 1j * np.float32(self._fid)
+            v = np.broadcast_to(rows, (rowend - rowstart, len(self.channel_idxs))).astype(np.complex64)
+            return v, v
+
+    ns["BasebandFloat"] = TaggedFloat
+    out = {}
+    with tempfile.TemporaryDirectory() as d:
+        for name, sc in gen.baseband_scenarios().items():
+            paths = gen.write_scenario(sc, d, name)
+            files_by_name.clear()
+            files_by_name.update({p: k for k, p in enumerate(paths)})
+            with contextlib.redirect_stdout(_io.StringIO()):
+                for k, p in enumerate(paths):
+                    b = ns["Baseband"](p)
+                    out[f"bb_{name}_{k}_hdr"] = np.array([b.header_bytes, b.bytes_per_packet, b.length_channels,
+                                                          b.spectra_per_packet, b.bit_mode, b.num_packets])
+                    out[f"bb_{name}_{k}_chans"] = np.asarray(b.channels, np.int64)
+                    out[f"bb_{name}_{k}_specnum"] = np.asarray(b.spec_num, np.int64)
+                    out[f"bb_{name}_{k}_overflowed"] = np.array(b._overflowed)
+                it = ns["BasebandFileIterator"](paths, 0, sc["idxstart"], sc["acclen"], nchunks=sc["nchunks"],
+                                                type="float")
+                start0 = int(it.spec_num_start)
+                sn, rows, fid, counts = [], [], [], []
+                for chunk in it:
+                    n = len(chunk["specnums"])
+                    counts.append(n)
+                    sn.append(chunk["specnums"])
+                    rows.append(chunk["pol0"][:n, 0].real.astype(np.int64))
+                    fid.append(chunk["pol0"][:n, 0].imag.astype(np.int64))
+                    assert not chunk["pol0"][n:].any()
+            out[f"bfi_{name}_start"] = np.array(start0)
+            out[f"bfi_{name}_counts"] = np.array(counts)
+            out[f"bfi_{name}_specnums"] = np.concatenate(sn)
+            out[f"bfi_{name}_rows"] = np.concatenate(rows)
+            out[f"bfi_{name}_files"] = np.concatenate(fid)
+    return out
+
+
 def xcorr_cases(co):
     out = {}
     d0, d1 = gen.sorted_4bit_pair(seed=21, nrows=2000, ncol=33)
@@ -168,6 +320,9 @@ def main():
     fx = {}
     fx.update(unpack_cases(up))
     fx.update(xcorr_cases(co))
+    fx.update(hist_cases(up))
+    fx.update(missing_cases())
+    fx.update(ingest_cases())
     np.savez_compressed(os.path.join(HERE, "golden_int.npz"), **fx)
     np.savez_compressed(os.path.join(HERE, "golden_pfb.npz"), **pfb_cases())
     print("wrote golden_int.npz, golden_pfb.npz")

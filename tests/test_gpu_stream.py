@@ -60,6 +60,14 @@ def test_stream_missing_spectra():
     vis, _ = run(raw, np.arange(200, 208), spec_map=spec_map, **kw)
     ref, _ = po.repfb_xcorr_avg(raw, np.arange(200, 208), spec_present=present, **kw)
     check(vis, ref)
+    # the reference's return with the missing-data percentage per antenna and job
+    from albatros_axion_detection_gb300 import output, stream
+    v2, mf, freqs = stream.repfb_xcorr_avg(torch.from_numpy(raw).cuda(), np.arange(200, 208),
+                                           spec_map=torch.from_numpy(spec_map).cuda(), with_missing=True, **kw)
+    assert np.array_equal(np.asarray(v2), vis) and len(freqs) == vis.shape[2]
+    counts = present.reshape(nant, nchunks, acclen).sum(-1)
+    assert mf.shape == (nant, vis.shape[-1]) and mf.max() > 0
+    np.testing.assert_array_equal(mf, output.missing_fraction(counts, acclen, 16, 4))
 
 
 def test_stream_channel_subset_and_gap_in_channel_numbers():

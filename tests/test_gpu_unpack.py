@@ -101,3 +101,41 @@ def test_make_continuous():
     full = cu(spec[:, :1])
     same = make_continuous_gpu(full, np.arange(50), 0, [0], 50, nchans=1)
     assert same.data_ptr() == full.data_ptr()
+
+
+@pytest.mark.parametrize("mode", [0, 1, -1])
+@pytest.mark.parametrize("name,bits,nchan,rows", [("h4_fix", 4, 10, (0, 2)), ("h4_rand", 4, 64, (7, 291)),
+                                                  ("h1_fix", 1, 8, (0, 2)), ("h1_rand", 1, 64, (3, 299))])
+def test_hist_golden(golden_int, name, bits, nchan, rows, mode):
+    from albatros_axion_detection_gb300.unpacking import hist
+    from tests.test_oracle_golden import hist_input
+    h = hist(cu(hist_input(name)), rows[0], rows[1], nchan, bits, mode)
+    assert h.dtype == torch.uint64 and h.shape == (2 ** bits, nchan)
+    np.testing.assert_array_equal(h.cpu().numpy(), golden_int[f"{name}_{'b' if mode == -1 else mode}"])
+
+
+@pytest.mark.parametrize("bits,nchan,nspec,r0,r1", [(4, 300, 70001, 13, 69990), (4, 2048, 4096, 0, 4096),
+                                                    (4, 3, 5000, 1, 4999), (1, 130, 90001, 5, 90000),
+                                                    (1, 2048, 3000, 0, 3000), (1, 2, 700, 0, 1)])
+def test_hist_vs_oracle(bits, nchan, nspec, r0, r1):
+    """Many CTAs over rows and channel tiles, ragged tile and row edges."""
+    from albatros_axion_detection_gb300.unpacking import hist
+    raw = gen.raw_4bit_uniform(seed=nchan, nspec=nspec, nchan=nchan) if bits == 4 else \
+        gen.raw_1bit(seed=nchan, nspec=nspec, nchan=nchan)
+    d = cu(raw)
+    for mode in (0, 1, -1):
+        np.testing.assert_array_equal(hist(d, r0, r1, nchan, bits, mode).cpu().numpy(),
+                                      io.hist(raw, r0, r1, nchan, bits, mode))
+
+
+def test_hist_edge_cases():
+    from albatros_axion_detection_gb300.unpacking import hist
+    d = cu(gen.raw_4bit_uniform(seed=3, nspec=10, nchan=8))
+    assert not hist(d, 4, 4, 8, 4, -1).any()  # empty row range: zeros
+    for bad in (dict(bit_depth=2, mode=0), dict(bit_depth=4, mode=2)):
+        with pytest.raises(ValueError):
+            hist(d, 0, 10, 8, **bad)
+    with pytest.raises(ValueError):
+        hist(d, 0, 11, 8, 4, 0)  # past the end of the data
+    with pytest.raises(ValueError):
+        hist(cu(gen.raw_1bit(seed=1, nspec=4, nchan=8)), 0, 4, 7, 1, 0)  # odd 1-bit channel count

@@ -69,3 +69,67 @@ def test_assign_lanes_balances_work():
     loads = [sum(work[i] for i in l) for l in lanes]
     assert max(loads) - min(loads) <= max(work)
     assert batch.assign_lanes([5, 5], 8) == [[0], [1]]
+
+
+@pytest.mark.parametrize("k", range(4))
+def test_missing_fraction_matches_reference(golden_int, k):
+    """Per-job missing percentage vs the reference's own tracker and buffer
+    bookkeeping run on the same per-chunk counts (tests/golden/make_golden.py:
+    missing_cases), including jobs filled by the carried overflow alone."""
+    from albatros_axion_detection_gb300.output import missing_fraction
+    nant, acclen, nblock, osamp, nchunks = golden_int[f"mf{k}_cfg"]
+    got = missing_fraction(golden_int[f"mf{k}_present"], int(acclen), int(nblock), int(osamp))
+    np.testing.assert_allclose(got, golden_int[f"mf{k}_out"], rtol=0, atol=1e-12)
+
+
+def test_chunk_presence_and_npz_roundtrip(tmp_path):
+    import torch
+    from albatros_axion_detection_gb300 import output
+    sm = np.arange(3 * 40, dtype=np.int32).reshape(3, 40)
+    sm[0, 5:9] = -1
+    sm[2, 30:] = -1
+    for m in (sm, torch.from_numpy(sm)):
+        np.testing.assert_array_equal(output.chunk_presence(m, 3, 4, 10), [[6, 10, 10, 10], [10] * 4, [10, 10, 10, 0]])
+    assert output.chunk_presence(None, 2, 3, 8).tolist() == [[8] * 3] * 2
+    assert output.missing_fraction(np.full((2, 5), 64), 64, 5, 4).max() == 0.0
+    vis = (np.arange(2 * 2 * 3 * 4) + 1j).astype(np.complex64).reshape(2, 2, 3, 4)
+    vis[0, 1, 2, 3] = np.nan
+    path = output.write_run(str(tmp_path), 1721800000, 2048, 64, 7, 10, 20, vis, np.ones((1, 4)), np.arange(3))
+    assert path.endswith("stream_xcorr_all_ant_4bit_1721800000_2048_64_7_10_20.npz")
+    v, mf, ch = output.load_xcorr_npz(path)
+    assert v.mask.sum() == 1 and v.mask[0, 1, 2, 3]
+    np.testing.assert_array_equal(v.filled(0), np.nan_to_num(vis, nan=0))
+    with np.load(path) as f:
+        assert sorted(f.files) == ["chans", "data", "mask", "missing_fraction"]
+
+
+@pytest.mark.parametrize("name", ["wrap", "gaps4", "gaps1"])
+def test_ingest_host_side_matches_reference(golden_int, name, tmp_path):
+    """Header fields, wrap-fixed spectrum numbers, the overflow counter across
+    files and the run's start, as the reference's Baseband and iterator."""
+    from albatros_axion_detection_gb300 import ingest
+    sc = gen.baseband_scenarios()[name]
+    paths = gen.write_scenario(sc, str(tmp_path), name)
+    for k, p in enumerate(paths):
+        h, pk, sn, over = ingest.read_packets(p)
+        g = golden_int[f"bb_{name}_{k}_hdr"]
+        assert (h.header_bytes, h.bytes_per_packet, h.length_channels, h.spectra_per_packet, h.bit_mode,
+                h.num_packets) == tuple(int(x) for x in g)
+        np.testing.assert_array_equal(h.channels, golden_int[f"bb_{name}_{k}_chans"])
+        np.testing.assert_array_equal(sn, golden_int[f"bb_{name}_{k}_specnum"])
+        assert over == bool(golden_int[f"bb_{name}_{k}_overflowed"])
+        assert pk.shape == (h.num_packets, h.bytes_per_packet)
+        assert ingest.get_header(p)["spectra_per_packet"] == h.spectra_per_packet
+    af = ingest.plan_antenna(paths, 0, sc["idxstart"], sc["acclen"] * sc["nchunks"])
+    assert af.start == int(golden_int[f"bfi_{name}_start"])
+    ctr = np.cumsum([0] + [int(golden_int[f"bb_{name}_{k}_overflowed"]) for k in range(len(paths))])
+    for k, sn in enumerate(af.specnums):
+        np.testing.assert_array_equal(sn, golden_int[f"bb_{name}_{k}_specnum"] + ctr[k] * (1 << 32))
+
+
+def test_fix_wraps_rejects_two_wraps():
+    from albatros_axion_detection_gb300 import ingest
+    s, over = ingest.fix_wraps(np.array([5, 9, 2, 6]))
+    assert over and s.tolist() == [5, 9, 2 + (1 << 32), 6 + (1 << 32)]
+    with pytest.raises(ValueError):
+        ingest.fix_wraps(np.array([5, 1, 7, 2]))

@@ -149,3 +149,62 @@ def test_fp64_ipfb_inverts_circular_pfb():
     filt = po.calculate_filter(po.get_matft(nslice), 0.0)
     back = po.ipfb(spec, filt).ravel()
     assert np.linalg.norm(back - x) / np.linalg.norm(x) < 1e-8
+
+
+HIST_CASES = [("h4_fix", 4, 10, (0, 2)), ("h4_rand", 4, 64, (7, 291)), ("h1_fix", 1, 8, (0, 2)),
+              ("h1_rand", 1, 64, (3, 299))]
+
+
+def hist_input(name):
+    """Raw rows of the histogram fixtures (tests/golden/make_golden.py:hist_cases)."""
+    return {"h4_fix": lambda: gen.fixture_4bit_packed().reshape(-1, 20),
+            "h4_rand": lambda: gen.raw_4bit(seed=11, nspec=300, nchan=64),
+            "h1_fix": lambda: gen.fixture_1bit_packed().reshape(-1, 4),
+            "h1_rand": lambda: gen.raw_1bit(seed=12, nspec=300, nchan=64)}[name]()
+
+
+@pytest.mark.parametrize("mode", [0, 1, -1])
+@pytest.mark.parametrize("name,bits,nchan,rows", HIST_CASES)
+def test_oracle_hist_golden(golden_int, name, bits, nchan, rows, mode):
+    h = io.hist(hist_input(name), rows[0], rows[1], nchan, bits, mode)
+    np.testing.assert_array_equal(h, golden_int[f"{name}_{'b' if mode == -1 else mode}"])
+    # every selected level lands in exactly one bin
+    assert int(h.sum()) == (rows[1] - rows[0]) * nchan * (4 if mode == -1 else 2)
+
+
+def test_hist_reference_known_answers(golden_int):
+    """The reference's own assertions (test_1bit_unpack.py:110-133,
+    test_4bit_float_unpack.py:131-170) on the fixtures."""
+    h = {m: golden_int[f"h1_fix_{m}"] for m in ("0", "1", "b")}
+    assert (h["0"][0, 3], h["0"][1, 3], h["0"][0, 4]) == (1, 3, 2)
+    assert (h["1"][0, 3], h["1"][1, 3], h["1"][0, 4]) == (3, 1, 2)
+    assert (h["b"][0, 3], h["b"][1, 3], h["b"][0, 4]) == (4, 4, 4)
+    h4 = {m: golden_int[f"h4_fix_{m}"] for m in ("0", "1", "b")}
+    e0, e1 = gen.fixture_4bit_expected()
+    r0, i0, r1, i1 = e0.real, e0.imag, e1.real, e1.imag
+    assert h4["0"][0, 3] == 1 and h4["0"][4, 3] == 1
+    assert h4["0"][0, :].sum() == np.sum(r0 == 0) + np.sum(i0 == 0)
+    assert h4["1"][0, 3] == 1 and h4["1"][12, 3] == 1
+    assert h4["1"][7, :].sum() == np.sum(r1 == 7) + np.sum(i1 == 7)
+    assert h4["b"][12, 3] == 1 and h4["b"][4, 3] == 1
+    assert h4["b"][0, :].sum() == sum(np.sum(a == 0) for a in (r0, i0, r1, i1))
+
+
+@pytest.mark.parametrize("name", ["wrap", "gaps4", "gaps1"])
+def test_oracle_file_iterator(golden_int, name, tmp_path):
+    """Chunk spectrum numbers and the file rows serving them vs the
+    reference's BasebandFileIterator on the same files; header fields and
+    wrap-fixed spectrum numbers vs its Baseband."""
+    from oracle import ingest_oracle as ig
+    sc = gen.baseband_scenarios()[name]
+    paths = gen.write_scenario(sc, str(tmp_path), name)
+    for k, p in enumerate(paths):
+        hdr, chans, sn, over, _ = ig.read_file(p)
+        np.testing.assert_array_equal(hdr, golden_int[f"bb_{name}_{k}_hdr"])
+        np.testing.assert_array_equal(chans, golden_int[f"bb_{name}_{k}_chans"])
+        np.testing.assert_array_equal(sn, golden_int[f"bb_{name}_{k}_specnum"])
+        assert over == bool(golden_int[f"bb_{name}_{k}_overflowed"])
+    chunks = ig.iterate(paths, 0, sc["idxstart"], sc["acclen"], sc["nchunks"])
+    np.testing.assert_array_equal([len(c[0]) for c in chunks], golden_int[f"bfi_{name}_counts"])
+    for i, key in enumerate(("specnums", "files", "rows")):
+        np.testing.assert_array_equal(np.concatenate([c[i] for c in chunks]), golden_int[f"bfi_{name}_{key}"])
