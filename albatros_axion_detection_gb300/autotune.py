@@ -119,7 +119,8 @@ def set_plan(n: int, radices: Optional[Sequence[int]], device: Optional[int] = N
 
 
 DEFAULT_MODE = 0
-_filter_setting = {"mode": DEFAULT_MODE, "row_tile": 32}
+DEFAULT_ROW_TILE = 16  # rows-per-thread class of the IIR / FIR time stage (21 / 17 rows)
+_filter_setting = {"mode": DEFAULT_MODE, "row_tile": DEFAULT_ROW_TILE}
 
 
 def set_time_filter(mode: int = DEFAULT_MODE, row_tile: int = 0, device: Optional[int] = None) -> None:
@@ -136,12 +137,19 @@ OPT_ROW_FFTS_PER_CTA = 1
 
 
 OPT_COARSE_MMA_BITS = 3
+OPT_ROW_PREFETCH = 5
 
 
 def set_coarse_mma_bits(bits: int, device: Optional[int] = None) -> None:
     """Operand type of the coarse correlator's tensor-core MMA: 16 (fp16,
     exact, the default) or 8 (int8)."""
     _lib.call("ab_ctx_set_option", _lib.ctx(device), OPT_COARSE_MMA_BITS, int(bits))
+
+
+def set_row_prefetch(on: bool, device: Optional[int] = None) -> None:
+    """Time-paired row stage as persistent CTAs with cp.async prefetch (the
+    default) or one CTA per tile."""
+    _lib.call("ab_ctx_set_option", _lib.ctx(device), OPT_ROW_PREFETCH, 1 if on else 0)
 
 
 def set_row_ffts_per_cta(n: int, device: Optional[int] = None) -> None:
@@ -151,7 +159,7 @@ def set_row_ffts_per_cta(n: int, device: Optional[int] = None) -> None:
 
 
 def _time_chain(acclen: int, cut: int, osamp: int, nchunks: int = 2, reps: int = 2, mode: int = 0,
-                row_tile: int = 32) -> Tuple[float, Tuple[str, int]]:
+                row_tile: int = DEFAULT_ROW_TILE) -> Tuple[float, Tuple[str, int]]:
     """(ms per launch of the chain's time stage for one antenna, the form that
     ran) with the given time-filter setting; the previous setting is restored."""
     from .stream import StreamCorrelator

@@ -126,7 +126,7 @@ class BatchCorrelator:
                 members.append(i)
             self.workspaces.append(ws)
         if self.tuned:
-            autotune.set_time_filter(autotune.DEFAULT_MODE, 32)  # back to the defaults for later streams
+            autotune.set_time_filter(autotune.DEFAULT_MODE, autotune.DEFAULT_ROW_TILE)  # defaults for later streams
         self.streams = [torch.cuda.Stream(device=self.files[0].raw.device) for _ in self.lanes]
         self.vis_host = None
         if vis_to_host:

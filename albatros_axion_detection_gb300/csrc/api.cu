@@ -299,6 +299,10 @@ int ab_ctx_set_option(ab_ctx* ctx, int32_t option, int32_t value) {
                    "ab_ctx_set_option: row stage spectra per CTA must be 8 (time-paired), 4 or 2 (pol-paired)");
       ctx->row_ffts_per_cta = value;
       return AB_OK;
+    case AB_OPT_ROW_PREFETCH:
+      AB_CHECK_ARG(value == 0 || value == 1, "ab_ctx_set_option: row prefetch must be 0 or 1");
+      ctx->row_prefetch = value;
+      return AB_OK;
     case AB_OPT_COARSE_MMA_BITS:
       AB_CHECK_ARG(value == 8 || value == 16, "ab_ctx_set_option: coarse MMA input bits must be 8 or 16");
       ctx->coarse_f16 = value == 16;

@@ -49,7 +49,7 @@ struct ab_stream {
   float* state = nullptr;    // fused: last 4*osamp timestream rows per column (x2 for the FIR path)
   int fir_J = 0;             // > 0: time stage as a (2J+1)-tap FIR (fir.cu)
   int iir_W = 0;             // > 0: time stage as the IIR factorisation, warm-up iir_W (fir.cu)
-  int fir_row_tile = 32;     // kept rows per thread of the FIR stage
+  int fir_row_tile = 16;     // rows-per-thread class of the IIR / FIR stage
   const float* fir_taps = nullptr;
   float* W = nullptr;
   float2* Y = nullptr;

@@ -39,6 +39,23 @@ __device__ __forceinline__ void st_global_v8(float* p, float a0, float a1, float
                : "memory");
 }
 
+// Asynchronous global -> shared copies (cp.async): 4 bytes through L1, 16
+// bytes bypassing it; commit closes a group, wait<N> leaves at most N of this
+// thread's groups in flight.
+template <class T>
+__device__ __forceinline__ void cp_async4(T* dst, const T* src) {
+  static_assert(sizeof(T) == 4, "4-byte elements");
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async16(float* dst, const float* src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
   return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
 }

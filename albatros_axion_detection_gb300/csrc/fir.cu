@@ -389,6 +389,7 @@ int get_iir_coeffs(ab_ctx* ctx, int P, int ntap, float thresh, int* W_out, const
 // O/2 points plus the real-input untangle), then writes the O packed floats
 // of W with 32-byte stores.
 constexpr int kFirThreads = 256;
+constexpr int kYPad = 3;  // pad floats per O rows of the y buffer (yidx)
 
 __constant__ float2 c_fir_tw[64];  // exp(-2 pi i k / 64)
 
@@ -416,7 +417,7 @@ struct FirLayout {
   static constexpr int WT = 4 * O;                      // window coefficients, float4 per t'
   static constexpr int STAGE = XS + TAPS + ST + WT;     // floats per staging buffer (multiple of 4)
   static constexpr int YROWS = R + 8 * O + U;           // y rows held (incl. zeros past the end)
-  static constexpr int YS = YROWS + YROWS / O + 4;      // one pad float per O rows
+  static constexpr int YS = YROWS + kYPad * (YROWS / O + 1) + 4;  // kYPad pad floats per O rows
   static constexpr size_t bytes() { return sizeof(float) * (2 * (size_t)STAGE + (size_t)YS); }
 };
 
@@ -431,7 +432,7 @@ struct IirLayout {
   static constexpr int R = (kFirThreads - 2 * D) * U;
   static constexpr int XW = kFirThreads * U + 6;  // all threads' rows, 3 before, up to 3 of alignment shift
   static constexpr int YROWS = R + 8 * O;
-  static constexpr int YS = YROWS + YROWS / O + 4;
+  static constexpr int YS = YROWS + kYPad * (YROWS / O + 1) + 4;
   static constexpr int XS = ((XW > YS ? XW : YS) + 3) & ~3;
   static constexpr int TAPS = kIirCoef;
   static constexpr int STAGE = XS + TAPS + 4 * O + 4 * O;
@@ -439,17 +440,6 @@ struct IirLayout {
   static constexpr size_t bytes() { return sizeof(float) * (2 * (size_t)STAGE + XCH); }
 };
 
-__device__ __forceinline__ void cp_async4(float* dst, const float* src) {
-  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async16(float* dst, const float* src) {
-  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
 // d * exp(-2 pi i e / N) for a compile-time e
 template <int N>
@@ -554,12 +544,17 @@ __device__ __forceinline__ void prefetch_item_extras(float* st_taps, int K, int 
   }
 }
 
-// y rows are padded one float per O rows, with the pads at the fine blocks'
-// first rows (y row phi + k*O): a block's 4*O rows then sit at base + c + c/O
-// for compile-time c, and blocks O + 1 floats apart fall in distinct banks.
+// y rows are padded kYPad floats per O rows, with the pads at the fine
+// blocks' first rows (y row phi + k*O): a block's 4*O rows then sit at
+// base + c + kYPad*(c/O) for compile-time c; blocks O + kYPad floats apart
+// fall in distinct banks (one lane per block), and the filter's stores of
+// lanes U rows apart meet at most 2-way conflicts for any U (a 1-float pad
+// gives 3-way at U = 41, 11-way at U = 21).  (Two lanes per block, each
+// taking half the FFT, removed the fold's idle threads but met 2-way
+// conflicts on every y load and cost more than it saved.)
 template <int O>
 __device__ __forceinline__ int yidx(int q, int phi) {
-  return q + (q - phi + O) / O;
+  return q + kYPad * ((q - phi + O) / O);
 }
 template <int O>
 __device__ __forceinline__ int y_phase(const FirItem& it, const FoldArgs& fa) {
@@ -598,7 +593,7 @@ __device__ __forceinline__ void fold_item_blocks(const float* ys, int phi, const
       continue;
     }
     const int q0 = 4 * O - it.s0 + rfirst;  // y row of the block's first row (= phi mod O)
-    const float* yb = ys + yidx<O>(q0, phi);  // rows q0 + c at yb[c + c/O]
+    const float* yb = ys + yidx<O>(q0, phi);  // rows q0 + c at yb[c + kYPad*(c/O)]
     float2 a[NC];
 #pragma unroll
     for (int m = 0; m < NC; m++) {
@@ -607,8 +602,8 @@ __device__ __forceinline__ void fold_item_blocks(const float* ys, int phi, const
       for (int e = 0; e < 2; e++) {
         const int tp = 2 * m + e;
         const float4 w4 = wt[tp];
-        zz[e] = fmaf(w4.x, yb[tp], fmaf(w4.y, yb[tp + (O + 1)],
-                                        fmaf(w4.z, yb[tp + 2 * (O + 1)], w4.w * yb[tp + 3 * (O + 1)])));
+        zz[e] = fmaf(w4.x, yb[tp], fmaf(w4.y, yb[tp + (O + kYPad)],
+                                        fmaf(w4.z, yb[tp + 2 * (O + kYPad)], w4.w * yb[tp + 3 * (O + kYPad)])));
       }
       a[m] = make_float2(zz[0], zz[1]);
     }
@@ -923,7 +918,10 @@ template <int U, int G, int D>
 static int launch_iir_t(const FirArgs& a, const FoldArgs& fa, cudaStream_t s) {
   constexpr int O = 2 * G;
   using Lay = IirLayout<U, O, D>;
-  constexpr int S = Lay::R - 4 * O;
+  // new rows per item: a whole number of fold rounds (one block per thread
+  // per round) when at least one fits
+  constexpr int SMAX = Lay::R - 4 * O, ROUND = kFirThreads * O;
+  constexpr int S = SMAX >= ROUND ? SMAX / ROUND * ROUND : SMAX;
   static_assert(S > 0, "IIR tile too small for this osamp");
   int nseg;
   const int64_t nitems = fir_items<S, O>(a, &nseg);

@@ -462,6 +462,148 @@ __global__ void __launch_bounds__(4 * kRowThreadsPerFft)
   }
 }
 
+// Persistent form of the time-paired row stage.  CTAs walk the tiles (8
+// spectra of one input; tile = row block * inputs + input, so both pols of a
+// spectrum follow each other) with a stride of gridDim.x.  A tile's global
+// loads form a chain -- spectrum-map rows, then the packet words holding the
+// selected bytes -- so they are issued with cp.async two tiles (map rows) and
+// one tile (words) ahead into double-buffered shared slots and never stall
+// the transform.  Needs nsel <= kRowThreadsPerFft (one selected channel per
+// thread) and 4-byte-multiple packet rows and antenna strides (a word never
+// leaves the packet buffer, and a byte's place in its word does not depend
+// on the row).
+constexpr int kRowPfRows = 8;
+__host__ __device__ inline size_t row_pf_smem_bytes(int P) {
+  return row_smem_bytes(P, 4) + sizeof(int32_t) * 4 * kRowPfRows + sizeof(uint32_t) * 2 * kRowPfRows * kRowThreadsPerFft;
+}
+
+template <class PL>
+__global__ void __launch_bounds__(4 * kRowThreadsPerFft)
+    row_stage_tpair_pf_kernel(Packed4Src src, int nrows, int nin, FftPlan plan, const float2* __restrict__ tw,
+                              const float2* __restrict__ tws, float* __restrict__ out, int64_t ld) {
+  constexpr int FFTS = 4, ROWS = kRowPfRows, T = kRowThreadsPerFft;
+  static_assert(ROWS == 2 * FFTS, "two spectra per transform");
+  extern __shared__ float2 smem[];
+  const int P = plan.n, PL_ = padded_len(P);
+  const int sub = threadIdx.x / T, ltid = threadIdx.x % T;
+  float2* buf = smem + (size_t)sub * PL_;
+  int32_t* st_map = reinterpret_cast<int32_t*>(smem + (size_t)FFTS * PL_ + smem_tw_len(P));  // [2][ROWS] raw rows
+  int32_t* st_pres = st_map + 2 * ROWS;                                                         // [2][ROWS] present
+  uint32_t* st_w = reinterpret_cast<uint32_t*>(st_pres + 2 * ROWS);                              // [2][ROWS][T] words
+  SmemTw tws_s{nullptr, nullptr};
+  if constexpr (std::is_same<PL, NoPlan>::value)
+    tws_s = load_smem_tw(smem + (size_t)FFTS * PL_, tw, P, threadIdx.x, blockDim.x);
+  const int nrb = (nrows + ROWS - 1) / ROWS;
+  const int ntiles = nrb * nin, G = gridDim.x;
+  const bool has_k = ltid < src.nsel;
+  const int col = has_k ? __ldg(&src.chan_cols[ltid]) : 0;
+  const int kabs = has_k ? __ldg(&src.chan_abs[ltid]) : 0;
+  // map rows of tile x into slot sl (threads 0..ROWS-1)
+  auto issue_map = [&](int x, int sl) {
+    if (x >= ntiles || threadIdx.x >= ROWS) return;
+    const int rb = x / nin, a = (x % nin) >> 1;
+    const int64_t t = (int64_t)rb * ROWS + threadIdx.x, g = src.g0 + t;
+    int32_t* dst = st_map + sl * ROWS + threadIdx.x;
+    if (t >= nrows || g < 0) *dst = -1;
+    else if (src.spec_map) cp_async4(dst, src.spec_map + (int64_t)a * src.map_stride + g);
+    else *dst = (int32_t)g;
+  };
+  // packet words of tile x (rows from map slot sl) into word slot sl
+  auto issue_words = [&](int x, int sl) {
+    if (x >= ntiles) return;
+    const int in = x % nin, a = in >> 1, pol = in & 1;
+    const int boff = src.bits == 4 ? 2 * col + pol : col >> 1;
+#pragma unroll
+    for (int e = 0; e < 2; e++) {
+      const int r = 2 * sub + e;
+      const int32_t row = st_map[sl * ROWS + r];
+      if (ltid == 0) st_pres[sl * ROWS + r] = row >= 0;
+      if (has_k && row >= 0) {
+        const uint8_t* p = src.raw + (int64_t)a * src.ant_stride + (int64_t)row * src.row_bytes + (boff & ~3);
+        cp_async4(st_w + ((size_t)sl * ROWS + r) * T + ltid, reinterpret_cast<const uint32_t*>(p));
+      }
+    }
+  };
+  int x = blockIdx.x;
+  issue_map(x, 0);
+  issue_map(x + G, 1);
+  cp_async_commit();
+  cp_async_wait<0>();
+  __syncthreads();
+  issue_words(x, 0);
+  cp_async_commit();
+  for (int i = 0; x < ntiles; x += G, i++) {
+    const int sl = i & 1;
+    cp_async_wait<0>();
+    __syncthreads();  // words and presence of this tile, map rows of the next; buffers free
+    issue_words(x + G, sl ^ 1);
+    issue_map(x + 2 * G, sl);
+    cp_async_commit();
+    {
+      float4* b4 = reinterpret_cast<float4*>(smem);  // zero all buffers (PL_ * FFTS float2, even count)
+      const int n4 = (FFTS * PL_) / 2;
+      for (int q = threadIdx.x; q < n4; q += blockDim.x) b4[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    __syncthreads();
+    const int in = x % nin, pol = in & 1;
+    const int r0 = 2 * sub;
+    const bool p0 = st_pres[sl * ROWS + r0] != 0, p1 = st_pres[sl * ROWS + r0 + 1] != 0;
+    if (has_k && (p0 || p1)) {
+      const int boff = src.bits == 4 ? 2 * col + pol : col >> 1;
+      const int sh = 8 * (boff & 3);
+      float2 v[2];
+#pragma unroll
+      for (int e = 0; e < 2; e++) {
+        v[e] = make_float2(0.f, 0.f);
+        if (!(e ? p1 : p0)) continue;
+        const unsigned b = (st_w[((size_t)sl * ROWS + r0 + e) * T + ltid] >> sh) & 0xffu;
+        if (src.bits == 4) {
+          v[e] = make_float2(dec4f(b >> 4), dec4f(b & 15u));
+        } else {
+          const unsigned q = (b >> ((col & 1) ? 0 : 4)) & 15u;
+          const unsigned s2 = pol ? 0u : 2u;
+          v[e] = make_float2((float)(((q >> (s2 + 1)) & 1u) * 2) - 1.f, (float)(((q >> s2) & 1u) * 2) - 1.f);
+        }
+      }
+      put_pair_t<PL>(buf, plan, P, kabs, v[0], v[1]);
+    }
+    __syncthreads();
+    fft_inv<PL, kRowThreadsPerFft>(buf, plan, tws_s, P, tws, ltid);
+    const float inv = 1.0f / (float)P;
+    const int64_t t0 = (int64_t)(x / nin) * ROWS;
+    float* ocol = out + (int64_t)in * P * ld + t0;
+    if (t0 + ROWS <= nrows) {
+      for (int n = threadIdx.x; n < P; n += blockDim.x) {
+        const float2 z0 = smem[pidx(n)], z1 = smem[(size_t)PL_ + pidx(n)];
+        const float2 z2 = smem[(size_t)2 * PL_ + pidx(n)], z3 = smem[(size_t)3 * PL_ + pidx(n)];
+        st_global_v8(ocol + (int64_t)n * ld, z0.x * inv, z0.y * inv, z1.x * inv, z1.y * inv, z2.x * inv, z2.y * inv,
+                     z3.x * inv, z3.y * inv);
+      }
+    } else {
+      for (int q = threadIdx.x; q < ROWS * P; q += blockDim.x) {
+        const int n = q / ROWS, r = q - n * ROWS;
+        if (t0 + r >= nrows) continue;
+        const float2 z = smem[(size_t)(r >> 1) * PL_ + pidx(n)];
+        ocol[(int64_t)n * ld + r] = ((r & 1) ? z.y : z.x) * inv;
+      }
+    }
+  }
+  cp_async_wait<0>();  // nothing left in flight at exit
+}
+
+template <class PL>
+static int launch_row_tpair_pf_t(ab_ctx* ctx, const Packed4Src& src, int nant, int nrows, int P, const FftPlan& plan,
+                                 const float2* twP, const float2* tws, float* out, int64_t ld, cudaStream_t s) {
+  const size_t smem = row_pf_smem_bytes(P);
+  AB_TRY(set_smem_attr(row_stage_tpair_pf_kernel<PL>, smem));
+  const int64_t ntiles = (int64_t)((nrows + kRowPfRows - 1) / kRowPfRows) * 2 * nant;
+  AB_CHECK_ARG(ntiles < (1LL << 31), "row stage: too many tiles");
+  const int grid = (int)std::min<int64_t>(ntiles, std::max(ctx->num_sms, 1));
+  row_stage_tpair_pf_kernel<PL><<<grid, 4 * kRowThreadsPerFft, smem, s>>>(src, nrows, 2 * nant, plan, twP, tws, out, ld);
+  AB_LAUNCH_CHECK();
+  return AB_OK;
+}
+
 template <class PL>
 static int launch_row_tpair_t(ab_ctx* ctx, const Packed4Src& src, int nant, int nrows, int P, const FftPlan& plan,
                               const float2* twP, const float2* tws, float* out, int64_t ld, cudaStream_t s) {
@@ -500,15 +642,21 @@ int launch_row_stage_packed4(ab_ctx* ctx, const Packed4Src& src, int nant, int n
                              const float2* twP, float* out, int64_t ld, cudaStream_t s) {
   if (ctx->row_ffts_per_cta == 2) return launch_row_packed4_t<2>(ctx, src, nant, nrows, P, plan, twP, out, ld, s);
   if (ctx->row_ffts_per_cta == 4) return launch_row_packed4_t<4>(ctx, src, nant, nrows, P, plan, twP, out, ld, s);
-  // default: time-paired spectra
+  // default: time-paired spectra; the persistent prefetching form when its
+  // conditions hold (ld % 8 for the 32-byte column stores, as the other)
   AB_CHECK_ARG(row_smem_bytes(P, 4) <= ctx->smem_optin, "row stage: lblock %d too large", P);
   bool tuned = false;
   { FftPlan tmp; ctx_plan(ctx, P, &tmp, &tuned); }
+  const bool pf = ctx->row_prefetch && src.nsel <= kRowThreadsPerFft && src.row_bytes % 4 == 0 &&
+                  src.ant_stride % 4 == 0 && ((uintptr_t)src.raw & 3) == 0 && ld % 8 == 0 &&
+                  ((uintptr_t)out & 31) == 0 && row_pf_smem_bytes(P) <= ctx->smem_optin;
   if (P == Plan4096::N && !tuned) {
     const float2* tws;
     AB_TRY(get_twiddle_stream(ctx, P, {16, 16, 16}, &tws));
+    if (pf) return launch_row_tpair_pf_t<Plan4096>(ctx, src, nant, nrows, P, plan, twP, tws, out, ld, s);
     return launch_row_tpair_t<Plan4096>(ctx, src, nant, nrows, P, plan, twP, tws, out, ld, s);
   }
+  if (pf) return launch_row_tpair_pf_t<NoPlan>(ctx, src, nant, nrows, P, plan, twP, nullptr, out, ld, s);
   return launch_row_tpair_t<NoPlan>(ctx, src, nant, nrows, P, plan, twP, nullptr, out, ld, s);
 }
 

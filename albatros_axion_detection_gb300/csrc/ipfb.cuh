@@ -87,7 +87,7 @@ struct FirArgs {
   int P, ninputs, nslice, cut, acclen;
   const float* taps;      // FIR taps (P, 2J+1) or IIR coefficients (P, 24)
   int J;                  // FIR: 32 or 64 (ignored when iir_w > 0)
-  int row_tile;           // kept rows per thread: 16 or 32
+  int row_tile;           // rows-per-thread class: 16 or 32
   const float* state_in;  // previous chunk's last 4*O rows (ninputs, P, 4*O)
   float* state_out;       // this chunk's last 4*O rows (the other buffer)
   const float2* tw64;

@@ -174,9 +174,13 @@ def run_ours(args):
     if args.row_ffts:
         from albatros_axion_detection_gb300 import autotune
         autotune.set_row_ffts_per_cta(args.row_ffts)
-    if args.time_filter != "default":
+    if args.row_no_prefetch:
         from albatros_axion_detection_gb300 import autotune
-        autotune.set_time_filter({"iir": 0, "fir": 3, "fft": 1}[args.time_filter], args.row_tile)
+        autotune.set_row_prefetch(False)
+    if args.time_filter != "default" or args.row_tile:
+        from albatros_axion_detection_gb300 import autotune
+        mode = {"iir": 0, "fir": 3, "fft": 1}.get(args.time_filter, autotune.DEFAULT_MODE)
+        autotune.set_time_filter(mode, args.row_tile)
     sc = stream.StreamCorrelator(NANT, channels, 0, NCHAN_RAW, ACCLEN, NSPEC // ACCLEN, NBLOCK, OSAMP, CUT, THRESH,
                                  NTAP, nchan_raw=NCHAN_RAW)
     nchunks = NSPEC // ACCLEN
@@ -541,6 +545,7 @@ def main():
                     help="stream: IPFB time stage form (default: the library's choice)")
     ap.add_argument("--row-tile", type=int, default=0, help="stream: FIR rows per thread (16 or 32)")
     ap.add_argument("--row-ffts", type=int, default=0, help="stream: spectra per row-stage CTA (2 or 4)")
+    ap.add_argument("--row-no-prefetch", action="store_true", help="stream: one row-stage CTA per tile")
     ap.add_argument("--check", action="store_true", help="uneven-batch: job-0 error of every file vs the FP64 oracle")
     ap.add_argument("--mma-bits", type=int, default=0, help="coarse workloads: tensor-core operand bits (16 or 8)")
     args = ap.parse_args()

@@ -62,8 +62,9 @@ int ab_ctx_set_fft_plan(ab_ctx *ctx, int64_t n, const int32_t *radices, int64_t 
  * IIR and FIR need the fused PFB fold (osamp >= 4, ntap = 4) and run any
  * nslice.  mode 0 (default): IIR, else FIR, else FFT; mode 1: FFT only;
  * mode 2: FFT where it runs, else IIR/FIR; mode 3: FIR, else FFT.
- * row_tile: kept rows per thread of the FIR stage (16 or 32; 0 keeps the
- * current value), taken by streams created after the call.  No reference counterpart: the reference
+ * row_tile: rows-per-thread class of the IIR / FIR stages (16, the default:
+ * 21 / 17 rows a thread; 32: 41 / 33; 0 keeps the current value), taken by
+ * streams created after the call.  No reference counterpart: the reference
  * always filters with cuFFT (albatros_analysis/src/utils/pfb_gpu_utils.py:56-91). */
 int ab_ctx_set_time_filter(ab_ctx *ctx, int32_t mode, int32_t row_tile);
 /* Launch-shape options of this context (no reference counterpart; set by the
@@ -77,6 +78,11 @@ int ab_ctx_set_time_filter(ab_ctx *ctx, int32_t mode, int32_t row_tile);
  * MMA, 16 (default: fp16 operands, fp32 partial sums, exact) or 8 (int8
  * operands, int32 partial sums). */
 #define AB_OPT_COARSE_MMA_BITS 3
+/* AB_OPT_ROW_PREFETCH: 1 (default) runs the time-paired row stage as
+ * persistent CTAs that prefetch the next tile's spectrum-map rows and packet
+ * words with cp.async (when at most 256 channels are selected and packet
+ * rows are 4-byte multiples); 0 launches one CTA per tile. */
+#define AB_OPT_ROW_PREFETCH 5
 int ab_ctx_set_option(ab_ctx *ctx, int32_t option, int32_t value);
 
 /* ---- unpacking ----------------------------------------------------------

@@ -26,7 +26,7 @@ def stream_vis(raw_np, channels, mode=FIR, row_tile=32, thresh=0.45, bits=4, **k
                                      kw["nchunks"], kw["nblock"], kw["osamp"], kw["cut"], thresh, 4,
                                      nchan_raw=len(channels), bits=bits)
     finally:
-        autotune.set_time_filter(autotune.DEFAULT_MODE, 32)
+        autotune.set_time_filter(autotune.DEFAULT_MODE, autotune.DEFAULT_ROW_TILE)
     try:
         raw = torch.from_numpy(raw_np).cuda()
         for j in range(kw["nchunks"]):
@@ -56,7 +56,7 @@ def test_fir_chosen_and_matches_fft_and_oracle():
 @pytest.mark.parametrize("mode", [FIR, IIR])
 def test_row_tiles_agree(mode):
     """Row tiles 33 and 17: the FIR sums are identical term by term (bitwise);
-    the IIR warm-up starts at different rows, so equal to rounding."""
+    the IIR threads' ranges (41 or 21 rows) differ, so equal to rounding."""
     raw = gen.raw_4bit(seed=22, nspec=3 * 1024, nchan=8, nant=1)
     ch = np.arange(100, 108)
     cfg = dict(CFG, osamp=64, nblock=16)
@@ -139,3 +139,4 @@ def test_multi_segment_columns(osamp, row_tile, mode):
     v, tf = stream_vis(raw, ch, mode=mode, row_tile=row_tile, **kw)
     assert tf[0] == ("fir" if mode == FIR else "iir")
     check(v, ref)
+

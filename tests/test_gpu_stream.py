@@ -135,3 +135,29 @@ def test_stream_row_stage_shapes(per_cta, nrows_extra):
     finally:
         autotune.set_row_ffts_per_cta(8)
     check(vis, ref)
+
+
+@pytest.mark.parametrize("bits,nrows_extra", [(4, 0), (4, 3), (1, 5)])
+def test_row_prefetch_equals_one_cta_per_tile(bits, nrows_extra):
+    """The persistent row stage (cp.async prefetch of map rows and packet
+    words) and the one-CTA-per-tile form compute the same transforms:
+    identical visibilities, with missing spectra and a ragged last tile."""
+    from albatros_axion_detection_gb300 import autotune
+    acclen, cut, nchan = 512 + nrows_extra, 32, 16
+    raw = (gen.raw_4bit(seed=5 + nrows_extra, nspec=3 * acclen, nchan=nchan, nant=2) if bits == 4 else
+           np.stack([gen.raw_1bit(seed=6 + a, nspec=3 * acclen, nchan=nchan) for a in range(2)]))
+    channels = np.arange(700, 700 + nchan)
+    kw = dict(acclen=acclen, nchunks=3, nblock=32, chanstart=2, chanend=14, osamp=16, cut=cut, bits=bits)
+    present = np.ones((2, 3 * acclen), bool)
+    present[0, 90:133] = False
+    present[1, 600:611] = False
+    spec_map = np.where(present, np.arange(3 * acclen)[None, :], -1).astype(np.int32)
+    a, _ = run(raw, channels, spec_map=spec_map, **kw)
+    autotune.set_row_prefetch(False)
+    try:
+        b, _ = run(raw, channels, spec_map=spec_map, **kw)
+    finally:
+        autotune.set_row_prefetch(True)
+    assert np.array_equal(a, b)
+    ref, _ = po.repfb_xcorr_avg(raw, channels, spec_present=present, **kw)
+    check(a, ref)

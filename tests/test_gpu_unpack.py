@@ -131,7 +131,7 @@ def test_hist_vs_oracle(bits, nchan, nspec, r0, r1):
 def test_hist_edge_cases():
     from albatros_axion_detection_gb300.unpacking import hist
     d = cu(gen.raw_4bit_uniform(seed=3, nspec=10, nchan=8))
-    assert not hist(d, 4, 4, 8, 4, -1).any()  # empty row range: zeros
+    assert not hist(d, 4, 4, 8, 4, -1).cpu().numpy().any()  # empty row range: zeros
     for bad in (dict(bit_depth=2, mode=0), dict(bit_depth=4, mode=2)):
         with pytest.raises(ValueError):
             hist(d, 0, 10, 8, **bad)
