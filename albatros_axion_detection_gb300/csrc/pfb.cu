@@ -430,6 +430,87 @@ __global__ void __launch_bounds__(kBandThreads, 3)
   }
 }
 
+// The same stage with two slots per CTA (O >= 4): slots 2j and 2j+1 fill the
+// two 16-byte halves of W's 32-byte (n, group) records, so a CTA reads whole
+// halves and each sector passes L1 twice instead of four times (once per
+// slot CTA).  Their transforms run side by side in two buffers; the pair
+// holding slot 0 takes W_{O/2}'s transform in a second round.  The twiddle
+// w_L^(s n) comes from three 64-entry tables (e = s n mod L < 2^18 split in
+// 6-bit digits), so two buffers still leave room for three CTAs per SM.
+__host__ __device__ inline size_t stage_band2_smem() {
+  return sizeof(float2) * (2 * (size_t)padded_len(4096) + 3 * 64 + 16);
+}
+
+__device__ __forceinline__ float2 tw3(const float2* t, int e) {  // exp(-2 pi i e / L), e < 2^18
+  return cmul(t[e >> 12], cmul(t[64 + ((e >> 6) & 63)], t[128 + (e & 63)]));
+}
+
+__global__ void __launch_bounds__(kBandThreads, 3)
+    pfb_stage_band2_kernel(const float* __restrict__ W, int O, int64_t nb, const float2* __restrict__ twL,
+                           const float2* __restrict__ tws, int u0, int u1, float2* __restrict__ out) {
+  constexpr int P = 4096, PER = P / kBandThreads;
+  extern __shared__ float2 sm2[];
+  float2* bufA = sm2;
+  float2* bufB = bufA + padded_len(P);
+  float2* t3 = bufB + padded_len(P);  // [64] w^(4096 i), [64] w^(64 i), [64] w^i
+  float2* w16 = t3 + 192;             // exp(-2 pi i m / 16)
+  const int GW = O < 8 ? O : 8, NG = O / GW;
+  const int j = blockIdx.x;  // slots 2j, 2j + 1
+  const int64_t b = blockIdx.y;
+  const int in = blockIdx.z;
+  const int L = P * O;
+  const int tid = threadIdx.x;
+  if (tid < 192) {
+    const int d = tid >> 6, i = tid & 63;
+    const int64_t e = d == 0 ? (int64_t)i * 4096 : d == 1 ? (int64_t)i * 64 : i;
+    t3[tid] = e < L ? __ldg(&twL[e]) : make_float2(1.f, 0.f);
+  }
+  if (tid < 16) w16[tid] = __ldg(&twL[(int64_t)tid * (L / 16)]);
+  const int c0 = 2 * j;
+  const int g = (2 * c0) / GW, e0 = (2 * c0) % GW;  // slot c0 at float e0 of group g (0 or 4)
+  const float* src = W + ((((int64_t)in * nb + b) * NG + g) * P) * GW + e0;
+  const int nu = u1 - u0;
+  float2* ob = out + ((int64_t)in * nb + b) * ((int64_t)nu * O);
+  __syncthreads();
+  const int sA = c0, sB = c0 + 1;
+#pragma unroll 4
+  for (int q = 0; q < PER; q++) {
+    const int n = tid + q * kBandThreads;
+    const float4 v = __ldg(reinterpret_cast<const float4*>(src + (size_t)n * GW));
+    float2 xa = j == 0 ? make_float2(v.x, 0.f) : make_float2(v.x, v.y);  // slot 0: the real W_0
+    if (sA) xa = cmul(xa, tw3(t3, (int)(((int64_t)sA * n) % L)));
+    bufA[pidx(n)] = xa;
+    bufB[pidx(n)] = cmul(make_float2(v.z, v.w), tw3(t3, (int)(((int64_t)sB * n) % L)));
+  }
+  __syncthreads();
+  spass<16, 256, 4096, kBandThreads, false>(bufA, tws + Plan4096::tw_off(0), tid);
+  spass<16, 256, 4096, kBandThreads, false>(bufB, tws + Plan4096::tw_off(0), tid);
+  __syncthreads();
+  spass<16, 16, 4096, kBandThreads, false>(bufA, tws + Plan4096::tw_off(1), tid);
+  spass<16, 16, 4096, kBandThreads, false>(bufB, tws + Plan4096::tw_off(1), tid);
+  __syncthreads();
+  band_outputs(bufA, w16, u0, nu, false, sA, O, ob, tid);
+  if (sA != 0) band_outputs(bufA, w16, u0, nu, true, O - sA, O, ob, tid);
+  band_outputs(bufB, w16, u0, nu, false, sB, O, ob, tid);
+  band_outputs(bufB, w16, u0, nu, true, O - sB, O, ob, tid);
+  if (j == 0) {  // W_{O/2}, the second real value of slot 0
+    const int sH = O / 2;
+    __syncthreads();
+#pragma unroll 4
+    for (int q = 0; q < PER; q++) {
+      const int n = tid + q * kBandThreads;
+      const float wv = __ldg(src + (size_t)n * GW + 1);
+      bufA[pidx(n)] = cmul(make_float2(wv, 0.f), tw3(t3, (int)(((int64_t)sH * n) % L)));
+    }
+    __syncthreads();
+    spass<16, 256, 4096, kBandThreads, false>(bufA, tws + Plan4096::tw_off(0), tid);
+    __syncthreads();
+    spass<16, 16, 4096, kBandThreads, false>(bufA, tws + Plan4096::tw_off(1), tid);
+    __syncthreads();
+    band_outputs(bufA, w16, u0, nu, false, sH, O, ob, tid);
+  }
+}
+
 int launch_pfb_stage_a(const TsSrc& src, int ninputs, int P, int O, int ntap, int64_t row0, int64_t nb,
                        const float* win, float* W, const float2* tw64, cudaStream_t s) {
   AB_CHECK_ARG(P % kFoldCols == 0, "pfb: lblock/osamp %d must be a multiple of %d", P, kFoldCols);
@@ -472,7 +553,14 @@ int launch_pfb_stage_b(ab_ctx* ctx, const float* W, int ninputs, int P, int O, i
   size_t smem = sizeof(float) * (size_t)P * GW + sizeof(float2) * ((size_t)padded_len(P) + smem_tw_len(P * O));
   AB_CHECK_ARG(smem <= 220 * 1024, "pfb: stage B needs %zu bytes of shared memory", smem);
   dim3 grid((unsigned)nb, (unsigned)(O / GW), (unsigned)ninputs);
-  if (P == Plan4096::N && O >= 2 && nb <= 65535 && u1 >= 0) {
+  if (P == Plan4096::N && O >= 4 && O <= 64 && nb <= 65535 && u1 >= 0 && ((uintptr_t)W & 15) == 0) {
+    const float2* tws;
+    AB_TRY(get_twiddle_stream(ctx, P, {16, 16, 16}, &tws));
+    size_t sm = stage_band2_smem();
+    AB_CUDA(cudaFuncSetAttribute(pfb_stage_band2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    dim3 g2((unsigned)(O / 4), (unsigned)nb, (unsigned)ninputs);
+    pfb_stage_band2_kernel<<<g2, kBandThreads, sm, s>>>(W, O, nb, twL, tws, u0, u1, out);
+  } else if (P == Plan4096::N && O >= 2 && nb <= 65535 && u1 >= 0) {
     const float2* tws;
     AB_TRY(get_twiddle_stream(ctx, P, {16, 16, 16}, &tws));
     size_t sm = stage_band_smem();
