@@ -138,6 +138,7 @@ OPT_ROW_FFTS_PER_CTA = 1
 
 OPT_COARSE_MMA_BITS = 3
 OPT_ROW_PREFETCH = 5
+DEFAULT_ROW_PREFETCH = 2
 
 
 def set_coarse_mma_bits(bits: int, device: Optional[int] = None) -> None:
@@ -146,10 +147,11 @@ def set_coarse_mma_bits(bits: int, device: Optional[int] = None) -> None:
     _lib.call("ab_ctx_set_option", _lib.ctx(device), OPT_COARSE_MMA_BITS, int(bits))
 
 
-def set_row_prefetch(on: bool, device: Optional[int] = None) -> None:
-    """Time-paired row stage as persistent CTAs with cp.async prefetch (the
-    default) or one CTA per tile."""
-    _lib.call("ab_ctx_set_option", _lib.ctx(device), OPT_ROW_PREFETCH, 1 if on else 0)
+def set_row_prefetch(mode, device: Optional[int] = None) -> None:
+    """Time-paired row stage: 2 (default) persistent CTAs with cp.async
+    prefetch and the FFT twiddles in shared memory, 1 the same with the
+    twiddles read from global memory, 0 one CTA per tile."""
+    _lib.call("ab_ctx_set_option", _lib.ctx(device), OPT_ROW_PREFETCH, int(mode))
 
 
 def set_row_ffts_per_cta(n: int, device: Optional[int] = None) -> None:

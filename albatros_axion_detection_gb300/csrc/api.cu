@@ -300,7 +300,7 @@ int ab_ctx_set_option(ab_ctx* ctx, int32_t option, int32_t value) {
       ctx->row_ffts_per_cta = value;
       return AB_OK;
     case AB_OPT_ROW_PREFETCH:
-      AB_CHECK_ARG(value == 0 || value == 1, "ab_ctx_set_option: row prefetch must be 0 or 1");
+      AB_CHECK_ARG(value >= 0 && value <= 2, "ab_ctx_set_option: row prefetch must be 0, 1 or 2");
       ctx->row_prefetch = value;
       return AB_OK;
     case AB_OPT_COARSE_MMA_BITS:

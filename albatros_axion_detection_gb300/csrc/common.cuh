@@ -80,7 +80,7 @@ struct ab_ctx {
   // 1: always FFT; 2: FFT where it runs, else IIR/FIR; 3: FIR, else FFT
   int time_filter_mode = 0;
   int fir_row_tile = 16;     // rows-per-thread class of the IIR / FIR time stage (16: 21 / 17 rows)
-  int row_prefetch = 1;      // time-paired row stage: persistent form with cp.async prefetch (1) or one CTA per tile (0)
+  int row_prefetch = 2;      // time-paired row stage: persistent + prefetch (1), + shared twiddles (2), one CTA per tile (0)
   bool coarse_f16 = true;    // coarse correlator on fp16 (exact) instead of int8 tensor-core MMA
   int row_ffts_per_cta = 8;  // row stage: 8 = time-paired spectra of one input per CTA;
                              // 4 or 2 = pol-paired spectra of one antenna per CTA

@@ -80,7 +80,9 @@ struct SPlan {
   }
 };
 
-template <int R, int S, int N, int NTHR, bool INV>
+// TWS: the twiddle stream lies in shared memory (plain loads) instead of
+// global memory (read-only cache loads)
+template <int R, int S, int N, int NTHR, bool INV, bool TWS = false>
 __device__ __forceinline__ void spass(float2* buf, const float2* __restrict__ tws, int tid) {
   constexpr int NBF = N / R;
 #pragma unroll 1
@@ -101,14 +103,14 @@ __device__ __forceinline__ void spass(float2* buf, const float2* __restrict__ tw
     if constexpr (INV) {
       if (S > 1 && j) {
 #pragma unroll
-        for (int k = 1; k < R; k++) x[k] = cmulc(x[k], __ldg(&tws[(k - 1) * S + j]));
+        for (int k = 1; k < R; k++) x[k] = cmulc(x[k], TWS ? tws[(k - 1) * S + j] : __ldg(&tws[(k - 1) * S + j]));
       }
       dft_any<R, true>(x);
     } else {
       dft_any<R, false>(x);
       if (S > 1 && j) {
 #pragma unroll
-        for (int k = 1; k < R; k++) x[k] = cmul(x[k], __ldg(&tws[(k - 1) * S + j]));
+        for (int k = 1; k < R; k++) x[k] = cmul(x[k], TWS ? tws[(k - 1) * S + j] : __ldg(&tws[(k - 1) * S + j]));
       }
     }
 #pragma unroll
@@ -125,12 +127,12 @@ __device__ __forceinline__ void sdif_from(float2* buf, const float2* tw, int tid
   }
 }
 
-template <class PL, int NTHR, int q>
+template <class PL, int NTHR, int q, bool TWS = false>
 __device__ __forceinline__ void sdit_from(float2* buf, const float2* tw, int tid) {
   if constexpr (q >= 0) {
-    spass<PL::R[q], PL::span(q), PL::N, NTHR, true>(buf, tw + PL::tw_off(q), tid);
+    spass<PL::R[q], PL::span(q), PL::N, NTHR, true, TWS>(buf, tw + PL::tw_off(q), tid);
     __syncthreads();
-    sdit_from<PL, NTHR, q - 1>(buf, tw, tid);
+    sdit_from<PL, NTHR, q - 1, TWS>(buf, tw, tid);
   }
 }
 
@@ -140,9 +142,9 @@ __device__ __forceinline__ void sdif(float2* buf, const float2* tw, int tid) {
   sdif_from<PL, NTHR, 0>(buf, tw, tid);
 }
 // inverse unnormalised (digit-reversed -> natural)
-template <class PL, int NTHR>
+template <class PL, int NTHR, bool TWS = false>
 __device__ __forceinline__ void sdit(float2* buf, const float2* tw, int tid) {
-  sdit_from<PL, NTHR, PL::NP - 1>(buf, tw, tid);
+  sdit_from<PL, NTHR, PL::NP - 1, TWS>(buf, tw, tid);
 }
 
 // position of frequency f after sdif

@@ -473,11 +473,14 @@ __global__ void __launch_bounds__(4 * kRowThreadsPerFft)
 // leaves the packet buffer, and a byte's place in its word does not depend
 // on the row).
 constexpr int kRowPfRows = 8;
-__host__ __device__ inline size_t row_pf_smem_bytes(int P) {
-  return row_smem_bytes(P, 4) + sizeof(int32_t) * 4 * kRowPfRows + sizeof(uint32_t) * 2 * kRowPfRows * kRowThreadsPerFft;
+__host__ __device__ inline size_t row_pf_smem_bytes(int P, int tw_len = 0) {
+  return row_smem_bytes(P, 4) + sizeof(int32_t) * 4 * kRowPfRows + sizeof(uint32_t) * 2 * kRowPfRows * kRowThreadsPerFft +
+         sizeof(float2) * (size_t)tw_len;
 }
 
-template <class PL>
+// TWS (compile-time plans only): the plan's twiddle stream is copied into
+// shared memory once per CTA and the FFT passes read it there.
+template <class PL, bool TWS = false>
 __global__ void __launch_bounds__(4 * kRowThreadsPerFft)
     row_stage_tpair_pf_kernel(Packed4Src src, int nrows, int nin, FftPlan plan, const float2* __restrict__ tw,
                               const float2* __restrict__ tws, float* __restrict__ out, int64_t ld) {
@@ -493,6 +496,13 @@ __global__ void __launch_bounds__(4 * kRowThreadsPerFft)
   SmemTw tws_s{nullptr, nullptr};
   if constexpr (std::is_same<PL, NoPlan>::value)
     tws_s = load_smem_tw(smem + (size_t)FFTS * PL_, tw, P, threadIdx.x, blockDim.x);
+  const float2* twf = tws;  // FFT twiddle stream (global, or its copy in shared memory)
+  if constexpr (TWS) {
+    static_assert(!std::is_same<PL, NoPlan>::value, "shared twiddles need a compile-time plan");
+    float2* tsh = reinterpret_cast<float2*>(st_w + 2 * ROWS * T);
+    for (int q = threadIdx.x; q < PL::tw_len(); q += blockDim.x) tsh[q] = __ldg(&tws[q]);
+    twf = tsh;  // visible after the first barrier of the loop
+  }
   const int nrb = (nrows + ROWS - 1) / ROWS;
   const int ntiles = nrb * nin, G = gridDim.x;
   const bool has_k = ltid < src.nsel;
@@ -568,7 +578,8 @@ __global__ void __launch_bounds__(4 * kRowThreadsPerFft)
       put_pair_t<PL>(buf, plan, P, kabs, v[0], v[1]);
     }
     __syncthreads();
-    fft_inv<PL, kRowThreadsPerFft>(buf, plan, tws_s, P, tws, ltid);
+    if constexpr (TWS) sdit<PL, kRowThreadsPerFft, true>(buf, twf, ltid);
+    else fft_inv<PL, kRowThreadsPerFft>(buf, plan, tws_s, P, tws, ltid);
     const float inv = 1.0f / (float)P;
     const int64_t t0 = (int64_t)(x / nin) * ROWS;
     float* ocol = out + (int64_t)in * P * ld + t0;
@@ -591,15 +602,18 @@ __global__ void __launch_bounds__(4 * kRowThreadsPerFft)
   cp_async_wait<0>();  // nothing left in flight at exit
 }
 
-template <class PL>
+template <class PL, bool TWS = false>
 static int launch_row_tpair_pf_t(ab_ctx* ctx, const Packed4Src& src, int nant, int nrows, int P, const FftPlan& plan,
                                  const float2* twP, const float2* tws, float* out, int64_t ld, cudaStream_t s) {
-  const size_t smem = row_pf_smem_bytes(P);
-  AB_TRY(set_smem_attr(row_stage_tpair_pf_kernel<PL>, smem));
+  size_t smem = row_pf_smem_bytes(P);
+  if constexpr (TWS) smem = row_pf_smem_bytes(P, PL::tw_len());
+  AB_CHECK_ARG(smem <= ctx->smem_optin, "row stage: %zu bytes of shared memory needed", smem);
+  AB_TRY(set_smem_attr(row_stage_tpair_pf_kernel<PL, TWS>, smem));
   const int64_t ntiles = (int64_t)((nrows + kRowPfRows - 1) / kRowPfRows) * 2 * nant;
   AB_CHECK_ARG(ntiles < (1LL << 31), "row stage: too many tiles");
   const int grid = (int)std::min<int64_t>(ntiles, std::max(ctx->num_sms, 1));
-  row_stage_tpair_pf_kernel<PL><<<grid, 4 * kRowThreadsPerFft, smem, s>>>(src, nrows, 2 * nant, plan, twP, tws, out, ld);
+  row_stage_tpair_pf_kernel<PL, TWS><<<grid, 4 * kRowThreadsPerFft, smem, s>>>(src, nrows, 2 * nant, plan, twP, tws, out,
+                                                                              ld);
   AB_LAUNCH_CHECK();
   return AB_OK;
 }
@@ -653,6 +667,8 @@ int launch_row_stage_packed4(ab_ctx* ctx, const Packed4Src& src, int nant, int n
   if (P == Plan4096::N && !tuned) {
     const float2* tws;
     AB_TRY(get_twiddle_stream(ctx, P, {16, 16, 16}, &tws));
+    if (pf && ctx->row_prefetch == 2)
+      return launch_row_tpair_pf_t<Plan4096, true>(ctx, src, nant, nrows, P, plan, twP, tws, out, ld, s);
     if (pf) return launch_row_tpair_pf_t<Plan4096>(ctx, src, nant, nrows, P, plan, twP, tws, out, ld, s);
     return launch_row_tpair_t<Plan4096>(ctx, src, nant, nrows, P, plan, twP, tws, out, ld, s);
   }

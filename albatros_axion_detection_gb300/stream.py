@@ -131,6 +131,36 @@ class StreamCorrelator:
         _lib.call(fn, self._h, raw.data_ptr(), raw.shape[1] * raw.shape[2], mp, mstride, int(chunk),
                   _lib.stream_ptr(raw))
 
+    def run_from_host(self, host: torch.Tensor, dev: torch.Tensor, spec_map: Optional[torch.Tensor] = None,
+                      copy_stream: Optional[torch.cuda.Stream] = None):
+        """Process every chunk from pinned host packets: chunk j's spectra are
+        copied from ``host`` into the device buffer ``dev`` (same shape) on a
+        side stream, ahead of the push that reads them, so the transfers
+        overlap the chain; each push waits only for its own chunk's copy
+        (its 2*cut earlier rows came with the previous chunk)."""
+        if host.shape != dev.shape or host.dtype != torch.uint8 or not host.is_pinned():
+            raise ValueError("host must be a pinned uint8 tensor shaped like dev")
+        if not dev.is_cuda or not dev.is_contiguous() or not host.is_contiguous():
+            raise ValueError("dev must be a contiguous device tensor")
+        cur = torch.cuda.current_stream(dev.device)
+        cs = copy_stream if copy_stream is not None else torch.cuda.Stream(device=dev.device)
+        cs.wait_stream(cur)  # earlier work on dev is done before it is overwritten
+        nspec = host.shape[1]
+        events = []
+        with torch.cuda.stream(cs):
+            for j in range(self.nchunks):
+                lo = j * self.acclen
+                hi = nspec if j == self.nchunks - 1 else min((j + 1) * self.acclen, nspec)
+                for a in range(host.shape[0]):
+                    dev[a, lo:hi].copy_(host[a, lo:hi], non_blocking=True)
+                ev = torch.cuda.Event()
+                ev.record(cs)
+                events.append(ev)
+        for j, ev in enumerate(events):
+            cur.wait_event(ev)
+            self.push(dev, j, spec_map, final=(j == self.nchunks - 1))
+        dev.record_stream(cs)
+
     def vis_device(self) -> torch.Tensor:
         """Device view (njobs, M, M, nq) complex64 of the accumulated visibilities."""
         n = max(len(self.jobs), 1) * self.M * self.M * self.nq

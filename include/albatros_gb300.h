@@ -78,10 +78,11 @@ int ab_ctx_set_time_filter(ab_ctx *ctx, int32_t mode, int32_t row_tile);
  * MMA, 16 (default: fp16 operands, fp32 partial sums, exact) or 8 (int8
  * operands, int32 partial sums). */
 #define AB_OPT_COARSE_MMA_BITS 3
-/* AB_OPT_ROW_PREFETCH: 1 (default) runs the time-paired row stage as
- * persistent CTAs that prefetch the next tile's spectrum-map rows and packet
- * words with cp.async (when at most 256 channels are selected and packet
- * rows are 4-byte multiples); 0 launches one CTA per tile. */
+/* AB_OPT_ROW_PREFETCH: 1 runs the time-paired row stage as persistent CTAs
+ * that prefetch the next tile's spectrum-map rows and packet words with
+ * cp.async (when at most 256 channels are selected and packet rows are
+ * 4-byte multiples); 2 (default) does the same with the FFT twiddles copied
+ * into shared memory once per CTA; 0 launches one CTA per tile. */
 #define AB_OPT_ROW_PREFETCH 5
 int ab_ctx_set_option(ab_ctx *ctx, int32_t option, int32_t value);
 

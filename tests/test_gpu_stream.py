@@ -140,8 +140,9 @@ def test_stream_row_stage_shapes(per_cta, nrows_extra):
 @pytest.mark.parametrize("bits,nrows_extra", [(4, 0), (4, 3), (1, 5)])
 def test_row_prefetch_equals_one_cta_per_tile(bits, nrows_extra):
     """The persistent row stage (cp.async prefetch of map rows and packet
-    words) and the one-CTA-per-tile form compute the same transforms:
-    identical visibilities, with missing spectra and a ragged last tile."""
+    words; FFT twiddles read from global or shared memory) and the
+    one-CTA-per-tile form compute the same transforms: identical
+    visibilities, with missing spectra and a ragged last tile."""
     from albatros_axion_detection_gb300 import autotune
     acclen, cut, nchan = 512 + nrows_extra, 32, 16
     raw = (gen.raw_4bit(seed=5 + nrows_extra, nspec=3 * acclen, nchan=nchan, nant=2) if bits == 4 else
@@ -152,12 +153,40 @@ def test_row_prefetch_equals_one_cta_per_tile(bits, nrows_extra):
     present[0, 90:133] = False
     present[1, 600:611] = False
     spec_map = np.where(present, np.arange(3 * acclen)[None, :], -1).astype(np.int32)
-    a, _ = run(raw, channels, spec_map=spec_map, **kw)
-    autotune.set_row_prefetch(False)
+    a, _ = run(raw, channels, spec_map=spec_map, **kw)  # default: twiddles in shared memory
     try:
+        autotune.set_row_prefetch(0)
         b, _ = run(raw, channels, spec_map=spec_map, **kw)
+        autotune.set_row_prefetch(1)  # twiddles from global memory
+        c, _ = run(raw, channels, spec_map=spec_map, **kw)
     finally:
-        autotune.set_row_prefetch(True)
-    assert np.array_equal(a, b)
+        autotune.set_row_prefetch(autotune.DEFAULT_ROW_PREFETCH)
+    assert np.array_equal(a, b) and np.array_equal(a, c)
     ref, _ = po.repfb_xcorr_avg(raw, channels, spec_present=present, **kw)
     check(a, ref)
+
+
+def test_run_from_host_overlapped_copies_equal_device_run():
+    """Per-chunk host->device copies on a side stream, each push waiting on
+    its own chunk's copy, give the visibilities of a run on device packets."""
+    from albatros_axion_detection_gb300 import stream
+    acclen, nchunks, nchan = 512, 3, 8
+    raw_np = gen.raw_4bit(seed=31, nspec=nchunks * acclen, nchan=nchan, nant=2)
+    mk = lambda: stream.StreamCorrelator(2, np.arange(40, 48), 0, nchan, acclen, nchunks, 16, 16, 32, nchan_raw=nchan)
+    a, b = mk(), mk()
+    try:
+        dev = torch.from_numpy(raw_np).cuda()
+        for j in range(nchunks):
+            a.push(dev, j, final=(j == nchunks - 1))
+        host = torch.from_numpy(raw_np).pin_memory()
+        target = torch.zeros_like(dev)
+        for _ in range(2):  # a second pass reuses the buffer after the first finished
+            b.reset()
+            b.run_from_host(host, target)
+        torch.cuda.synchronize()
+        assert torch.equal(a.vis_device(), b.vis_device())
+        with pytest.raises(ValueError):
+            b.run_from_host(torch.from_numpy(raw_np), target)  # not pinned
+    finally:
+        a.close()
+        b.close()
