@@ -133,3 +133,31 @@ def test_fix_wraps_rejects_two_wraps():
     assert over and s.tolist() == [5, 9, 2 + (1 << 32), 6 + (1 << 32)]
     with pytest.raises(ValueError):
         ingest.fix_wraps(np.array([5, 1, 7, 2]))
+
+
+def test_ingest_header_errors_and_readlen(tmp_path):
+    """Malformed headers raise ValueError; readlen follows the reference
+    (>= 1 packets, (0, 1) a fraction, 0 none, -1 all)."""
+    from albatros_axion_detection_gb300 import ingest
+    chans = gen.header_channels(100, 4, 4)
+    pay = np.random.default_rng(0).integers(0, 256, (10, 3 * len(chans)), dtype=np.uint8)
+    p = str(tmp_path / "ok.raw")
+    gen.write_baseband(p, 10 + 3 * np.arange(10), 3, chans, 4, pay)
+    for rl, n in ((-1, 10), (4, 4), (0.5, 5), (0, 0), (25, 10)):
+        _, pk, sn, _ = ingest.read_packets(p, readlen=rl)
+        assert pk.shape[0] == n and len(sn) == n
+    blob = open(p, "rb").read()
+    bad = tmp_path / "bad.raw"
+    bad.write_bytes(blob[:30])  # truncated header
+    with pytest.raises(ValueError):
+        ingest.read_header(str(bad))
+    b = bytearray(blob)
+    b[32:40] = (2).to_bytes(8, "big")  # bit_mode 2
+    bad.write_bytes(bytes(b))
+    with pytest.raises(ValueError):
+        ingest.read_header(str(bad))
+    b = bytearray(blob)
+    b[8:16] = (len(chans) * 3 + 5).to_bytes(8, "big")  # packet size not holding whole spectra
+    bad.write_bytes(bytes(b))
+    with pytest.raises(ValueError):
+        ingest.read_header(str(bad))
