@@ -151,6 +151,22 @@ def traffic_per_launch(stage):
     return None
 
 
+def replica_ms(ms: float, dist, device) -> float:
+    """Step time of the whole job: the slowest replica's (max over ranks)."""
+    if dist is None:
+        return ms
+    import torch
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(world: int, units_per_rank: float, ms: float) -> float:
+    """Units all ranks processed per second (weak scaling: each rank runs the
+    same per-replica workload)."""
+    return world * units_per_rank / (ms / 1e3)
+
+
 def run_ours(args):
     import torch
     global NSPEC, NANT
@@ -211,12 +227,9 @@ def run_ours(args):
         torch.cuda.synchronize()
     ms = e0.elapsed_time(e1) / args.steps
     barrier()
-    if dist is not None:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = replica_ms(ms, dist, dev)
     spectra_per_step = NANT * NSPEC
-    value = world * spectra_per_step / (ms / 1e3)
+    value = job_throughput(world, spectra_per_step, ms)
 
     # ---- end to end: pinned host packets -> device, chain, visibilities -> host
     host = torch.empty(raw.shape, dtype=torch.uint8, pin_memory=True)
@@ -241,11 +254,7 @@ def run_ours(args):
         e2e_step()
     f1.record(s)
     torch.cuda.synchronize()
-    ms_e2e = f0.elapsed_time(f1) / args.steps
-    if dist is not None:
-        t = torch.tensor([ms_e2e], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_e2e = float(t.item())
+    ms_e2e = replica_ms(f0.elapsed_time(f1) / args.steps, dist, dev)
 
     # ---- per-stage timing (serialised, separate pass) for the roofline
     sc.profile(True)
@@ -276,7 +285,7 @@ def run_ours(args):
                        "time_stage": "%s %d" % sc.time_filter(),
                        "parallelism": f"replicas x{world}",
                        "l2": "inputs larger than L2 (256 MiB packets, 2 x 4.3 GB IPFB intermediates per step)"},
-            "e2e": {"value": world * spectra_per_step / (ms_e2e / 1e3), "unit": "spectra/s",
+            "e2e": {"value": job_throughput(world, spectra_per_step, ms_e2e), "unit": "spectra/s",
                     "ms_per_step": ms_e2e, "h2d_bytes_per_step": int(host.numel()),
                     "d2h_bytes_per_step": int(vis_host.numel() * 8)},
             "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",

@@ -161,3 +161,37 @@ def test_ingest_header_errors_and_readlen(tmp_path):
     bad.write_bytes(bytes(b))
     with pytest.raises(ValueError):
         ingest.read_header(str(bad))
+
+
+def _replica_rank(rank, port, times, out_path):
+    import os
+    import sys
+    import torch.distributed as dist
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    import bench
+    dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank, world_size=len(times))
+    try:
+        ms = bench.replica_ms(times[rank], dist, "cpu")
+        with open(f"{out_path}.{rank}", "w") as f:
+            f.write(repr(ms))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_replica_timing_is_max_over_ranks_gloo(tmp_path):
+    """bench.py's multi-replica timing on two gloo ranks: every rank reports
+    the slowest rank's step time, and the job throughput counts both ranks'
+    spectra."""
+    import socket
+    import torch.multiprocessing as mp
+    import bench
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    times = [120.5, 131.25]
+    out = str(tmp_path / "ms")
+    mp.start_processes(_replica_rank, args=(port, times, out), nprocs=2, join=True, start_method="spawn")
+    for r in range(2):
+        assert float(open(f"{out}.{r}").read()) == max(times)
+    assert bench.replica_ms(7.0, None, "cpu") == 7.0
+    assert bench.job_throughput(2, 2 ** 21, 131.25) == pytest.approx(2 * 2 ** 21 / 0.13125)
