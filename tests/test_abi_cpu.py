@@ -55,3 +55,23 @@ def test_ops_fail_loudly_without_gpu():
     from albatros_axion_detection_gb300 import unpacking
     with pytest.raises((RuntimeError, TypeError)):
         unpacking.unpack_4bit(np.zeros((4, 8), np.uint8), 0, 4, np.arange(4), 4)
+
+
+def test_new_entry_points_check_arguments_on_host():
+    """Histogram and ingest entry points reject bad arguments before any
+    CUDA call (so this runs without a GPU)."""
+    from albatros_axion_detection_gb300 import _lib
+    lib = _lib.load()
+    call = lambda name, *a: getattr(lib, name)(*a)
+    assert call("ab_hist", None, None, 0, 4, 8, 4, 0, None) == -1                      # NULL data
+    assert call("ab_hist", 16, 16, 0, 4, 8, 2, 0, None) == -1                          # bit depth 2
+    assert call("ab_hist", 16, 16, 0, 4, 8, 4, 3, None) == -1                          # mode 3
+    assert call("ab_hist", 16, 16, 0, 4, 7, 1, 0, None) == -1                          # odd 1-bit channels
+    assert call("ab_hist", 17, 16, 0, 4, 8, 4, 0, None) == -1                          # odd 4-bit address
+    assert call("ab_packets_to_rows", None, 4, 24, 16, None) == -1
+    assert call("ab_packets_to_rows", 16, 4, 4, 16, None) == -1                        # no payload
+    assert call("ab_spec_map_add", 16, 4, 0, 0, 0, 16, 8, None) == -1                  # spp 0
+    assert call("ab_spec_map_add", 16, 4, 5, (1 << 31) - 4, 0, 16, 8, None) == -1      # rows beyond int32
+    assert call("ab_spec_map_init", None, 8, None) == -1
+    assert call("ab_spec_map_finish", None, 8, None) == -1
+    assert b"ab_" in lib.ab_last_error()
