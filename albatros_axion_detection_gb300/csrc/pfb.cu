@@ -438,7 +438,7 @@ __global__ void __launch_bounds__(kBandThreads, 3)
 // w_L^(s n) comes from three 64-entry tables (e = s n mod L < 2^18 split in
 // 6-bit digits), so two buffers still leave room for three CTAs per SM.
 __host__ __device__ inline size_t stage_band2_smem() {
-  return sizeof(float2) * (2 * (size_t)padded_len(4096) + 3 * 64 + 16);
+  return sizeof(float2) * (2 * (size_t)padded_len(4096) + 3 * 64 + 16 + 32);
 }
 
 __device__ __forceinline__ float2 tw3(const float2* t, int e) {  // exp(-2 pi i e / L), e < 2^18
@@ -454,6 +454,7 @@ __global__ void __launch_bounds__(kBandThreads, 3)
   float2* bufB = bufA + padded_len(P);
   float2* t3 = bufB + padded_len(P);  // [64] w^(4096 i), [64] w^(64 i), [64] w^i
   float2* w16 = t3 + 192;             // exp(-2 pi i m / 16)
+  float2* qtw = w16 + 16;             // [2][16] w_L^(256 s q) for the two slots
   const int GW = O < 8 ? O : 8, NG = O / GW;
   const int j = blockIdx.x;  // slots 2j, 2j + 1
   const int64_t b = blockIdx.y;
@@ -467,20 +468,27 @@ __global__ void __launch_bounds__(kBandThreads, 3)
   }
   if (tid < 16) w16[tid] = __ldg(&twL[(int64_t)tid * (L / 16)]);
   const int c0 = 2 * j;
+  const int sA = c0, sB = c0 + 1;
+  // w_L^(s n) for n = tid + 256 q is w_L^(s tid) w_L^(256 s q): one factor per
+  // thread, one per q (exact table entries, so two roundings as tw3)
+  if (tid < 32) {
+    const int s = tid < 16 ? sA : sB, q = tid & 15;
+    qtw[tid] = __ldg(&twL[((int64_t)s * kBandThreads * q) % L]);
+  }
   const int g = (2 * c0) / GW, e0 = (2 * c0) % GW;  // slot c0 at float e0 of group g (0 or 4)
   const float* src = W + ((((int64_t)in * nb + b) * NG + g) * P) * GW + e0;
   const int nu = u1 - u0;
   float2* ob = out + ((int64_t)in * nb + b) * ((int64_t)nu * O);
   __syncthreads();
-  const int sA = c0, sB = c0 + 1;
+  const float2 bA = tw3(t3, (int)(((int64_t)sA * tid) % L)), bB = tw3(t3, (int)(((int64_t)sB * tid) % L));
 #pragma unroll 4
   for (int q = 0; q < PER; q++) {
     const int n = tid + q * kBandThreads;
     const float4 v = __ldg(reinterpret_cast<const float4*>(src + (size_t)n * GW));
     float2 xa = j == 0 ? make_float2(v.x, 0.f) : make_float2(v.x, v.y);  // slot 0: the real W_0
-    if (sA) xa = cmul(xa, tw3(t3, (int)(((int64_t)sA * n) % L)));
+    if (sA) xa = cmul(cmul(xa, bA), qtw[q]);
     bufA[pidx(n)] = xa;
-    bufB[pidx(n)] = cmul(make_float2(v.z, v.w), tw3(t3, (int)(((int64_t)sB * n) % L)));
+    bufB[pidx(n)] = cmul(cmul(make_float2(v.z, v.w), bB), qtw[16 + q]);
   }
   __syncthreads();
   spass<16, 256, 4096, kBandThreads, false>(bufA, tws + Plan4096::tw_off(0), tid);
