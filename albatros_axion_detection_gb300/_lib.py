@@ -32,6 +32,8 @@ SIGNATURES = {
     "ab_sortpols": (I32, [P, P, P, I64, I64, I64, I64, I32, I64, I64, P]),
     "ab_make_continuous": (I32, [P, I64, I64, P, I64, P, I64, I64, P, P]),
     "ab_hist": (I32, [P, P, I64, I64, I64, I32, I32, P]),
+    "ab_unpack_4bit_i8": (I32, [P, P, P, I64, I64, P, I64, I64, P]),
+    "ab_unpack_1bit_i8": (I32, [P, P, P, I64, I64, P, I64, I64, P]),
     "ab_packets_to_rows": (I32, [P, I64, I64, P, P]),
     "ab_spec_map_init": (I32, [P, I64, P]),
     "ab_spec_map_add": (I32, [P, I64, I32, I64, I64, P, I64, P]),

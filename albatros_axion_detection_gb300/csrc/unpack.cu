@@ -65,6 +65,34 @@ __global__ void unpack1_kernel(const uint8_t* __restrict__ data, float4* __restr
 #undef PM1
 }
 
+// Int8-complex outputs (re, im as a char2 per value; the 4-bit levels -7..8
+// and the 1-bit +-1 fit exactly), for consumers that keep small integers.
+__device__ __forceinline__ signed char dec4i(unsigned v) { return (signed char)((int)((v + 7u) & 15u) - 7); }
+
+__global__ void unpack4_i8_kernel(const uint8_t* __restrict__ data, char2* __restrict__ pol0, char2* __restrict__ pol1,
+                                  int64_t rowstart, int64_t nrows, const int64_t* __restrict__ channels, int64_t ncols,
+                                  int64_t rowbytes) {
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= nrows * ncols) return;
+  const int64_t r = idx / ncols, k = idx - r * ncols;
+  const uchar2 b = *reinterpret_cast<const uchar2*>(data + (rowstart + r) * rowbytes + 2 * __ldg(&channels[k]));
+  pol0[idx] = make_char2(dec4i(b.x >> 4), dec4i(b.x & 15u));
+  pol1[idx] = make_char2(dec4i(b.y >> 4), dec4i(b.y & 15u));
+}
+
+__global__ void unpack1_i8_kernel(const uint8_t* __restrict__ data, char4* __restrict__ pol0, char4* __restrict__ pol1,
+                                  int64_t rowstart, int64_t nrows, const int64_t* __restrict__ cols, int64_t nbytes_sel,
+                                  int64_t rowbytes) {
+  const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= nrows * nbytes_sel) return;
+  const int64_t r = idx / nbytes_sel, j = idx - r * nbytes_sel;
+  const unsigned b = data[(rowstart + r) * rowbytes + __ldg(&cols[j])];
+#define PM1I(s) ((signed char)((int)(((b) >> (s)) & 1u) * 2 - 1))
+  pol0[idx] = make_char4(PM1I(7), PM1I(6), PM1I(3), PM1I(2));  // channels 2j, 2j+1 of pol0
+  pol1[idx] = make_char4(PM1I(5), PM1I(4), PM1I(1), PM1I(0));
+#undef PM1I
+}
+
 // Device sortpols (unpacking.c:248-368). One thread per output byte.
 __global__ void sortpols_kernel(const uint8_t* __restrict__ data, uint8_t* __restrict__ pol0,
                                 uint8_t* __restrict__ pol1, int64_t rowstart, int64_t nrows, int64_t ncols,
@@ -233,6 +261,33 @@ extern "C" int ab_unpack_4bit_range(const uint8_t* data, float* pol0, float* pol
   if (total <= 0) return AB_OK;
   unpack4_contig_kernel<<<(unsigned)((total + 255) / 256), 256, 0, as_stream(stream)>>>(
       data, (float4*)pol0, (float4*)pol1, rowstart, nrows, c0, ncols, 2 * nchan);
+  AB_LAUNCH_CHECK();
+  return AB_OK;
+}
+
+extern "C" int ab_unpack_4bit_i8(const uint8_t* data, int8_t* pol0, int8_t* pol1, int64_t rowstart, int64_t rowend,
+                                 const int64_t* channels, int64_t ncols, int64_t nchan, void* stream) {
+  AB_CHECK_ARG(data && pol0 && pol1 && channels, "ab_unpack_4bit_i8: NULL pointer");
+  AB_CHECK_ARG(rowstart >= 0 && rowend >= rowstart && ncols >= 0 && nchan > 0, "ab_unpack_4bit_i8: bad sizes");
+  AB_CHECK_ARG(((uintptr_t)data & 1) == 0 && ((uintptr_t)pol0 & 1) == 0 && ((uintptr_t)pol1 & 1) == 0,
+               "ab_unpack_4bit_i8: buffers must be 2-byte aligned");
+  const int64_t total = (rowend - rowstart) * ncols;
+  if (total == 0) return AB_OK;
+  unpack4_i8_kernel<<<(unsigned)((total + 255) / 256), 256, 0, as_stream(stream)>>>(
+      data, (char2*)pol0, (char2*)pol1, rowstart, rowend - rowstart, channels, ncols, 2 * nchan);
+  AB_LAUNCH_CHECK();
+  return AB_OK;
+}
+
+extern "C" int ab_unpack_1bit_i8(const uint8_t* data, int8_t* pol0, int8_t* pol1, int64_t rowstart, int64_t rowend,
+                                 const int64_t* cols, int64_t ncols_bytes, int64_t nchan, void* stream) {
+  AB_CHECK_ARG(data && pol0 && pol1 && cols, "ab_unpack_1bit_i8: NULL pointer");
+  AB_CHECK_ARG(rowstart >= 0 && rowend >= rowstart && ncols_bytes >= 0 && nchan > 1, "ab_unpack_1bit_i8: bad sizes");
+  AB_CHECK_ARG(((uintptr_t)pol0 & 3) == 0 && ((uintptr_t)pol1 & 3) == 0, "ab_unpack_1bit_i8: outputs must be 4-byte aligned");
+  const int64_t total = (rowend - rowstart) * ncols_bytes;
+  if (total == 0) return AB_OK;
+  unpack1_i8_kernel<<<(unsigned)((total + 255) / 256), 256, 0, as_stream(stream)>>>(
+      data, (char4*)pol0, (char4*)pol1, rowstart, rowend - rowstart, cols, ncols_bytes, nchan / 2);
   AB_LAUNCH_CHECK();
   return AB_OK;
 }

@@ -23,12 +23,14 @@ def _rows_view(data: torch.Tensor, bytes_per_spectrum: int, rowend: int, name: s
         raise ValueError(f"rowend {rowend} beyond the {n // bytes_per_spectrum} spectra in {name}")
 
 
-def unpack_4bit(data, rowstart, rowend, channels, length_channels):
+def unpack_4bit(data, rowstart, rowend, channels, length_channels, dtype=torch.complex64):
     """4-bit baseband -> (pol0, pol1) complex64 (rowend-rowstart, len(channels)).
 
     data: device uint8 array holding spectra of 2*length_channels bytes (pol0
     byte then pol1 byte per channel; real = high nibble, imag = low nibble,
-    nibble v > 8 decodes to v - 16). channels: channel INDICES (host)."""
+    nibble v > 8 decodes to v - 16). channels: channel INDICES (host).
+    dtype=torch.int8 returns the same levels as int8 complex instead,
+    (rows, len(channels), 2) with (re, im) last."""
     d = device_array(data, torch.uint8, "data")
     rowstart, rowend, length_channels = int(rowstart), int(rowend), int(length_channels)
     ch = host_int64(channels, "channels")
@@ -38,6 +40,16 @@ def unpack_4bit(data, rowstart, rowend, channels, length_channels):
     if ch.size and (ch.min() < 0 or ch.max() >= length_channels):
         raise ValueError("channel index out of range")
     nrows, ncols = rowend - rowstart, ch.size
+    if dtype == torch.int8:
+        pol0 = torch.empty((nrows, ncols, 2), dtype=torch.int8, device=d.device)
+        pol1 = torch.empty((nrows, ncols, 2), dtype=torch.int8, device=d.device)
+        if nrows and ncols:
+            dch = torch.from_numpy(ch).to(d.device)
+            _lib.call("ab_unpack_4bit_i8", d.data_ptr(), pol0.data_ptr(), pol1.data_ptr(), rowstart, rowend,
+                      dch.data_ptr(), ncols, length_channels, _lib.stream_ptr(d))
+        return pol0, pol1
+    if dtype != torch.complex64:
+        raise ValueError("dtype must be torch.complex64 or torch.int8")
     pol0 = torch.empty((nrows, ncols), dtype=torch.complex64, device=d.device)
     pol1 = torch.empty((nrows, ncols), dtype=torch.complex64, device=d.device)
     if nrows == 0 or ncols == 0:
@@ -55,8 +67,9 @@ def unpack_4bit(data, rowstart, rowend, channels, length_channels):
     return pol0, pol1
 
 
-def unpack_1bit(data, rowstart, rowend, channels, length_channels):
-    """1-bit baseband -> (pol0, pol1) complex64 (rows, len(channels)), values +-1.
+def unpack_1bit(data, rowstart, rowend, channels, length_channels, dtype=torch.complex64):
+    """1-bit baseband -> (pol0, pol1) complex64 (rows, len(channels)), values +-1
+    (dtype=torch.int8: int8 complex, (rows, len(channels), 2)).
 
     Like the reference's GPU path, byte columns channels[::2]//2 are decoded and
     each byte fills two consecutive output channels (the channel list must be
@@ -73,6 +86,16 @@ def unpack_1bit(data, rowstart, rowend, channels, length_channels):
     _rows_view(d, length_channels // 2, rowend)
     cols = ch[::2] // 2
     nrows = rowend - rowstart
+    if dtype == torch.int8:
+        pol0 = torch.empty((nrows, ch.size, 2), dtype=torch.int8, device=d.device)
+        pol1 = torch.empty((nrows, ch.size, 2), dtype=torch.int8, device=d.device)
+        if nrows and ch.size:
+            dcols = torch.from_numpy(np.ascontiguousarray(cols)).to(d.device)
+            _lib.call("ab_unpack_1bit_i8", d.data_ptr(), pol0.data_ptr(), pol1.data_ptr(), rowstart, rowend,
+                      dcols.data_ptr(), cols.size, length_channels, _lib.stream_ptr(d))
+        return pol0, pol1
+    if dtype != torch.complex64:
+        raise ValueError("dtype must be torch.complex64 or torch.int8")
     pol0 = torch.empty((nrows, ch.size), dtype=torch.complex64, device=d.device)
     pol1 = torch.empty((nrows, ch.size), dtype=torch.complex64, device=d.device)
     if nrows == 0 or ch.size == 0:

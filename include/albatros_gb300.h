@@ -109,6 +109,15 @@ int ab_unpack_4bit_range(const uint8_t *data, float *pol0, float *pol1, int64_t 
 int ab_unpack_1bit(const uint8_t *data, float *pol0, float *pol1, int64_t rowstart, int64_t rowend,
                    const int64_t *cols, int64_t ncols_bytes, int64_t nchan, void *stream);
 
+/* ab_unpack_4bit_i8 / ab_unpack_1bit_i8: the same decodes (arguments as
+ * ab_unpack_4bit / ab_unpack_1bit) into int8 complex, (re, im) byte pairs:
+ * pol0/pol1 (rows, ncols, 2) int8.  The levels (-7..8 for 4-bit, +-1 for
+ * 1-bit) are exact in int8; for consumers that keep small integers. */
+int ab_unpack_4bit_i8(const uint8_t *data, int8_t *pol0, int8_t *pol1, int64_t rowstart, int64_t rowend,
+                      const int64_t *channels, int64_t ncols, int64_t nchan, void *stream);
+int ab_unpack_1bit_i8(const uint8_t *data, int8_t *pol0, int8_t *pol1, int64_t rowstart, int64_t rowend,
+                      const int64_t *cols, int64_t ncols_bytes, int64_t nchan, void *stream);
+
 /* ab_sortpols: replaces sortpols (albatros_analysis/src/correlations/unpacking.c:248-368,
  * albatros_analysis/src/correlations/unpacking.py:305-377), on the device.
  * pol0/pol1: (rowend-rowstart, ncols) bytes. bit_depth 4 or 1. */

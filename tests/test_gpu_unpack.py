@@ -139,3 +139,24 @@ def test_hist_edge_cases():
         hist(d, 0, 11, 8, 4, 0)  # past the end of the data
     with pytest.raises(ValueError):
         hist(cu(gen.raw_1bit(seed=1, nspec=4, nchan=8)), 0, 4, 7, 1, 0)  # odd 1-bit channel count
+
+
+@pytest.mark.parametrize("bits", [4, 1])
+def test_unpack_int8_complex_equals_float(bits):
+    """The int8-complex outputs hold exactly the complex64 decodes' levels."""
+    from albatros_axion_detection_gb300.unpacking import unpack_1bit, unpack_4bit
+    if bits == 4:
+        raw = cu(gen.raw_4bit_uniform(seed=8, nspec=777, nchan=40))
+        ch, fn = np.array([0, 3, 4, 17, 39, 21]), unpack_4bit
+    else:
+        raw = cu(gen.raw_1bit(seed=8, nspec=777, nchan=40))
+        ch, fn = np.arange(6, 30), unpack_1bit
+    f0, f1 = fn(raw, 5, 770, ch, 40)
+    i0, i1 = fn(raw, 5, 770, ch, 40, dtype=torch.int8)
+    assert i0.dtype == torch.int8 and i0.shape == (765, len(ch), 2)
+    for f, i in ((f0, i0), (f1, i1)):
+        assert torch.equal(torch.view_as_real(f), i.float())
+    e0, _ = fn(raw, 3, 3, ch, 40, dtype=torch.int8)
+    assert e0.shape == (0, len(ch), 2)
+    with pytest.raises(ValueError):
+        fn(raw, 0, 4, ch, 40, dtype=torch.float16)
