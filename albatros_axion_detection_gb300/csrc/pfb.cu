@@ -481,7 +481,7 @@ __global__ void __launch_bounds__(kBandThreads, 3)
   float2* ob = out + ((int64_t)in * nb + b) * ((int64_t)nu * O);
   __syncthreads();
   const float2 bA = tw3(t3, (int)(((int64_t)sA * tid) % L)), bB = tw3(t3, (int)(((int64_t)sB * tid) % L));
-#pragma unroll 8
+#pragma unroll 16
   for (int q = 0; q < PER; q++) {
     const int n = tid + q * kBandThreads;
     const float4 v = __ldg(reinterpret_cast<const float4*>(src + (size_t)n * GW));
