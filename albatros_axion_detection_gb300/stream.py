@@ -6,8 +6,9 @@ ProcessingConfig fields, the same job planner (JobChunkPlanner.plan_chunks
 :233-263), the same band [channels[chanstart]*osamp, channels[chanend]*osamp)
 (:342-343) and visibility layout (M, M, nchan, njobs) F-ordered (:347).  The
 per-chunk work and all overlap state live on the device in an ``ab_stream``
-object (csrc/chain.cu).  Inputs are 4-bit packets already on the device
-(file ingest is the caller's).
+object (csrc/chain.cu).  Inputs are 4-bit or 1-bit packets on the device
+(``ingest`` builds them, with their spectrum map, from baseband files), or
+pinned host packets streamed in chunk by chunk (``run_from_host``).
 """
 from __future__ import annotations
 
