@@ -48,7 +48,7 @@ struct ab_stream {
   bool fused = false;        // PFB fold fused into the time stage (osamp >= 4)
   float* state = nullptr;    // fused: last 4*osamp timestream rows per column (x2 for the FIR path)
   int fir_J = 0;             // > 0: time stage as a (2J+1)-tap FIR (fir.cu)
-  int iir_W = 0;             // > 0: time stage as the IIR factorisation, warm-up iir_W (fir.cu)
+  int iir_W = 0;             // > 0: time stage as the IIR factorisation, states carried over iir_W rows (fir.cu)
   int fir_row_tile = 16;     // rows-per-thread class of the IIR / FIR stage
   const float* fir_taps = nullptr;
   float* W = nullptr;

@@ -291,7 +291,7 @@ static bool iir_factor(const double* w, double t, double coef[kIirCoef], int* wa
     if (std::fabs(br * br + bi * bi - dd) > 1e-11 * dd) return false;
   }
   const double a1 = b[1] / b[0], a2 = b[2] / b[0], a3 = b[3] / b[0];
-  // decay of 1/A: warm-up length
+  // decay of 1/A: rows over which a recursion state must be carried
   double h[600] = {1.0};
   double peak = 1.0;
   int last = 0;
@@ -318,8 +318,8 @@ static bool iir_factor(const double* w, double t, double coef[kIirCoef], int* wa
   return true;
 }
 
-// Per-column IIR coefficients as float (P, kIirCoef) and the
-// warm-up IW in {40, 80} (0 when no factorisation or a longer warm-up is
+// Per-column IIR coefficients as float (P, kIirCoef) and the state-carry
+// length IW in {40, 80} rows (0 when no factorisation or a longer carry is
 // needed), cached in the context per (P, ntap, thresh).
 int get_iir_coeffs(ab_ctx* ctx, int P, int ntap, float thresh, int* W_out, const float** coef_out) {
   *W_out = 0;

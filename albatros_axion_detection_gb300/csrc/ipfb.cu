@@ -374,8 +374,8 @@ static int set_smem_attr(K kernel, size_t bytes) {
 // Time-paired form: a CTA takes 8 consecutive spectra of ONE input (antenna
 // a, pol p = blockIdx.y % 2) and transforms spectra (t, t+1) together as
 // Z = A_t + i A_{t+1}.  Each column then receives 8 consecutive rows (32 bytes,
-// one full sector), written by two lanes with 16-byte stores, so a warp store
-// covers 16 whole sectors.  (Pairing the two pols of one spectrum instead
+// one full sector) in one 32-byte store (two 16-byte stores by a lane pair
+// when the column is only 16-byte aligned).  (Pairing the two pols of one spectrum instead
 // leaves 16 bytes per column and input, half a sector per lane.)
 template <class PL>
 __global__ void __launch_bounds__(4 * kRowThreadsPerFft)

@@ -92,7 +92,7 @@ struct FirArgs {
   float* state_out;       // this chunk's last 4*O rows (the other buffer)
   const float2* tw64;
   int num_sms;            // persistent grid: CTAs per SM x num_sms
-  int iir_w;              // > 0: IIR form with this warm-up
+  int iir_w;              // > 0: IIR form, states carried over iir_w rows
 };
 // Per-device constants of the FIR time stage (call once per device).
 int fir_init_device();

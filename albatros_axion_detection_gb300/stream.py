@@ -174,7 +174,7 @@ class StreamCorrelator:
         return int(_lib.load().ab_stream_fir_taps(self._h))
 
     def time_filter(self):
-        """("fft", 0), ("fir", J) or ("iir", warm-up samples): the form of the
+        """("fft", 0), ("fir", J) or ("iir", rows a state is carried): the form of the
         IPFB time stage this stream runs."""
         kind, param = ctypes.c_int32(), ctypes.c_int32()
         _lib.call("ab_stream_time_filter", self._h, ctypes.byref(kind), ctypes.byref(param))

@@ -317,7 +317,7 @@ int64_t ab_stream_kernel_launches(const ab_stream *st);
 /* Half-length J of the FIR time stage this stream runs (0: another form). */
 int64_t ab_stream_fir_taps(const ab_stream *st);
 /* Time stage form of this stream: kind 0 = FFT, 1 = FIR (param = J),
- * 2 = IIR (param = warm-up samples). */
+ * 2 = IIR (param = rows over which a recursion state is carried). */
 int ab_stream_time_filter(const ab_stream *st, int32_t *kind, int32_t *param);
 int64_t ab_stream_workspace_bytes(const ab_stream *st);
 int ab_stream_set_workspace(ab_stream *st, void *ws, int64_t bytes);
