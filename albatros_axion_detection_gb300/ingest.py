@@ -131,6 +131,17 @@ def read_packets(path: str, readlen=-1, header: Optional[BasebandHeader] = None)
     return h, buf, sn, over
 
 
+def first_specnum(path: str, header: Optional[BasebandHeader] = None) -> Optional[int]:
+    """Spectrum number of a file's first packet (None when it has none), read
+    without loading the file; an inside-file wrap never changes it."""
+    h = header or read_header(path)
+    if h.num_packets == 0:
+        return None
+    with open(path, "rb") as f:
+        f.seek(h.header_bytes)
+        return int(struct.unpack(">I", f.read(4))[0])
+
+
 @dataclass
 class AntennaFiles:
     """The files of one antenna that a run reads, with each file's rows in
@@ -140,11 +151,12 @@ class AntennaFiles:
     paths: List[str] = field(default_factory=list)
     row0: List[int] = field(default_factory=list)
     specnums: List[np.ndarray] = field(default_factory=list)
-    packets: List[torch.Tensor] = field(default_factory=list)
+    packets: List[torch.Tensor] = field(default_factory=list)  # pinned host packets, released after upload
+    npkt: List[int] = field(default_factory=list)
 
     @property
     def rows(self) -> int:
-        return sum(p.shape[0] for p in self.packets) * self.header.spectra_per_packet
+        return sum(self.npkt) * self.header.spectra_per_packet
 
 
 def plan_antenna(paths: Sequence[str], fileidx: int, idxstart: int, nspec: int) -> AntennaFiles:
@@ -154,6 +166,10 @@ def plan_antenna(paths: Sequence[str], fileidx: int, idxstart: int, nspec: int) 
     inside (the BasebandFileIterator's overflow counter, :594-603)."""
     ctr, af = 0, None
     for path in paths[fileidx:]:
+        if af is not None:  # a file starting past the run is not read at all
+            s0 = first_specnum(path)
+            if s0 is not None and s0 + ctr * WRAP >= af.start + nspec:
+                break
         h, pk, sn, over = read_packets(path)
         sn = sn + ctr * WRAP
         if over:
@@ -172,6 +188,7 @@ def plan_antenna(paths: Sequence[str], fileidx: int, idxstart: int, nspec: int) 
         af.row0.append(af.rows)
         af.specnums.append(sn)
         af.packets.append(pk)
+        af.npkt.append(int(pk.shape[0]))
         if len(sn) and sn[-1] + h.spectra_per_packet >= af.start + nspec:
             break
     if af is None:
@@ -201,13 +218,14 @@ def ingest(files: Sequence[Sequence[str]], idxs: Sequence[int], nspec: int, devi
         for r0, sn, pk in zip(a.row0, a.specnums, a.packets):
             if pk.shape[0] == 0:
                 continue
-            body = pk.to(dev, non_blocking=True)
+            body = pk.to(dev, non_blocking=True)  # the pinned buffer is held until this copy is done
             dst = raw[k, r0: r0 + pk.shape[0] * a.header.spectra_per_packet]
             _lib.call("ab_packets_to_rows", body.data_ptr(), pk.shape[0], pk.shape[1], dst.data_ptr(), s)
             dsn = torch.from_numpy(sn).to(dev, non_blocking=True)
             _lib.call("ab_spec_map_add", dsn.data_ptr(), len(sn), a.header.spectra_per_packet, r0, a.start,
                       m.data_ptr(), m.numel(), s)
         _lib.call("ab_spec_map_finish", m.data_ptr(), m.numel(), s)
+        a.packets = []  # the uploads hold their pinned buffers until done; nothing else needs them
     return raw, spec_map, ants
 
 
