@@ -127,6 +127,30 @@ def test_ingest_host_side_matches_reference(golden_int, name, tmp_path):
         np.testing.assert_array_equal(sn, golden_int[f"bb_{name}_{k}_specnum"] + ctr[k] * (1 << 32))
 
 
+def test_plan_antenna_reads_only_files_in_the_run(tmp_path, monkeypatch):
+    """A file whose first spectrum lies past the run is only peeked at: its
+    packets are not read and it is not part of the antenna's rows."""
+    from albatros_axion_detection_gb300 import ingest
+    chans = gen.header_channels(100, 4, 4)
+    rng = np.random.default_rng(1)
+    paths = []
+    for k, s0 in enumerate((1000, 1030, 5000)):  # the run [1000, 1060) ends inside a gap before the third file
+        p = str(tmp_path / f"f{k}.raw")
+        gen.write_baseband(p, s0 + 3 * np.arange(8), 3, chans, 4,
+                           rng.integers(0, 256, (8, 3 * len(chans)), dtype=np.uint8))
+        paths.append(p)
+    assert ingest.first_specnum(paths[2]) == 5000
+    read = []
+    real = ingest.read_packets
+    monkeypatch.setattr(ingest, "read_packets", lambda p, *a, **k: (read.append(p), real(p, *a, **k))[1])
+    af = ingest.plan_antenna(paths, 0, 0, 60)
+    assert read == paths[:2] and af.paths == paths[:2]
+    assert af.row0 == [0, 24] and af.rows == 48 and af.npkt == [8, 8]
+    empty = str(tmp_path / "empty.raw")
+    gen.write_baseband(empty, np.zeros(0, np.int64), 3, chans, 4, np.zeros((0, 3 * len(chans)), np.uint8))
+    assert ingest.first_specnum(empty) is None
+
+
 def test_fix_wraps_rejects_two_wraps():
     from albatros_axion_detection_gb300 import ingest
     s, over = ingest.fix_wraps(np.array([5, 9, 2, 6]))
