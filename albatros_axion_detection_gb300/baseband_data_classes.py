@@ -2,7 +2,6 @@
 (albatros_analysis/src/correlations/baseband_data_classes.py:48-73)."""
 from __future__ import annotations
 
-import numpy as np
 import torch
 
 from . import _lib

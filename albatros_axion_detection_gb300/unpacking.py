@@ -4,8 +4,6 @@ unpack_1bit :248-302, sortpols :305-377, hist :82-138), computed by the CUDA ker
 csrc/unpack.cu through the C-ABI."""
 from __future__ import annotations
 
-import ctypes
-
 import numpy as np
 import torch
 

@@ -24,7 +24,7 @@ import time
 import numpy as np
 import scipy.fft as sfft
 
-from . import HERE, c_oracle, ref_libs
+from . import c_oracle, ref_libs
 from . import pfb_oracle as po
 
 

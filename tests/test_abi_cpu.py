@@ -1,7 +1,6 @@
 """C-ABI shape checks that need no GPU: the library loads, exports every
 symbol declared in include/*.h, and rejects bad arguments with AB_ERR_ARG
 before touching the device."""
-import ctypes
 import glob
 import os
 import re

@@ -8,7 +8,6 @@ a row with different data (the shared buffer must not leak the first call's
 sums into the second).  This file is collected last so a failure here does not
 hide the rest of the suite; it passes alone or after the other tests.
 """
-import numpy as np
 import pytest
 import torch
 
