@@ -619,7 +619,7 @@ static int launch_row_tpair_pf_t(ab_ctx* ctx, const Packed4Src& src, int nant, i
 }
 
 template <class PL>
-static int launch_row_tpair_t(ab_ctx* ctx, const Packed4Src& src, int nant, int nrows, int P, const FftPlan& plan,
+static int launch_row_tpair_t(ab_ctx* /*ctx*/, const Packed4Src& src, int nant, int nrows, int P, const FftPlan& plan,
                               const float2* twP, const float2* tws, float* out, int64_t ld, cudaStream_t s) {
   const size_t smem = row_smem_bytes(P, 4);
   AB_TRY(set_smem_attr(row_stage_tpair_kernel<PL>, smem));
@@ -700,7 +700,7 @@ int launch_row_stage_c64(ab_ctx* ctx, const float2* dat, int64_t nslice, int P, 
 }
 
 template <class PL, int NTHR>
-static int launch_time_t(ab_ctx* ctx, float* buf, int64_t ld, int ninputs, int P, int N, const FftPlan& planM,
+static int launch_time_t(ab_ctx* /*ctx*/, float* buf, int64_t ld, int ninputs, int P, int N, const FftPlan& planM,
                          const float2* twN, const float2* tws, const int2* pairs, const float2* table,
                          const float* wtaps, int ntap, float thresh, size_t smem, cudaStream_t s) {
   dim3 grid((unsigned)P, (unsigned)ninputs);
