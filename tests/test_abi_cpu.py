@@ -36,6 +36,13 @@ def test_library_exports_every_declared_symbol():
     assert set(_lib.SIGNATURES) <= set(declared_symbols())
 
 
+def test_integration_guide_binds_every_symbol():
+    """Every declared entry point appears in the maintainer's binding guide."""
+    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    missing = [n for n in declared_symbols() if not re.search(rf"\b{n}\b", text)]
+    assert not missing, f"no binding shown for: {missing}"
+
+
 def test_bad_arguments_are_rejected_on_host():
     from albatros_axion_detection_gb300 import _lib
     lib = _lib.load()
