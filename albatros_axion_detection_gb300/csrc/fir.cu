@@ -236,7 +236,7 @@ int get_fir_taps(ab_ctx* ctx, int P, int N, int ntap, float thresh, int* J_out, 
 // thread's rows), each padded to 8 floats.
 constexpr int kIirU32 = 41, kIirU16 = 21, kIirCoef = 24;
 
-static bool iir_factor(const double* w, double t, double coef[kIirCoef], int* warm) {
+static bool iir_factor(const double* w, double t, double coef[kIirCoef], int* carry) {
   const int m = 3;
   double d[4];
   for (int k = 0; k <= m; k++) {
@@ -301,7 +301,7 @@ static bool iir_factor(const double* w, double t, double coef[kIirCoef], int* wa
     if (std::fabs(h[k]) > 1e-10 * peak) last = k;
   }
   if (last >= 590 || peak > 1e6) return false;
-  *warm = last + 1;
+  *carry = last + 1;  // rows after which 1/A's impulse response stays below 1e-10 of its peak
   const double g = (1.0 + t * t) / (b[0] * b[0]);  // folded into the FIR taps
   coef[0] = g * w[0];
   coef[1] = g * w[1];
@@ -340,17 +340,17 @@ int get_iir_coeffs(ab_ctx* ctx, int P, int ntap, float thresh, int* W_out, const
   std::vector<double> w;
   sinc_hamming_host(ntap, P, w);
   std::vector<float> cf((size_t)P * kIirCoef);
-  int warm = 0;
+  int carry = 0;
   bool ok = thresh > 0.f;
   for (int n = 0; n < P && ok; n++) {
     double wn[4], c[kIirCoef];
     for (int k = 0; k < 4; k++) wn[k] = w[(size_t)k * P + n];
     int wm = 0;
     ok = iir_factor(wn, (double)thresh, c, &wm);
-    warm = std::max(warm, wm);
+    carry = std::max(carry, wm);
     for (int k = 0; k < kIirCoef; k++) cf[(size_t)n * kIirCoef + k] = (float)c[k];
   }
-  const int IW = !ok ? 0 : warm <= 40 ? 40 : warm <= 80 ? 80 : 0;
+  const int IW = !ok ? 0 : carry <= 40 ? 40 : carry <= 80 ? 80 : 0;
   float* dc = nullptr;
   if (IW > 0) {
     if (cudaMalloc(&dc, sizeof(float) * cf.size()) != cudaSuccess) {

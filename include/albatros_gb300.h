@@ -54,7 +54,7 @@ int ab_ctx_set_fft_plan(ab_ctx *ctx, int64_t n, const int32_t *radices, int64_t 
  * compute the reference's circular Wiener deconvolution:
  *  - IIR: the filter W(z)(1+t^2)/D(z) factored (FP64, Wilson's spectral
  *    factorisation) into a 4-tap FIR and causal + anti-causal 3-pole
- *    recursions, warmed up over 40 or 80 samples; usable when the
+ *    recursions, whose states are carried over 40 or 80 rows; usable when the
  *    factorisation converges and the poles decay fast enough;
  *  - FIR: a (2J+1)-tap FIR (J = 32 or 64, taps of the FP64 filter at the same
  *    nslice bins), usable when the dropped tail is below 1e-7 of the norm;
