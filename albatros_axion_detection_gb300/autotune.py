@@ -1,8 +1,8 @@
-"""Autotuner for the chain's time stage: FIR row tile, or FFT radix order.
+"""Autotuner for the chain's time stage: IIR / FIR row tile, or FFT radix order.
 
 The IPFB time-axis deconvolution has three forms in the library.  The IIR and
 FIR forms (the default wherever the reference's Wiener filter decays fast
-enough) have one tunable tile: the kept rows per thread (16 or 32), which sets
+enough; IIR first) have one tunable tile: the kept rows per thread (16 or 32), which sets
 the rows a CTA filters and how many CTAs share an SM.  The FFT form runs one real FFT of
 nslice = acclen + 2*cut points per coarse sample phase (a complex FFT of
 n = nslice/2 points) and its inverse; two lengths have compile-time plans
@@ -124,18 +124,18 @@ _filter_setting = {"mode": DEFAULT_MODE, "row_tile": DEFAULT_ROW_TILE}
 
 
 def set_time_filter(mode: int = DEFAULT_MODE, row_tile: int = 0, device: Optional[int] = None) -> None:
-    """Time stage of streams created from now on: mode 0 = FIR where it is
-    accurate, else FFT (the default), 1 = FFT only, 2 = FFT where it runs,
-    else FIR; row_tile 16/32 (0 keeps it)."""
+    """Time stage of streams created from now on: mode 0 = IIR where the
+    filter factors and decays fast enough, else FIR where it is accurate,
+    else FFT (the default); 1 = FFT only; 2 = FFT where its length factors,
+    else IIR or FIR; 3 = FIR, else FFT.  row_tile 16/32 (0 keeps it)."""
     _lib.call("ab_ctx_set_time_filter", _lib.ctx(device), int(mode), int(row_tile))
     _filter_setting["mode"] = int(mode)
     if row_tile:
         _filter_setting["row_tile"] = int(row_tile)
 
 
+# ab_ctx_set_option keys (AB_OPT_* in include/albatros_gb300.h)
 OPT_ROW_FFTS_PER_CTA = 1
-
-
 OPT_COARSE_MMA_BITS = 3
 OPT_ROW_PREFETCH = 5
 DEFAULT_ROW_PREFETCH = 2
