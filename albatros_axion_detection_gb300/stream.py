@@ -170,7 +170,7 @@ class StreamCorrelator:
         return t.view(max(len(self.jobs), 1), self.M, self.M, self.nq)[: len(self.jobs)]
 
     def fir_taps(self) -> int:
-        """Half-length J of the FIR time stage (0: the FFT time stage runs)."""
+        """Half-length J of the FIR time stage (0: the IIR or FFT form runs)."""
         return int(_lib.load().ab_stream_fir_taps(self._h))
 
     def time_filter(self):
