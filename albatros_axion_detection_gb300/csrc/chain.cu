@@ -3,23 +3,28 @@
 // (albatros_analysis/scripts/xcorr/helper_gpu_stream_clean.py:295-456).
 //
 // Per pushed chunk of acclen new spectra (all M = 2*nant inputs at once):
-//   1. row stage   : decode the 4-bit packets of local rows [0, nslice)
-//                    (global spectra chunk*acclen - 2cut ...), place the
-//                    selected channels, P-point inverse FFT, write the
-//                    [n][t] intermediate (ping-pong buffer chunk % 2);
-//   2. time stage  : per column, rfft -> Wiener filter (evaluated on the
-//                    fly from the ntap window taps) -> irfft, in place;
+//   1. row stage   : decode the 4-bit (or 1-bit) packets of local rows
+//                    [0, nslice) (global spectra chunk*acclen - 2cut ...)
+//                    through the spectrum map, place the selected channels,
+//                    P-point inverse FFT, write the [n][t] intermediate;
+//   2. time stage  : per column, the Wiener deconvolution along time, in one
+//                    of three forms (fir.cu, ipfb.cu): the IIR factorisation
+//                    (default), a (2J+1)-tap FIR, or rfft -> filter -> irfft;
 //   3. PFB stage A : tap fold + osamp-point DFT for every fine block whose
-//                    ntap*osamp rows are now available (rows before this
-//                    chunk come from the other ping-pong buffer);
+//                    ntap*osamp rows are now available;
 //   4. PFB stage B : osamp fine offsets x P-point DFT, keeping only the
 //                    fine band [q0, q1);
 //   5. correlate   : accumulate Y_i conj(Y_j) / nblock into each block's job.
+// With osamp >= 4 and ntap = 4 ("fused"), step 3 runs inside the IIR / FIR
+// time stage, and the last 4*osamp timestream rows of every column are kept
+// in `state` for the blocks that straddle the next chunk; otherwise the
+// intermediate is a ping-pong pair (buffer chunk % 2) and step 3 reads the
+// previous chunk's rows from the other buffer.
 //
 // The reference's overlap state (the 2*cut coarse rows carried between IPFB
 // chunks and the ntap-1 fine blocks carried between PFB jobs) is realised by
-// re-decoding the previous 2*cut packets in step 1 and by reading the previous
-// chunk's IPFB output in step 3; nothing is copied between chunks.
+// re-decoding the previous 2*cut packets in step 1 and by the carried rows
+// of step 3; no packets are copied between chunks.
 #include <algorithm>
 
 #include "ipfb.cuh"
