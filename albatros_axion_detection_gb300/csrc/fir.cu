@@ -1,5 +1,7 @@
-// fir.cu -- the IPFB time-axis Wiener deconvolution as a short two-sided FIR,
-// fused with the forward-PFB fold, for the streaming chain.
+// fir.cu -- the IPFB time-axis Wiener deconvolution as a short filter, fused
+// with the forward-PFB fold, for the streaming chain: as a (2J+1)-tap FIR
+// (this header) or as its IIR factorisation (from "IIR time stage" on), which
+// the chain tries first.
 //
 // Reference (cupy_ipfb, albatros_analysis/src/utils/pfb_gpu_utils.py:56-91):
 // per sample phase n the column x[t] (t < nslice) is transformed along time,
@@ -19,7 +21,9 @@
 // FFT time stage runs).  This replaces two nslice-point FFTs per column with
 // 2J+1 FMAs per kept sample.
 //
-// Kernel layout: one CTA per (segment of a column, column n, input).  A
+// Kernel layout: persistent CTAs (two per SM; one for the 129-tap FIR) walk the items
+// (segment of a column, column n, input), staging the next item's rows with
+// cp.async while they compute the current one.  A
 // segment owns the fine blocks whose last row falls in its kept rows
 // [s0, s0 + S); it recomputes the 4*O rows before s0 (segment 0 reads them
 // from the previous chunk's tail state instead), folds and DFTs its blocks

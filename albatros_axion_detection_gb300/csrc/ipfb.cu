@@ -7,8 +7,9 @@
 //   ddft = rfft(dd.T, axis=1)                 (P, nslice/2+1)
 //   res  = irfft(ddft * filt, axis=1).T       /nslice
 // Here stage 1 computes dd in the [n][t] layout (column n = sample phase,
-// contiguous in t), stage 2 does rfft -> *filt -> irfft on each column inside
-// one CTA's shared memory.
+// contiguous in t); stage 2 in its FFT form (this file) does rfft -> *filt ->
+// irfft on each column inside one CTA's shared memory.  The IIR and FIR forms
+// of stage 2, the streaming chain's default, are in fir.cu.
 #include <math.h>
 
 #include <type_traits>

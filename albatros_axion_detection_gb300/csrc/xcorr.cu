@@ -4,10 +4,13 @@
 //    (albatros_analysis/src/correlations/correlations_gpu.py:95-121), which the
 //    reference runs as cublasCgemmStridedBatched (cgemm_batch.cu:8-53);
 //  * the streaming chain's per-job accumulation of the same products;
-//  * exact integer coarse correlator on raw 4-bit packets with tensor cores
-//    (mma.sync m16n8k32 s8 -> s32, flushed into int64): tcgen05 kind::i8 is
-//    not offered for sm_103a, kind::f16 would need an exactness argument on
-//    the FP32 accumulator, the s8 mma is exact by construction;
+//  * exact integer coarse correlator on raw 4-bit packets with tensor cores,
+//    flushed into int64: by default mma.sync m16n8k16 with fp16 operands and
+//    fp32 partial sums, exact because the levels (-8..7) are exact in fp16,
+//    products are at most 64 and a CTA's partial sums over at most 4096
+//    samples stay below 2^24; or mma.sync m16n8k32 s8 -> s32
+//    (AB_OPT_COARSE_MMA_BITS = 8).  tcgen05 kind::i8 is not offered for
+//    sm_103a;
 //  * pairwise 4-bit / 1-bit correlators on sortpols'd bytes
 //    (albatros_analysis/src/correlations/correlations_cpu.c:128-638).
 #include <cuda_fp16.h>
