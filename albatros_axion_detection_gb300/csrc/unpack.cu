@@ -1,5 +1,6 @@
-// unpack.cu -- packed-baseband decode kernels: 4-bit and 1-bit unpack to c64,
-// device sortpols, and make_continuous placement.
+// unpack.cu -- packed-baseband decode kernels: 4-bit and 1-bit unpack to c64
+// or int8 complex, device sortpols, make_continuous placement, and the
+// quantisation histograms.
 //
 // 4-bit rule (albatros_analysis/src/correlations/unpacking.c:187-202): a
 // nibble v maps to v-16 when v > 8, else v, so 0x8 decodes to +8.  In integer
