@@ -13,7 +13,7 @@ device memory grows with the number of lanes, not the number of files.  The
 whole batch (optionally with the host->device copies of the packets and the
 device->host copies of the visibilities) is captured once into a CUDA graph
 and replayed.  The time stage of each (acclen, cut, osamp) comes from the
-autotuner (``autotune.tune_configs``: FIR row tile, or FFT radix order).
+autotuner (``autotune.tune_configs``: IIR / FIR row tile, or FFT radix order).
 """
 from __future__ import annotations
 
