@@ -367,6 +367,15 @@ static int stream_push(ab_stream* st, const uint8_t* raw, int64_t ant_stride, co
                (long long)chunk);
   const int P = st->P, O = st->O, M = st->M;
   const int64_t acclen = st->acclen, cut = st->cut, nslice = st->nslice;
+  // the row stage reads spectra up to (chunk+1)*acclen - 1: through the map,
+  // or as raw rows when there is none
+  const int64_t need = (chunk + 1) * acclen, row_bytes = st->bits == 4 ? 2 * st->nchan_raw : st->nchan_raw / 2;
+  if (spec_map)
+    AB_CHECK_ARG(map_stride >= need, "ab_stream_push: spectrum map of %lld entries, chunk %lld needs %lld",
+                 (long long)map_stride, (long long)chunk, (long long)need);
+  else
+    AB_CHECK_ARG(ant_stride >= need * row_bytes, "ab_stream_push: %lld bytes per antenna, chunk %lld needs %lld",
+                 (long long)ant_stride, (long long)chunk, (long long)(need * row_bytes));
   float* cur = st->fused ? st->interm[0] : st->interm[chunk & 1];
   float* prev = (!st->fused && chunk > 0) ? st->interm[(chunk - 1) & 1] : nullptr;
   // fine blocks completed by this chunk: block B needs timestream rows

@@ -284,7 +284,9 @@ int ab_stream_reset(ab_stream *st, void *stream);
  * g (global, 0-based) of antenna a is row spec_map[a*map_stride + g] when
  * spec_map != NULL (negative = missing, zero-filled), else row g. Rows for
  * g in [chunk*acclen - 2*cut, (chunk+1)*acclen) are read.  Rows are
- * 2*nchan_raw bytes (4-bit) or nchan_raw/2 bytes (1-bit). */
+ * 2*nchan_raw bytes (4-bit) or nchan_raw/2 bytes (1-bit).  AB_ERR_ARG when
+ * map_stride (with a map) or ant_stride / row bytes (without) is below
+ * (chunk+1)*acclen; map entries must name rows inside the antenna's array. */
 int ab_stream_push(ab_stream *st, const uint8_t *raw, int64_t ant_stride, const int32_t *spec_map,
                    int64_t map_stride, int64_t chunk, void *stream);
 /* The last chunk: as ab_stream_push, then every remaining fine block of the
