@@ -6,7 +6,7 @@
 //  * the streaming chain's per-job accumulation of the same products;
 //  * exact integer coarse correlator on raw 4-bit packets with tensor cores,
 //    flushed into int64: by default mma.sync m16n8k16 with fp16 operands and
-//    fp32 partial sums, exact because the levels (-8..7) are exact in fp16,
+//    fp32 partial sums, exact because the levels (-7..8) are exact in fp16,
 //    products are at most 64 and a CTA's partial sums over at most 4096
 //    samples stay below 2^24; or mma.sync m16n8k32 s8 -> s32
 //    (AB_OPT_COARSE_MMA_BITS = 8).  tcgen05 kind::i8 is not offered for
@@ -290,7 +290,7 @@ __global__ void __launch_bounds__(kCcThreads)
 }
 
 // FP16 form of the same Gram matrix.  The decoded values are integers in
-// [-8, 7], exact in fp16; mma.sync m16n8k16 multiplies them exactly and
+// [-7, 8] (nibble 0x8 is +8), exact in fp16; mma.sync m16n8k16 multiplies them exactly and
 // accumulates in fp32, which stays exact while |sum| < 2^24: a CTA slice of
 // at most 4096 samples sums at most 4096 * 64 = 2^18.  The fp32 partials are
 // converted to int64 exactly and flushed with int64 atomics, as in the int8
