@@ -57,6 +57,7 @@ def unpacker():
 
 
 def ipfb_f32(dat, filt, cut, workers):
+    """cpu_ipfb (src/utils/pfb_cpu_utils.py:90-121) in float32, then the chunk's [cut, -cut) rows raveled."""
     dd = sfft.irfft(dat, axis=1, workers=workers)
     ddft = sfft.rfft(dd.T, axis=1, workers=workers)
     ddft *= filt
@@ -65,6 +66,7 @@ def ipfb_f32(dat, filt, cut, workers):
 
 
 def pfb_f32(ts, win, lblock, ntap, workers):
+    """cpu_pfb (src/utils/pfb_cpu_utils.py:143-172): tap fold, then rfft of each block."""
     nblock = ts.size // lblock - (ntap - 1)
     t = ts[: (nblock + ntap - 1) * lblock].reshape(-1, lblock)
     w = win.reshape(ntap, lblock)
@@ -75,7 +77,8 @@ def pfb_f32(ts, win, lblock, ntap, workers):
 
 
 class CpuChain:
-    """One chunk of the streaming chain on the host (float32)."""
+    """One chunk of the streaming chain on the host (float32), per input as
+    the reference's driver runs it (scripts/xcorr/helper_gpu_stream_clean.py:295-456)."""
 
     def __init__(self, channels_abs, acclen, cut, osamp, q0, q1, thresh=0.45, ntap=4, workers=None):
         self.chan_abs = np.asarray(channels_abs, np.int64)

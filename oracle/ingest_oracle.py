@@ -25,7 +25,8 @@ import numpy as np
 def read_file(path: str):
     """(header tuple (header_bytes, bytes_per_packet, length_channels,
     spectra_per_packet, bit_mode, num_packets), channels, spec_num (int64,
-    internal wrap undone), overflowed, payload (npkt, bytes_per_packet-4))."""
+    internal wrap undone), overflowed, payload (npkt, bytes_per_packet-4)), as
+    Baseband reads a file (src/correlations/baseband_data_classes.py:156-228)."""
     with open(path, "rb") as f:
         blob = f.read()
     hb, bpp, lch, spp, bits, _ = struct.unpack(">6Q", blob[:48])
@@ -49,9 +50,10 @@ def read_file(path: str):
 
 def iterate(paths: Sequence[str], fileidx: int, idxstart: int, acclen: int, nchunks: int):
     """Per chunk (spectrum numbers present, file index, row in that file),
-    rows counted in spectra (packet * spp + j).  Like the reference, a chunk
-    that reaches the last file's last spectrum ends the iteration
-    undelivered."""
+    rows counted in spectra (packet * spp + j), following
+    BasebandFileIterator (src/correlations/baseband_data_classes.py:522-715).
+    Like the reference, a chunk that reaches the last file's last spectrum
+    ends the iteration undelivered."""
     files = []
     ctr = 0
     for p in paths:

@@ -15,6 +15,7 @@ def _c(a, dt):
 
 
 def unpack_4bit(raw2d, rowstart, rowend, channels, nchan):
+    """unpack_4bit_float (src/correlations/unpacking.c:155-205): 2 x (rows, ncols) complex64."""
     raw2d = _c(raw2d, np.uint8)
     ch = _c(channels, np.int64)
     p0 = np.empty((rowend - rowstart, ch.size), np.complex64)
@@ -25,6 +26,7 @@ def unpack_4bit(raw2d, rowstart, rowend, channels, nchan):
 
 
 def unpack_4bit_mt(raw2d, rowstart, rowend, channels, nchan, nthreads):
+    """unpack_4bit (above) split over nthreads host threads (the CPU baseline)."""
     raw2d = _c(raw2d, np.uint8)
     ch = _c(channels, np.int64)
     p0 = np.empty((rowend - rowstart, ch.size), np.complex64)
@@ -35,6 +37,7 @@ def unpack_4bit_mt(raw2d, rowstart, rowend, channels, nchan, nthreads):
 
 
 def unpack_1bit(raw2d, rowstart, rowend, chanstart, chanend, nchan):
+    """unpack_1bit_float (src/correlations/unpacking.c:207-246) over channels [chanstart, chanend)."""
     raw2d = _c(raw2d, np.uint8)
     p0 = np.empty((rowend - rowstart, chanend - chanstart), np.complex64)
     p1 = np.empty_like(p0)
@@ -44,6 +47,7 @@ def unpack_1bit(raw2d, rowstart, rowend, chanstart, chanend, nchan):
 
 
 def sortpols(raw2d, nchan, bit_depth, rowstart, rowend, chanstart, chanend):
+    """sortpols (src/correlations/unpacking.c:248-368): the pols' bytes, undecoded."""
     raw2d = _c(raw2d, np.uint8)
     nc = (chanend - chanstart) if bit_depth == 4 else int(np.ceil((chanend - chanstart) / 4))
     p0 = np.empty((rowend - rowstart, nc), np.uint8)
@@ -54,6 +58,7 @@ def sortpols(raw2d, nchan, bit_depth, rowstart, rowend, chanstart, chanend):
 
 
 def hist(raw2d, rowstart, rowend, nchan, bit_depth, mode):
+    """hist_4bit / hist_1bit (src/correlations/unpacking.c:7-153): (2**bit_depth, nchan) uint64 counts."""
     raw2d = _c(raw2d, np.uint8)
     nbins = 2 ** bit_depth - 1
     h = np.empty((nbins + 1, nchan), np.uint64)
@@ -63,6 +68,7 @@ def hist(raw2d, rowstart, rowend, nchan, bit_depth, mode):
 
 
 def avg_xcorr_4bit_sums(d0, d1, nrows):
+    """avg_xcorr_4bit (src/correlations/correlations_cpu.c:128-186) as exact int64 sums, not yet / rows."""
     d0, d1 = _c(d0, np.uint8), _c(d1, np.uint8)
     re = np.empty(d0.shape[1], np.int64)
     im = np.empty_like(re)
@@ -71,6 +77,8 @@ def avg_xcorr_4bit_sums(d0, d1, nrows):
 
 
 def avg_xcorr_4bit_2ant_sums(d0, d1, s0, s1, off0, off1):
+    """avg_xcorr_4bit_2ant (src/correlations/correlations_cpu.c:188-271): int64 sums over the
+    intersected spectrum numbers, and their count."""
     d0, d1 = _c(d0, np.uint8), _c(d1, np.uint8)
     s0, s1 = _c(s0, np.int64), _c(s1, np.int64)
     re = np.empty(d0.shape[1], np.int64)
@@ -81,6 +89,7 @@ def avg_xcorr_4bit_2ant_sums(d0, d1, s0, s1, off0, off1):
 
 
 def avg_xcorr_1bit_sums(d0, d1, nchan, nspec):
+    """avg_xcorr_1bit (src/correlations/correlations_cpu.c:273-433) as exact int64 sums."""
     d0, d1 = _c(d0, np.uint8), _c(d1, np.uint8)
     re = np.empty(nchan, np.int64)
     im = np.empty_like(re)
@@ -90,6 +99,8 @@ def avg_xcorr_1bit_sums(d0, d1, nchan, nspec):
 
 
 def vanvleck_2ant_sums(d0, d1, nchan, s0, s1, off0, off1):
+    """avg_xcorr_1bit_vanvleck_2ant (src/correlations/correlations_cpu.c:527-638): the four
+    int64 partial sums per channel over the intersected spectra, and their count."""
     d0, d1 = _c(d0, np.uint8), _c(d1, np.uint8)
     s0, s1 = _c(s0, np.int64), _c(s1, np.int64)
     out = [np.empty(nchan, np.int64) for _ in range(4)]
@@ -100,6 +111,8 @@ def vanvleck_2ant_sums(d0, d1, nchan, s0, s1, off0, off1):
 
 
 def vanvleck_sums(d0, d1, nchan, nrows):
+    """avg_xcorr_1bit_vanvleck (src/correlations/correlations_cpu.c:435-525): the four int64
+    partial sums per channel."""
     d0, d1 = _c(d0, np.uint8), _c(d1, np.uint8)
     out = [np.empty(nchan, np.int64) for _ in range(4)]
     c_oracle().or_avg_xcorr_1bit_vanvleck(d0.ctypes.data, d1.ctypes.data, *[o.ctypes.data for o in out], nchan, nrows,
@@ -108,7 +121,8 @@ def vanvleck_sums(d0, d1, nchan, nrows):
 
 
 def xcorr_all_ant_4bit(raw3d, rowstart, rowend, channels, nchan, nthreads=1):
-    """Exact (M, M, ncols) int64 re/im sums of x_i conj(x_j) over rows."""
+    """Exact (M, M, ncols) int64 re/im sums of x_i conj(x_j) over rows: the all-baseline form of
+    avg_xcorr_4bit (src/correlations/correlations_cpu.c:128-186) for every input pair."""
     raw3d = _c(raw3d, np.uint8)
     ch = _c(channels, np.int64)
     nant, nspec = raw3d.shape[0], raw3d.shape[1]

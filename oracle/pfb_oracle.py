@@ -71,7 +71,9 @@ def calculate_filter(matft: np.ndarray, thresh: float) -> np.ndarray:
 
 
 def ipfb(dat: np.ndarray, filt: np.ndarray) -> np.ndarray:
-    """Inverse PFB of (nslice, nchan) spectra -> (nslice, lblock) timestream.
+    """Inverse PFB of (nslice, nchan) spectra -> (nslice, lblock) timestream,
+    cupy_ipfb (src/utils/pfb_gpu_utils.py:56-91): irfft along channels, rfft
+    along time, times filt, irfft along time.
 
     Returns the transposed view like the reference (F-ordered result)."""
     dd = np.fft.irfft(dat, axis=1)
@@ -112,7 +114,8 @@ def decode_4bit(b: np.ndarray):
 
 
 def unpack_4bit_np(raw2d: np.ndarray, rowstart: int, rowend: int, channels) -> tuple:
-    """Pure NumPy 4-bit unpack of (nspec, 2*nchan) bytes -> 2 x (rows, ncols) complex128."""
+    """Pure NumPy 4-bit unpack of (nspec, 2*nchan) bytes -> 2 x (rows, ncols) complex128,
+    the decode of unpack_4bit_float (src/correlations/unpacking.c:155-205)."""
     ch = np.asarray(channels, dtype=np.int64)
     r = raw2d[rowstart:rowend]
     out = []
