@@ -12,7 +12,9 @@ def make_continuous_gpu(spec, chan_specnum, start_specnum, channels, nspec, ncha
     """Scatter the rows of `spec` to (specnum - start_specnum) % nspec and its
     columns to the absolute channel numbers `channels` of a zero
     (nspec, nchans) complex64 grid.  When nothing is missing and all nchans
-    channels are present, `spec` itself is returned (or copied into `out`)."""
+    channels are present, `spec` itself is returned (or copied into `out`).
+
+    Reference: src/correlations/baseband_data_classes.py:48-73."""
     s = device_array(spec, torch.complex64, "spec")
     sn = host_int64(chan_specnum, "chan_specnum")
     ch = host_int64(channels, "channels")

@@ -45,7 +45,9 @@ def _pairs4(d0, d1, r0, r1, nmatch, ncol):
 def avg_xcorr_4bit(data0, data1, specnums):
     """Time-averaged d0 * conj(d1) per channel of sortpols'd 4-bit data
     (rows, ncol); the first len(specnums) rows are used.  complex64 (ncol,),
-    or nan for an empty block."""
+    or nan for an empty block.
+
+    Reference: src/correlations/correlations.py:296-327 (C correlations_cpu.c:128-186)."""
     assert data0.shape[1] == data1.shape[1]
     assert data0.shape[0] == data1.shape[0]
     rowcount = len(specnums)
@@ -61,7 +63,9 @@ def avg_xcorr_4bit(data0, data1, specnums):
 
 def avg_xcorr_4bit_2ant(data0, data1, specnum0, specnum1, start_idx0, start_idx1):
     """Cross-correlation of two antennas over the spectra present in both
-    (specnum - start_idx equal).  complex64 (ncol,) / rowcount, or nan."""
+    (specnum - start_idx equal).  complex64 (ncol,) / rowcount, or nan.
+
+    Reference: src/correlations/correlations.py:330-383 (C correlations_cpu.c:188-271)."""
     assert data0.shape[1] == data1.shape[1]
     if len(specnum0) == 0 or len(specnum1) == 0:
         return np.nan
@@ -90,7 +94,9 @@ def _pairs1(data0, data1, r0, r1, nmatch, nchannels):
 
 
 def avg_xcorr_1bit(data0, data1, specnums, nchannels):
-    """1-bit (sortpols layout) time-averaged d0 * conj(d1), complex64 (nchannels,)."""
+    """1-bit (sortpols layout) time-averaged d0 * conj(d1), complex64 (nchannels,).
+
+    Reference: src/correlations/correlations.py:386-408 (C correlations_cpu.c:273-433)."""
     assert data0.shape[0] == data1.shape[0]
     assert data0.shape[1] == data1.shape[1]
     rowcount = len(specnums)
@@ -102,7 +108,9 @@ def avg_xcorr_1bit(data0, data1, specnums, nchannels):
 
 
 def avg_xcorr_1bit_vanvleck(data0, data1, specnums, nchannels):
-    """Van Vleck partial sums [R0, R1, IM0, IM1] (float32, / rowcount)."""
+    """Van Vleck partial sums [R0, R1, IM0, IM1] (float32, / rowcount).
+
+    Reference: src/correlations/correlations.py:411-443 (C correlations_cpu.c:435-525)."""
     assert data0.shape[0] == data1.shape[0]
     assert data0.shape[1] == data1.shape[1]
     rowcount = len(specnums)
@@ -113,7 +121,9 @@ def avg_xcorr_1bit_vanvleck(data0, data1, specnums, nchannels):
 
 
 def avg_xcorr_1bit_vanvleck_2ant(data0, data1, nchannels, specnum0, specnum1, idxstart0, idxstart1):
-    """Two-antenna Van Vleck partial sums ([R0, R1, IM0, IM1] float32, rowcount)."""
+    """Two-antenna Van Vleck partial sums ([R0, R1, IM0, IM1] float32, rowcount).
+
+    Reference: src/correlations/correlations.py:446-489 (C correlations_cpu.c:527-638)."""
     assert data0.shape[0] == data1.shape[0]
     assert data0.shape[1] == data1.shape[1]
     nanv = [np.full(nchannels, np.nan, np.float32) for _ in range(4)]
@@ -141,7 +151,9 @@ def avg_xcorr_all_ant_gpu(x, nant: int, npol: int, ntime: int, nfreq: int, split
 
     x: complex64 F-ordered (nant*npol, ntime, nfreq) device array (a torch
     tensor with those strides, or any contiguous buffer of that many
-    elements read in F order).  Returns F-ordered (M, M, nfreq) complex64."""
+    elements read in F order).  Returns F-ordered (M, M, nfreq) complex64.
+
+    Reference: src/correlations/correlations_gpu.py:95-121 (cuBLAS, cgemm_batch.cu:8-53)."""
     M = int(nant) * int(npol)
     K = int(ntime)
     if K % split != 0:
@@ -169,7 +181,9 @@ def avg_xcorr_4bit_float_gpu(data0, data1, specnum0, specnum1):
 
     Same specnum array (same antenna): mean of data0 * conj(data1) over the
     first len(specnum0) rows, returned with that count, as the reference.
-    Different antennas: over the rows whose specnums match."""
+    Different antennas: over the rows whose specnums match.
+
+    Reference: src/correlations/correlations.py:180-207."""
     d0 = device_array(data0, torch.complex64, "data0")
     d1 = device_array(data1, torch.complex64, "data1")
     same = specnum0 is specnum1 or (hasattr(specnum0, "__array_interface__") and hasattr(specnum1, "__array_interface__")
@@ -198,7 +212,9 @@ def xcorr_coarse_4bit(raw, rowstart, rowend, channels, length_channels, chunk=No
     rows [rowstart, rowend) (or per-antenna row indices `rows` (nant, nrows)),
     channels: channel indices; chunk: spectra per average (None = all).
     Returns complex64 (nchunks, M, M, ncols) averages (average=True, /rows per
-    chunk) or the exact int64 (re, im) sums.  M = 2*nant, input 2a+p."""
+    chunk) or the exact int64 (re, im) sums.  M = 2*nant, input 2a+p.
+
+    Reference: no single counterpart: every input pair of avg_xcorr_4bit (correlations_cpu.c:128-186)."""
     r = device_array(raw, torch.uint8, "raw")
     if r.dim() == 2:
         r = r.unsqueeze(0)

@@ -55,6 +55,7 @@ class BasebandHeader:
 
 
 def read_header(path: str) -> BasebandHeader:
+    """Reference: src/correlations/baseband_data_classes.py:100-185 (Baseband header fields)."""
     with open(path, "rb") as f:
         head = f.read(48)
         if len(head) < 48:
@@ -86,7 +87,9 @@ def read_header(path: str) -> BasebandHeader:
 
 
 def get_header(path: str, verbose: bool = False) -> Dict:
-    """The reference's get_header dictionary (header fields only)."""
+    """The reference's get_header dictionary (header fields only).
+
+    Reference: src/correlations/baseband_data_classes.py:344-365."""
     h = read_header(path)
     if verbose:
         print(h)
@@ -109,7 +112,9 @@ def fix_wraps(spec_num: np.ndarray) -> Tuple[np.ndarray, bool]:
 def read_packets(path: str, readlen=-1, header: Optional[BasebandHeader] = None):
     """(header, pinned uint8 (npkt, bytes_per_packet) packets, wrap-fixed
     int64 spectrum numbers, overflowed).  readlen as the reference: >= 1
-    packets, (0, 1) a fraction, 0 none, -1 all."""
+    packets, (0, 1) a fraction, 0 none, -1 all.
+
+    Reference: src/correlations/baseband_data_classes.py:156-228 (packets, spectrum numbers, wrap fix)."""
     h = header or read_header(path)
     if readlen >= 1:
         npk = min(int(readlen), h.num_packets)
@@ -199,7 +204,10 @@ def plan_antenna(paths: Sequence[str], fileidx: int, idxstart: int, nspec: int) 
 def ingest(files: Sequence[Sequence[str]], idxs: Sequence[int], nspec: int, device=None, fileidx: int = 0):
     """Device (raw, spec_map, antennas): raw (nant, rows, row_bytes) uint8 with
     each antenna's files' spectra back to back, spec_map (nant, nspec) int32
-    (row of spectrum start_a + g, -1 when missing) for the streaming chain."""
+    (row of spectrum start_a + g, -1 when missing) for the streaming chain.
+
+    Reference: the per-chunk host walk of BasebandFileIterator.__next__
+    (src/correlations/baseband_data_classes.py:614-715)."""
     if len(files) != len(idxs) or not files:
         raise ValueError("one file list and one start index per antenna")
     dev = torch.device(device if device is not None else "cuda")

@@ -75,7 +75,9 @@ def missing_fraction(present, acclen: int, nblock: int, osamp: int, ntap: int = 
 def chunk_presence(spec_map, nant: int, nchunks: int, acclen: int) -> np.ndarray:
     """(nant, nchunks) spectra present per chunk from a device or host
     spectrum map (row g of antenna a present when spec_map[a, g] >= 0);
-    None means every spectrum is present."""
+    None means every spectrum is present.
+
+    Reference: the per-chunk counts MissingDataTracker keeps (scripts/xcorr/helper_gpu_stream_clean.py:200-226)."""
     if spec_map is None:
         return np.full((nant, nchunks), acclen, dtype=np.int64)
     m = spec_map[:, : nchunks * acclen]
@@ -104,13 +106,17 @@ def save_xcorr_npz(path: str, vis, missing: np.ndarray, chans: Sequence[int]) ->
 
 
 def load_xcorr_npz(path: str) -> Tuple[np.ma.MaskedArray, np.ndarray, np.ndarray]:
-    """(vis as a masked array, missing_fraction, chans) from a saved product."""
+    """(vis as a masked array, missing_fraction, chans) from a saved product.
+
+    Reference: the product of scripts/xcorr/xcorr_gpu_cpu.py:113-118."""
     with np.load(path) as f:
         return np.ma.MaskedArray(f["data"], mask=f["mask"]), f["missing_fraction"], f["chans"]
 
 
 def write_run(outdir: str, init_t, acclen: int, osamp: int, nchunks: int, chanstart: int, chanend: int, vis,
               missing: np.ndarray, chans: Sequence[int], name: Optional[str] = None) -> str:
-    """Save a run under outdir with the reference's file name; returns the path."""
+    """Save a run under outdir with the reference's file name; returns the path.
+
+    Reference: scripts/xcorr/xcorr_gpu_cpu.py:113-118."""
     path = os.path.join(outdir, name or xcorr_npz_name(init_t, acclen, osamp, nchunks, chanstart, chanend))
     return save_xcorr_npz(path, vis, missing, chans)

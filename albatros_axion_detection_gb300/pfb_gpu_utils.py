@@ -18,7 +18,9 @@ from ._arrays import device_array, to_device
 
 
 def sinc_hamming(ntap, lblock):
-    """Hamming window times sinc over ntap blocks, float64 on the host."""
+    """Hamming window times sinc over ntap blocks, float64 on the host.
+
+    Reference: src/utils/pfb_utils.py:4-7."""
     n = ntap * lblock
     w = np.arange(0, n) - n / 2
     return np.hamming(n) * np.sinc(w / lblock)
@@ -26,7 +28,9 @@ def sinc_hamming(ntap, lblock):
 
 def get_matft(nslice, nchan=2049, ntap=4):
     """Spectrum of the zero-padded window matrix, (lblock, nslice//2+1) complex64,
-    evaluated directly in FP64 on the GPU (4 nonzero taps per column)."""
+    evaluated directly in FP64 on the GPU (4 nonzero taps per column).
+
+    Reference: src/utils/pfb_gpu_utils.py:123-137."""
     nslice, nchan, ntap = int(nslice), int(nchan), int(ntap)
     lblock = 2 * (nchan - 1)
     out = torch.empty((lblock, nslice // 2 + 1), dtype=torch.complex64, device="cuda")
@@ -35,7 +39,9 @@ def get_matft(nslice, nchan=2049, ntap=4):
 
 
 def calculate_filter(matft, thresh):
-    """Wiener-regularised inverse 1/conj(m) * |m|^2/(t^2+|m|^2) * (1+t^2), in FP64."""
+    """Wiener-regularised inverse 1/conj(m) * |m|^2/(t^2+|m|^2) * (1+t^2), in FP64.
+
+    Reference: src/utils/pfb_gpu_utils.py:29-36."""
     m = device_array(matft, torch.complex64, "matft").contiguous()
     out = torch.empty_like(m)
     _lib.call("ab_calculate_filter", m.data_ptr(), out.data_ptr(), m.numel(), float(thresh), _lib.stream_ptr(m))
@@ -43,7 +49,9 @@ def calculate_filter(matft, thresh):
 
 
 def build_filter(nslice, thresh, nchan=2049, ntap=4):
-    """calculate_filter(get_matft(nslice, nchan, ntap), thresh) in one FP64 pass."""
+    """calculate_filter(get_matft(nslice, nchan, ntap), thresh) in one FP64 pass.
+
+    Reference: scripts/xcorr/helper_gpu_stream_clean.py:281-292 (get_matft then calculate_filter)."""
     lblock = 2 * (int(nchan) - 1)
     out = torch.empty((lblock, int(nslice) // 2 + 1), dtype=torch.complex64, device="cuda")
     _lib.call("ab_build_filter", _lib.ctx(), out.data_ptr(), int(nslice), int(nchan), int(ntap), float(thresh),
@@ -56,7 +64,9 @@ def cupy_ipfb(dat, filt):
     (lblock, nslice//2+1) -> (nslice, lblock) float32.
 
     Like the reference, the result is the transpose of a C-ordered
-    (lblock, nslice) array (an F-ordered view)."""
+    (lblock, nslice) array (an F-ordered view).
+
+    Reference: src/utils/pfb_gpu_utils.py:56-91."""
     d = device_array(dat, torch.complex64, "dat").contiguous()
     f = device_array(filt, torch.complex64, "filt").contiguous()
     if d.dim() != 2:
@@ -84,7 +94,9 @@ def _pfb_args(timestream, win, nchan, ntap):
 def cupy_pfb(timestream, win, out=None, nchan=2049, ntap=4):
     """Forward PFB: tap-fold the timestream with `win` and real-FFT each block of
     lblock = 2*(nchan-1) samples -> (nblock, nchan) complex64.  As in the
-    reference, `out` is only checked for shape."""
+    reference, `out` is only checked for shape.
+
+    Reference: src/utils/pfb_gpu_utils.py:105-121."""
     ts, w, lblock, nblock = _pfb_args(timestream, win, nchan, ntap)
     if out is not None:
         assert tuple(out.shape) == (nblock, nchan)
@@ -97,7 +109,10 @@ def cupy_pfb(timestream, win, out=None, nchan=2049, ntap=4):
 
 def cupy_pfb_band(timestream, win, q0, q1, nchan=2049, ntap=4):
     """cupy_pfb(...)[:, q0:q1] without forming the other bins (q0, q1 multiples
-    of osamp = lblock/4096)."""
+    of osamp = lblock/4096).
+
+    Reference: src/utils/pfb_gpu_utils.py:105-121 with the band slice of
+    scripts/xcorr/helper_gpu_stream_clean.py:342-346."""
     ts, w, lblock, nblock = _pfb_args(timestream, win, nchan, ntap)
     res = torch.empty((max(nblock, 0), int(q1) - int(q0)), dtype=torch.complex64, device=ts.device)
     if nblock > 0:

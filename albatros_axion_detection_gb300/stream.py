@@ -40,6 +40,8 @@ class ProcessingConfig:
 
 
 class JobChunkPlanner:
+    """Reference: scripts/xcorr/helper_gpu_stream_clean.py:229-263."""
+
     @staticmethod
     def plan_chunks(nchunks: int, lchunk: int, nblock: int, lblock: int, ntap: int) -> List[Tuple[int, Optional[int]]]:
         """Job -> chunk ranges: a job needs (nblock + ntap - 1) * lblock samples,
@@ -64,7 +66,9 @@ class JobChunkPlanner:
 
 def band_edges(channels, chanstart: int, chanend: int, osamp: int) -> Tuple[int, int]:
     """Fine band [channels[chanstart]*osamp, channels[chanend]*osamp); when
-    chanend is one past the last recorded channel, (channels[-1]+1)*osamp."""
+    chanend is one past the last recorded channel, (channels[-1]+1)*osamp.
+
+    Reference: scripts/xcorr/helper_gpu_stream_clean.py:342-343."""
     ch = host_int64(channels)
     q0 = int(ch[chanstart]) * osamp
     q1 = int(ch[chanend]) * osamp if chanend < ch.size else (int(ch[chanend - 1]) + 1) * osamp
@@ -72,7 +76,9 @@ def band_edges(channels, chanstart: int, chanend: int, osamp: int) -> Tuple[int,
 
 
 class StreamCorrelator:
-    """Device state of one streaming run; push chunks in order, read vis."""
+    """Device state of one streaming run; push chunks in order, read vis.
+
+    Reference: scripts/xcorr/helper_gpu_stream_clean.py:295-456 (the per-chunk loop and its overlap state)."""
 
     def __init__(self, nant: int, channels, chanstart: int, chanend: int, acclen: int, nchunks: int, nblock: int,
                  osamp: int, cut: int = 10, filt_thresh: float = 0.45, ntap: int = 4, nchan_raw: Optional[int] = None,

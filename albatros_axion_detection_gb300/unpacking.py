@@ -28,7 +28,9 @@ def unpack_4bit(data, rowstart, rowend, channels, length_channels, dtype=torch.c
     byte then pol1 byte per channel; real = high nibble, imag = low nibble,
     nibble v > 8 decodes to v - 16). channels: channel INDICES (host).
     dtype=torch.int8 returns the same levels as int8 complex instead,
-    (rows, len(channels), 2) with (re, im) last."""
+    (rows, len(channels), 2) with (re, im) last.
+
+    Reference: src/correlations/unpacking.py:193-245 (GPU :140-155; C unpacking.c:155-205)."""
     d = device_array(data, torch.uint8, "data")
     rowstart, rowend, length_channels = int(rowstart), int(rowend), int(length_channels)
     ch = host_int64(channels, "channels")
@@ -108,7 +110,9 @@ def sortpols(data, length_channels, bit_mode, rowstart, rowend, chanstart, chane
     """Separate the pols of packed data without decoding (device uint8 out).
 
     4-bit: (rows, chanend-chanstart) bytes per pol. 1-bit: four channels per
-    byte, (rows, ceil((chanend-chanstart)/4)) bytes per pol."""
+    byte, (rows, ceil((chanend-chanstart)/4)) bytes per pol.
+
+    Reference: src/correlations/unpacking.py:305-377 (C unpacking.c:248-408)."""
     d = device_array(data, torch.uint8, "data")
     length_channels, rowstart, rowend = int(length_channels), int(rowstart), int(rowend)
     if chanend is None:
@@ -141,7 +145,9 @@ def hist(data, rowstart, rowend, length_channels, bit_depth, mode):
     hist[v, c] counts the real and imaginary levels of channel c in rows
     [rowstart, rowend) equal to v (the raw nibble for 4-bit data, the bit for
     1-bit data), over pol0 (mode 0), pol1 (mode 1) or both (mode -1).  The
-    reference asserts on a bad bit_depth or mode; here they raise ValueError."""
+    reference asserts on a bad bit_depth or mode; here they raise ValueError.
+
+    Reference: src/correlations/unpacking.py:82-138 (C unpacking.c:7-153)."""
     d = device_array(data, torch.uint8, "data")
     rowstart, rowend, length_channels = int(rowstart), int(rowend), int(length_channels)
     if bit_depth not in (1, 4):
