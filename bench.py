@@ -410,9 +410,9 @@ def _line(metric, value, unit, ms, args, workload, extra):
 
 
 def run_coarse(args, nant, nchan, nspec, chunk, workload):
-    """Exact all-baseline coarse correlation of 4-bit packets (int8 tensor
-    cores, int64 sums): configurations 'plain unpack + xcorr' and 'many-antenna
-    coarse correlator'."""
+    """Exact all-baseline coarse correlation of 4-bit packets (tensor-core MMA
+    on fp16 operands, or int8 with --mma-bits 8; int64 sums): configurations
+    'plain unpack + xcorr' and 'many-antenna coarse correlator'."""
     import torch
     from albatros_axion_detection_gb300 import correlations
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -450,12 +450,14 @@ def run_coarse(args, nant, nchan, nspec, chunk, workload):
     achieved = bytes_in / (ms / 1e3) / 1e9
     M = 2 * nant
     macs = spectra // nant * nchan * (M * (M + 1) // 2) * 4  # real int MACs, unique pairs
-    _line("input spectra/s, exact all-baseline coarse correlation (int8 tensor cores, int64 sums)",
+    _line("input spectra/s, exact all-baseline coarse correlation (tensor cores, int64 sums)",
           spectra / (ms / 1e3), "spectra/s", ms, args, workload,
           {"dtype": ("int8" if args.mma_bits == 8 else "fp16 (exact small integers)") + " -> int64", "clocks": clk,
            "e2e": {"value": spectra / (ms_e2e / 1e3), "unit": "spectra/s", "ms_per_step": ms_e2e,
                    "h2d_bytes_per_step": int(bytes_in), "d2h_bytes_per_step": int(out_re.numel() * 16)},
-           "roofline": {"bound": "hbm", "kernel": "coarse_xcorr_kernel", "achieved": achieved, "peak": peak,
+           "roofline": {"bound": "hbm",
+                        "kernel": "coarse_xcorr_kernel" if args.mma_bits == 8 else "coarse_xcorr_f16_kernel",
+                        "achieved": achieved, "peak": peak,
                         "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
                         "int_macs_per_s_unique_pairs": macs / (ms / 1e3)},
            "gpu_launches": None})
