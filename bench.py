@@ -556,10 +556,11 @@ def main():
     ap.add_argument("--lanes", type=int, default=4, help="uneven-batch: concurrent CUDA streams")
     ap.add_argument("--time-filter", default="default", choices=["default", "iir", "fir", "fft"],
                     help="stream: IPFB time stage form (default: the library's choice)")
-    ap.add_argument("--row-tile", type=int, default=0, help="stream: FIR rows per thread (16 or 32)")
-    ap.add_argument("--row-ffts", type=int, default=0, help="stream: spectra per row-stage CTA (2 or 4)")
+    ap.add_argument("--row-tile", type=int, default=0, help="stream: IIR / FIR row tile (16 or 32)")
+    ap.add_argument("--row-ffts", type=int, default=0, help="stream: spectra per row-stage CTA (8, 4 or 2)")
     ap.add_argument("--row-prefetch", type=int, default=-1,
-                    help="stream: row stage 0 = one CTA per tile, 1 = persistent prefetching, 2 (default) = + shared twiddles")
+                    help="stream: row stage 0 = one CTA per tile, 1 = persistent prefetching, "
+                         "2 (default) = + shared twiddles")
     ap.add_argument("--check", action="store_true", help="uneven-batch: job-0 error of every file vs the FP64 oracle")
     ap.add_argument("--mma-bits", type=int, default=0, help="coarse workloads: tensor-core operand bits (16 or 8)")
     args = ap.parse_args()
