@@ -611,16 +611,17 @@ static bool split_lblock(int64_t L, int* P, int* O) {
 
 static int pfb_common(ab_ctx* ctx, const float* ts, int64_t nsamp, const float* win, int64_t nchan, int64_t ntap,
                       int64_t q0, int64_t q1, bool band, float* out, void* stream) {
-  AB_CHECK_ARG(ctx && ts && win && out, "ab_pfb: NULL pointer");
-  AB_CHECK_ARG(nchan >= 2 && ntap >= 1, "ab_pfb: bad nchan/ntap");
+  const char* name = band ? "ab_pfb_band" : "ab_pfb";
+  AB_CHECK_ARG(ctx && ts && win && out, "%s: NULL pointer", name);
+  AB_CHECK_ARG(nchan >= 2 && ntap >= 1, "%s: bad nchan/ntap", name);
   const int64_t L = 2 * (nchan - 1);
   int P, O;
   if (!split_lblock(L, &P, &O)) {
-    set_error("ab_pfb: lblock %lld must be a power of two in [64, 262144]", (long long)L);
+    set_error("%s: lblock %lld must be a power of two in [64, 262144]", name, (long long)L);
     return AB_ERR_UNSUPPORTED;
   }
   int64_t nblock = nsamp / L - (ntap - 1);
-  AB_CHECK_ARG(nblock >= 0, "ab_pfb: timestream shorter than ntap blocks");
+  AB_CHECK_ARG(nblock >= 0, "%s: timestream shorter than ntap blocks", name);
   if (nblock == 0) return AB_OK;
   int u0 = -1, u1 = -1;
   if (band) {

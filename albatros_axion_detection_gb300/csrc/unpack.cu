@@ -283,7 +283,8 @@ extern "C" int ab_unpack_4bit_i8(const uint8_t* data, int8_t* pol0, int8_t* pol1
 extern "C" int ab_unpack_1bit_i8(const uint8_t* data, int8_t* pol0, int8_t* pol1, int64_t rowstart, int64_t rowend,
                                  const int64_t* cols, int64_t ncols_bytes, int64_t nchan, void* stream) {
   AB_CHECK_ARG(data && pol0 && pol1 && cols, "ab_unpack_1bit_i8: NULL pointer");
-  AB_CHECK_ARG(rowstart >= 0 && rowend >= rowstart && ncols_bytes >= 0 && nchan > 1, "ab_unpack_1bit_i8: bad sizes");
+  AB_CHECK_ARG(rowstart >= 0 && rowend >= rowstart && ncols_bytes >= 0 && nchan > 1 && nchan % 2 == 0,
+               "ab_unpack_1bit_i8: bad sizes (1-bit rows hold an even channel count)");
   AB_CHECK_ARG(((uintptr_t)pol0 & 3) == 0 && ((uintptr_t)pol1 & 3) == 0, "ab_unpack_1bit_i8: outputs must be 4-byte aligned");
   const int64_t total = (rowend - rowstart) * ncols_bytes;
   if (total == 0) return AB_OK;
@@ -296,7 +297,8 @@ extern "C" int ab_unpack_1bit_i8(const uint8_t* data, int8_t* pol0, int8_t* pol1
 extern "C" int ab_unpack_1bit(const uint8_t* data, float* pol0, float* pol1, int64_t rowstart, int64_t rowend,
                               const int64_t* cols, int64_t ncols_bytes, int64_t nchan, void* stream) {
   AB_CHECK_ARG(data && pol0 && pol1 && cols, "ab_unpack_1bit: NULL pointer");
-  AB_CHECK_ARG(rowstart >= 0 && rowend >= rowstart && ncols_bytes >= 0 && nchan > 1, "ab_unpack_1bit: bad sizes");
+  AB_CHECK_ARG(rowstart >= 0 && rowend >= rowstart && ncols_bytes >= 0 && nchan > 1 && nchan % 2 == 0,
+               "ab_unpack_1bit: bad sizes (1-bit rows hold an even channel count)");
   AB_CHECK_ARG(((uintptr_t)pol0 & 15) == 0 && ((uintptr_t)pol1 & 15) == 0, "ab_unpack_1bit: outputs must be 16-byte aligned");
   int64_t nrows = rowend - rowstart;
   int64_t total = nrows * ncols_bytes;

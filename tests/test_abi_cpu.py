@@ -81,3 +81,53 @@ def test_new_entry_points_check_arguments_on_host():
     assert call("ab_spec_map_init", None, 8, None) == -1
     assert call("ab_spec_map_finish", None, 8, None) == -1
     assert b"ab_" in lib.ab_last_error()
+
+
+def test_every_entry_point_rejects_bad_arguments_on_host():
+    """Each compute entry point returns AB_ERR_ARG (-1) for NULL pointers or
+    impossible sizes before any CUDA call, so these run without a GPU; NULL
+    objects are harmless to destroy and read back as -1 / NULL."""
+    import ctypes
+    from albatros_axion_detection_gb300 import _lib
+    lib = _lib.load()
+    bad = [
+        ("ab_unpack_1bit", None, None, None, 0, 10, None, 4, 8, None),
+        ("ab_unpack_1bit", 16, 16, 16, 0, 10, 16, 4, 7, None),               # odd 1-bit channel count
+        ("ab_unpack_4bit_i8", None, None, None, 0, 10, None, 4, 8, None),
+        ("ab_unpack_1bit_i8", 16, 16, 16, 0, 10, 16, 4, 7, None),
+        ("ab_unpack_4bit_range", 16, 16, 16, 0, 10, 1, 4, 8, None),          # range not 4-aligned
+        ("ab_unpack_4bit", 16, 16, 16, 5, 2, 16, 4, 8, None),                # rowend < rowstart
+        ("ab_make_continuous", 16, 4, 2, 16, 0, 16, 0, 8, 16, None),         # nspec 0
+        ("ab_calculate_filter", None, None, 10, 0.45, None),
+        ("ab_get_matft", None, 16, 64, 2049, 4, None),
+        ("ab_build_filter", None, 16, 64, 2049, 4, 0.45, None),
+        ("ab_ipfb", None, 16, 16, 16, 64, 2049, None),
+        ("ab_pfb", None, 16, 4096 * 8, 16, 2049, 4, 16, None),
+        ("ab_pfb_band", None, 16, 4096 * 8, 16, 2049, 4, 0, 64, 16, None),
+        ("ab_avg_xcorr_all_ant", None, 2, 2, 10, 4, 16, None),
+        ("ab_avg_xcorr_all_ant", 16, 0, 2, 10, 4, 16, None),                 # no antennas
+        ("ab_xcorr_coarse_4bit", None, 16, 100, 2, 100, 8, 0, 10, None, 16, 4, 0, 16, 16, None),
+        ("ab_xcorr_coarse_4bit_noalloc", 16, 100, 2, 100, 8, 90, 20, None, 16, 4, 0, 16, 16, None),  # rows past nspec
+        ("ab_xcorr_coarse_4bit_noalloc", 16, 100, 40, 100, 8, 0, 20, None, 16, 4, 0, 16, 16, None),  # 40 antennas
+        ("ab_avg_xcorr_4bit_pairs", None, 16, 16, 16, 4, 4, 16, 16, None),
+        ("ab_avg_xcorr_1bit_pairs", None, 16, 16, 16, 4, 4, 8, 16, None),
+        ("ab_stream_create", None, 2, 64, 4, 16, 16, 64, 32768, 80, 64, 4, 0.45, 512, 2, 0, 4096,
+         ctypes.byref(ctypes.c_void_p())),
+        ("ab_stream_push", None, 16, 100, None, 0, 0, None),
+        ("ab_stream_push_final", None, 16, 100, None, 0, 0, None),
+        ("ab_stream_reset", None, None),
+        ("ab_stream_profile", None, 1),
+        ("ab_stream_stage_times", None, 16, 16),
+        ("ab_stream_time_filter", None, 16, 16),
+        ("ab_stream_set_workspace", None, 16, 100),
+        ("ab_ctx_set_option", None, 3, 8),
+        ("ab_ctx_set_time_filter", None, 0, 16),
+        ("ab_ctx_set_fft_plan", None, 16, None, 0),
+    ]
+    for name, *args in bad:
+        assert getattr(lib, name)(*args) == -1, (name, args, lib.ab_last_error())
+        assert lib.ab_last_error().startswith(name.encode()[:9]), (name, lib.ab_last_error())
+    for name in ("ab_stream_kernel_launches", "ab_stream_fir_taps", "ab_stream_workspace_bytes"):
+        assert getattr(lib, name)(None) == -1
+    assert lib.ab_stream_vis(None) is None
+    assert lib.ab_stream_destroy(None) == 0 and lib.ab_ctx_destroy(None) == 0
