@@ -112,7 +112,7 @@ def test_fold_bookkeeping_random_geometries(U, D):
     rng = np.random.default_rng(U * 10 + D)
     for _ in range(60):
         O = int(rng.choice([4, 8, 16, 32, 64]))
-        acclen = int(rng.integers(4 * O // 2, 40000))
+        acclen = int(rng.integers(NTAP * O, 40000))  # ab_stream_create needs acclen >= ntap * osamp
         nchunks = int(rng.integers(1, 5))
         nblock = int(rng.integers(1, 600))
         nb_stream = max(nchunks * acclen // O - (NTAP - 1), 1)
