@@ -131,3 +131,23 @@ def test_every_entry_point_rejects_bad_arguments_on_host():
         assert getattr(lib, name)(None) == -1
     assert lib.ab_stream_vis(None) is None
     assert lib.ab_stream_destroy(None) == 0 and lib.ab_ctx_destroy(None) == 0
+
+
+def test_integration_guide_argtypes_match_the_bindings():
+    """The argtypes lists shown in the binding guide agree with the
+    package's own ctypes signatures (same count, same C type sizes)."""
+    import ctypes
+    from albatros_axion_detection_gb300 import _lib
+    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    env = {"P": ctypes.c_void_p, "I64": ctypes.c_int64, "D": ctypes.c_double, "ctypes": ctypes}
+    shown = re.findall(r"^ab\.(ab_\w+)\.argtypes = (\[.*?\])", text, flags=re.M)
+    assert len(shown) >= 30
+    for name, lst in shown:
+        doc = eval(lst, env)
+        if name not in _lib.SIGNATURES:
+            continue  # ab_ctx_create takes an out-pointer; bound separately in _lib
+        ours = _lib.SIGNATURES[name][1]
+        assert len(doc) == len(ours), name
+        kind = lambda t: ("f" if t in (ctypes.c_double, ctypes.c_float) else "i", ctypes.sizeof(t))
+        for a, b in zip(doc, ours):  # doubles travel in other registers than integers and pointers
+            assert kind(a) == kind(b), (name, a, b)
