@@ -151,3 +151,37 @@ def test_integration_guide_argtypes_match_the_bindings():
         kind = lambda t: ("f" if t in (ctypes.c_double, ctypes.c_float) else "i", ctypes.sizeof(t))
         for a, b in zip(doc, ours):  # doubles travel in other registers than integers and pointers
             assert kind(a) == kind(b), (name, a, b)
+
+
+def test_python_signatures_match_the_header():
+    """Every ctypes signature the package binds has the header's argument
+    count and C types (pointer, 32/64-bit integer, double), return included."""
+    import ctypes
+    from albatros_axion_detection_gb300 import _lib
+    src = open(os.path.join(ROOT, "include", "albatros_gb300.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    protos = {m.group(2): (m.group(1), m.group(3))
+              for m in re.finditer(r"^\s*((?:const\s+)?[\w ]+?\s*\**)\s*(ab_\w+)\s*\(([^)]*)\)\s*;", src, flags=re.M)}
+
+    def ckind(decl):
+        decl = decl.strip()
+        if "*" in decl:
+            return ("i", 8)
+        if decl.startswith("double"):
+            return ("f", 8)
+        if decl.startswith("int64_t"):
+            return ("i", 8)
+        if decl.startswith(("int32_t", "int")):
+            return ("i", 4)
+        raise AssertionError(decl)
+
+    def pkind(t):
+        return ("f" if t in (ctypes.c_double, ctypes.c_float) else "i", ctypes.sizeof(t))
+
+    for name, (res, args) in _lib.SIGNATURES.items():
+        ret, params = protos[name]
+        params = [] if params.strip() in ("", "void") else params.split(",")
+        assert len(params) == len(args), name
+        for decl, t in zip(params, args):
+            assert ckind(decl) == pkind(t), (name, decl, t)
+        assert ckind(ret) == pkind(res), (name, ret, res)
