@@ -552,8 +552,9 @@ __device__ __forceinline__ void prefetch_item_extras(float* st_taps, int K, int 
 // blocks' first rows (y row phi + k*O): a block's 4*O rows then sit at
 // base + c + kYPad*(c/O) for compile-time c; blocks O + kYPad floats apart
 // fall in distinct banks (one lane per block), and the filter's stores of
-// lanes U rows apart meet at most 2-way conflicts for any U (a 1-float pad
-// gives 3-way at U = 41, 11-way at U = 21).  (Two lanes per block, each
+// lanes U rows apart meet at most 2-way conflicts at osamp 64 for U = 21 and
+// 41 (at most 4-way at the other osamp values; a 1-float pad gives 3-way at
+// U = 41, 11-way at U = 21).  (Two lanes per block, each
 // taking half the FFT, removed the fold's idle threads but met 2-way
 // conflicts on every y load and cost more than it saved.)
 template <int O>
