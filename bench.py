@@ -2,19 +2,25 @@
 
 Workload (the full-chain streaming configuration): 2 antennas x 2 pols of
 4-bit packets, 64 contiguous coarse channels, 2^20 spectra per antenna fed in
-chunks of 2^15 spectra (IPFB cut 80 -> nslice 32928 = 2^5*3*7^3), PFB osamp 64
-(4096 fine channels), 512 fine blocks per job (31 jobs), fine 4x4 visibilities
-per job.  One step = the whole 2^20-spectrum stream.  Synthetic seeded data
-(Gaussian nibbles, sigma 2.5, clipped to +-7).
+chunks of 2^15 spectra (IPFB cut 10, the reference's default -> nslice 32788;
+--cut 80 gives nslice 32928 = 2^5*3*7^3), PFB osamp 64 (4096 fine channels),
+512 fine blocks per job (31 jobs), fine 4x4 visibilities per job.  One step =
+the whole 2^20-spectrum stream.  Synthetic seeded data (Gaussian nibbles,
+sigma 2.5, clipped to +-7).
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference|plain-gpu] [--cut C]
 
 Prints one JSON line (rank 0).  `value` is device-resident throughput; `e2e`
 is the same through the public API from pinned host packets with the H2D copy
 of the step's packets and the D2H read of the visibilities inside the timed
 region; `roofline` is the dominant kernel's achieved HBM bandwidth against
 MEASURED_PEAKS.json; `cpu_baseline` the CPU chain on this host's cores over a
-bounded sample.  `--impl reference` times the reference's CPU path.
+bounded sample; `parity` the error of jobs 0-1 and of the IPFB and PFB outputs
+against the FP64 oracle (computed after the timed regions); `plain_gpu` the
+reference's plain GPU path (its CuPy glue restated in torch around cuFFT and
+cuBLAS, baseline/plain_gpu.py) on the same workload.  `--impl reference` times
+the reference's CPU path; `--impl plain-gpu` prints the plain GPU path's own
+line.
 """
 from __future__ import annotations
 
@@ -33,11 +39,15 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "input spectra/s, unpack→IPFB→PFB→xcorr on 1 GB300 vs plain GPU path; HBM % roofline"
-NANT, NCHAN_RAW, NSPEC, ACCLEN, CUT, OSAMP, NBLOCK, NTAP, THRESH = 2, 64, 2 ** 20, 2 ** 15, 80, 64, 512, 4, 0.45
+NANT, NCHAN_RAW, NSPEC, ACCLEN, CUT, OSAMP, NBLOCK, NTAP, THRESH = 2, 64, 2 ** 20, 2 ** 15, 10, 64, 512, 4, 0.45
 CHAN0 = 640  # absolute number of the first recorded coarse channel
-WORKLOAD = ("full-chain streaming: 2 ant x 2 pol 4-bit, 64 coarse ch, 2^20 spectra in 2^15-spectrum chunks, "
-            "cut 80 (nslice 32928), osamp 64 -> 4096 fine ch, 512 fine blocks/job (31 jobs), fine xcorr")
 P = 4096
+
+
+def workload():
+    return ("full-chain streaming: 2 ant x 2 pol 4-bit, 64 coarse ch, 2^20 spectra in 2^15-spectrum chunks, "
+            f"cut {CUT} (nslice {ACCLEN + 2 * CUT}), osamp 64 -> 4096 fine ch, 512 fine blocks/job (31 jobs), "
+            "fine xcorr")
 
 
 def peaks():
@@ -272,6 +282,15 @@ def run_ours(args):
     achieved = per_launch / (avg_ms / 1e3) / 1e9
     traffic = traffic_per_launch(dom)
 
+    parity = None
+    if rank == 0 and not args.no_check and nchunks >= 3 and NANT == 2:
+        vis01 = sc.vis_device()[:2].permute(1, 2, 3, 0).cpu().numpy()
+        parity = parity_check(raw[:, : 3 * ACCLEN].cpu().numpy(), vis01)
+
+    plain = None
+    if rank == 0 and not args.no_plain:
+        plain = plain_gpu_leg(args, raw, local)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline_sample(raw.cpu().numpy(), sc)
@@ -281,7 +300,7 @@ def run_ours(args):
             "metric": METRIC, "value": value, "unit": "spectra/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded Gaussian 4-bit packets)",
-            "config": {"workload": WORKLOAD, "spectra_per_step": spectra_per_step, "chunks_per_step": nchunks,
+            "config": {"workload": workload(), "spectra_per_step": spectra_per_step, "chunks_per_step": nchunks,
                        "time_stage": "%s %d" % sc.time_filter(),
                        "parallelism": f"replicas x{world}",
                        "l2": "inputs larger than L2 (256 MiB packets, 2 x 4.3 GB IPFB intermediates per step)"},
@@ -296,12 +315,117 @@ def run_ours(args):
             "gpu_launches": int(launches_per_step * args.steps),
             "clocks": clk.summary(),
         }
+        if parity:
+            out["parity"] = parity
+            out["max_rel_err"] = parity["vis_max_rel_err"]
+        if plain:
+            out["plain_gpu"] = dict(plain, speedup=value / plain["value"],
+                                    e2e_speedup=out["e2e"]["value"] / plain["e2e"]["value"])
         if cpu:
             out["cpu_baseline"] = cpu
         print(json.dumps(out), flush=True)
     sc.close()
     if dist is not None:
         dist.destroy_process_group()
+
+
+def parity_check(raw3, vis01):
+    """Errors of the benchmark's own outputs against the FP64 oracle, over the
+    first three chunks (which fully determine jobs 0 and 1):
+    - fine visibilities of jobs 0-1 (norm-wise relative, per job);
+    - the IPFB timestream: cupy_ipfb on chunk 0's rows of input 0 (with the
+      2*cut zero rows before them) against the FP64 IPFB and filter;
+    - the PFB band spectra: cupy_pfb_band over job 0's float32 timestream of
+      input 0 against the FP64 PFB of the same samples."""
+    import torch
+    from albatros_axion_detection_gb300 import pfb_gpu_utils as pg
+    from oracle import pfb_oracle as po
+    t0 = time.perf_counter()
+    channels = np.arange(CHAN0, CHAN0 + NCHAN_RAW)
+    sel = np.arange(NCHAN_RAW)
+    nslice = ACCLEN + 2 * CUT
+    filt = po.calculate_filter(po.get_matft(nslice), THRESH)
+    ref, (q0, q1) = po.repfb_xcorr_avg(raw3, channels, ACCLEN, 3, NBLOCK, 0, NCHAN_RAW, OSAMP, cut=CUT, filt=filt,
+                                       max_jobs=2)
+    vis_errs = [float(np.linalg.norm(vis01[..., k] - ref[..., k]) / np.linalg.norm(ref[..., k])) for k in range(2)]
+    out = {"vis_rel_err_per_job": vis_errs, "vis_max_rel_err": max(vis_errs), "jobs_checked": [0, 1]}
+    # IPFB timestream through cupy_ipfb
+    spec = po.unpack_4bit_np(raw3[0], 0, ACCLEN, sel)[0]
+    dat = np.zeros((nslice, 2049), np.complex128)
+    dat[2 * CUT:] = po.make_continuous(spec, np.arange(ACCLEN), 0, channels, ACCLEN)
+    try:
+        got = pg.cupy_ipfb(torch.from_numpy(dat.astype(np.complex64)).cuda(), pg.build_filter(nslice, THRESH))
+        exp = po.ipfb(dat, filt)
+        out["ipfb_timestream_rel_err"] = float(np.linalg.norm(got.cpu().numpy() - exp) / np.linalg.norm(exp))
+    except Exception as e:  # a length the library's cupy_ipfb does not run
+        out["ipfb_timestream_rel_err"] = None
+        out["ipfb_timestream_note"] = str(e).splitlines()[0][:160]
+    del dat
+    # PFB band spectra through cupy_pfb_band
+    lblock = P * OSAMP
+    ts = po.stream_timestream(raw3, 0, 0, sel, channels, ACCLEN, 2, CUT, filt)
+    ts32 = ts[: (NBLOCK + NTAP - 1) * lblock].astype(np.float32)
+    del ts
+    win = po.sinc_hamming(NTAP, lblock)
+    exp = po.pfb(ts32.astype(np.float64), win, nchan=lblock // 2 + 1, ntap=NTAP)[:, q0:q1]
+    got = pg.cupy_pfb_band(torch.from_numpy(ts32).cuda(), win.astype(np.float32), q0, q1, nchan=lblock // 2 + 1)
+    out["pfb_band_rel_err"] = float(np.linalg.norm(got.cpu().numpy() - exp) / np.linalg.norm(exp))
+    out["oracle"] = "FP64 (pocketfft float64), norm-wise relative error"
+    out["check_s"] = time.perf_counter() - t0
+    return out
+
+
+def plain_gpu_leg(args, raw, local):
+    """The reference's plain GPU path on the same device-resident packets:
+    `value` with the packets already on the device (its per-job D2H of the
+    visibilities included, as the reference does it), `e2e` with the packets'
+    H2D from pinned host memory inside the timed region too."""
+    import torch
+    try:
+        from baseline import plain_gpu
+        plain_gpu.lib()
+    except Exception as e:
+        return {"unavailable": str(e).splitlines()[0][:160]}
+    channels = np.arange(CHAN0, CHAN0 + NCHAN_RAW)
+    nchunks = raw.shape[1] // ACCLEN
+    chain = plain_gpu.PlainGpuChain(raw.shape[0], channels, ACCLEN, nchunks, NBLOCK, OSAMP, CUT, THRESH, NTAP)
+    ms, clk = _timed(torch, lambda: chain.run(raw), args.steps, args.warmup, local)
+    host = torch.empty(raw.shape, dtype=torch.uint8, pin_memory=True)
+    host.copy_(raw)
+    dev_in = torch.empty_like(raw)
+
+    def e2e():
+        dev_in.copy_(host, non_blocking=True)
+        chain.run(dev_in)
+    ms_e2e, _ = _timed(torch, e2e, args.steps, 1, local)
+    chain.close()
+    spectra = raw.shape[0] * raw.shape[1]
+    return {"impl": "plain-gpu", "value": spectra / (ms / 1e3), "unit": "spectra/s", "ms_per_step": ms,
+            "e2e": {"value": spectra / (ms_e2e / 1e3), "unit": "spectra/s", "ms_per_step": ms_e2e,
+                    "h2d_bytes_per_step": int(host.numel()),
+                    "d2h_bytes_per_step": int(chain.vis.size * 8)},
+            "what": "reference's CuPy glue restated op for op in torch around cuFFT (R2C/C2R plans, shared work "
+                    "area) and cuBLAS CgemmStridedBatched (handle per call), baseline/plain_gpu.py",
+            "clocks": clk}
+
+
+def run_plain(args):
+    """--impl plain-gpu: the plain GPU path's own JSON line."""
+    import torch
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if rank != 0:
+        return
+    torch.cuda.set_device(local)
+    raw = synth_raw(torch, torch.device("cuda", local))
+    leg = plain_gpu_leg(args, raw, local)
+    out = {"impl": "plain-gpu", "metric": METRIC, "unit": "spectra/s", "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+           "data": "synthetic (seeded Gaussian 4-bit packets)",
+           "config": {"workload": workload(), "spectra_per_step": int(raw.shape[0] * raw.shape[1])}}
+    out.update(leg)
+    print(json.dumps(out), flush=True)
 
 
 BATCH_WORKLOAD = ("uneven batch: 24 files (16 x 4-bit, 8 x 1-bit), 2 ant x 2 pol each, channels from {32,64,128,512}, "
@@ -530,7 +654,7 @@ def run_reference(args):
     out = {"impl": "reference", "metric": METRIC, "value": value, "unit": "spectra/s", "n_gpus": world,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded Gaussian 4-bit packets)",
-           "config": {"workload": WORKLOAD, "step": f"one {ACCLEN}-spectrum chunk of both antennas"},
+           "config": {"workload": workload(), "step": f"one {ACCLEN}-spectrum chunk of both antennas"},
            "cpu_baseline": {"value": value, "unit": "spectra/s", "cores": chain.workers, "kind": chain.kind,
                             "sample": f"one {ACCLEN}-spectrum chunk of both antennas per step"},
            "e2e": {"value": value, "unit": "spectra/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -538,12 +662,17 @@ def run_reference(args):
 
 
 def main():
+    global CUT
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference", "plain-gpu"])
+    ap.add_argument("--cut", type=int, default=CUT,
+                    help="stream: IPFB cut (default 10, the reference's; 80 gives a 7-smooth nslice)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline sample")
+    ap.add_argument("--no-check", action="store_true", help="skip the parity check against the FP64 oracle")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain-GPU comparator leg")
     ap.add_argument("--chunks", type=int, default=None,
                     help="stream only this many 2^15-spectrum chunks (smaller case for profiling; "
                          "every launch keeps its full size)")
@@ -566,8 +695,11 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    CUT = args.cut
     if args.impl == "reference":
         run_reference(args)
+    elif args.impl == "plain-gpu":
+        run_plain(args)
     elif args.workload == "uneven-batch":
         run_batch(args)
     elif args.workload == "unpack-xcorr":

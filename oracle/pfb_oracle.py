@@ -19,22 +19,38 @@ pfb                    src/utils/pfb_gpu_utils.py:105-121
 xcorr_all_ant          src/correlations/correlations_gpu.py:95-121
 make_continuous        src/correlations/baseband_data_classes.py:48-73
 plan_chunks            scripts/xcorr/helper_gpu_stream_clean.py:233-263
+stream_timestream      scripts/xcorr/helper_gpu_stream_clean.py:178-197, :433-438
 repfb_xcorr_avg        scripts/xcorr/helper_gpu_stream_clean.py:295-456 (buffer
                        semantics of BufferManager :71-167, original channel mapping
                        of scripts/xcorr/helper_gpu_stream.py:196)
 =====================  ============================================================
 
-Everything is complex128/float64.  ``numpy.fft`` follows the same
-normalisation as the reference's cuFFT wrapper (forward unscaled, inverse
-divided by n, imaginary parts of the DC and Nyquist bins ignored by irfft).
+Everything is complex128/float64.  The FFTs are pocketfft's double-precision
+transforms (``scipy.fft`` with all host threads when SciPy is present, else
+``numpy.fft``: the same algorithm), with the same normalisation as the
+reference's cuFFT wrapper (forward unscaled, inverse divided by n, imaginary
+parts of the DC and Nyquist bins ignored by irfft).
 """
 from __future__ import annotations
 
+import os
+
 import numpy as np
+
+try:
+    import scipy.fft as _sfft
+
+    def _rfft(a, n=None, axis=-1):
+        return _sfft.rfft(a, n=n, axis=axis, workers=os.cpu_count() or 1)
+
+    def _irfft(a, n=None, axis=-1):
+        return _sfft.irfft(a, n=n, axis=axis, workers=os.cpu_count() or 1)
+except ImportError:  # pragma: no cover - SciPy is installed wherever the tests run
+    _rfft, _irfft = np.fft.rfft, np.fft.irfft
 
 __all__ = [
     "sinc_hamming", "get_matft", "calculate_filter", "ipfb", "pfb",
-    "xcorr_all_ant", "make_continuous", "plan_chunks", "repfb_xcorr_avg",
+    "xcorr_all_ant", "make_continuous", "plan_chunks", "repfb_xcorr_avg", "stream_timestream",
     "decode_4bit", "unpack_4bit_np", "unpack_1bit_np", "band_edges",
 ]
 
@@ -58,7 +74,7 @@ def get_matft(nslice: int, nchan: int = 2049, ntap: int = 4, window_f32: bool = 
         win = win.astype(np.float32).astype(np.float64)
     mat = np.zeros((nslice, nn))
     mat[:ntap, :] = win.reshape(ntap, nn)
-    return np.fft.rfft(mat.T, axis=1)
+    return _rfft(mat.T, axis=1)
 
 
 def calculate_filter(matft: np.ndarray, thresh: float) -> np.ndarray:
@@ -76,9 +92,10 @@ def ipfb(dat: np.ndarray, filt: np.ndarray) -> np.ndarray:
     along time, times filt, irfft along time.
 
     Returns the transposed view like the reference (F-ordered result)."""
-    dd = np.fft.irfft(dat, axis=1)
-    ddft = np.fft.rfft(dd.T, axis=1)
-    res = np.fft.irfft(ddft * filt, n=dd.shape[0], axis=1)
+    dd = _irfft(dat, axis=1)
+    ddft = _rfft(dd.T, axis=1)
+    ddft *= filt
+    res = _irfft(ddft, n=dd.shape[0], axis=1)
     return res.T
 
 
@@ -91,8 +108,8 @@ def pfb(timestream: np.ndarray, win: np.ndarray, nchan: int = 2049, ntap: int = 
     w = np.asarray(win, dtype=np.float64).reshape(ntap, lblock)
     y = ts[0:nblock] * w[0]
     for i in range(1, ntap):
-        y = y + ts[i:nblock + i] * w[i]
-    return np.fft.rfft(y, axis=1)
+        y += ts[i:nblock + i] * w[i]
+    return _rfft(y, axis=1)
 
 
 def xcorr_all_ant(x: np.ndarray, nant: int, npol: int, ntime: int, nfreq: int) -> np.ndarray:
@@ -192,10 +209,40 @@ def band_edges(channels, chanstart: int, chanend: int, osamp: int):
     return q0, q1
 
 
+def stream_timestream(raw: np.ndarray, a: int, p: int, sel, chan_abs, acclen: int, nchunks: int, cut: int,
+                      filt: np.ndarray, spec_present=None, bits: int = 4) -> np.ndarray:
+    """The IPFB timestream of input (antenna a, pol p) over the first nchunks
+    chunks, float64 (nchunks*acclen*4096 samples): per chunk, the previous
+    chunk's last 2*cut placed rows (zeros before the first) and this chunk's
+    acclen rows go through the IPFB and the [cut, nslice-cut) rows are kept
+    (IPFBProcessor.process_chunk, scripts/xcorr/helper_gpu_stream_clean.py:178-197,
+    and the cut_pol refresh :433-438)."""
+    nslice = acclen + 2 * cut
+    lchunk = acclen * 4096
+    ts = np.empty(nchunks * lchunk)
+    prev = np.zeros((2 * cut, 2049), np.complex128)
+    for j in range(nchunks):
+        rows = np.arange(j * acclen, (j + 1) * acclen)
+        if bits == 4:
+            spec = unpack_4bit_np(raw[a], rows[0], rows[-1] + 1, sel)[p]
+        else:
+            spec = unpack_1bit_channels(raw[a], rows[0], rows[-1] + 1, sel)[p]
+        if spec_present is not None:
+            keep = np.asarray(spec_present[a][rows], dtype=bool)
+            placed = make_continuous(spec[keep], rows[keep], 0, chan_abs, acclen)
+        else:
+            placed = make_continuous(spec, rows, 0, chan_abs, acclen)
+        x = np.concatenate([prev, placed], axis=0)
+        ts[j * lchunk:(j + 1) * lchunk] = ipfb(x, filt)[cut:nslice - cut].ravel()
+        prev = placed[acclen - 2 * cut:].copy()
+        del x, placed
+    return ts
+
+
 def repfb_xcorr_avg(raw: np.ndarray, channels, acclen: int, nchunks: int, nblock: int,
                     chanstart: int, chanend: int, osamp: int, cut: int = 10,
                     filt_thresh: float = 0.45, ntap: int = 4, spec_present=None,
-                    filt=None, bits: int = 4):
+                    filt=None, bits: int = 4, max_jobs=None):
     """Streaming unpack -> IPFB -> PFB -> xcorr, FP64 restatement of
     repfb_xcorr_avg (scripts/xcorr/helper_gpu_stream_clean.py:295-402).
 
@@ -204,7 +251,12 @@ def repfb_xcorr_avg(raw: np.ndarray, channels, acclen: int, nchunks: int, nblock
     channels: absolute channel numbers of the raw columns.
     spec_present: optional (nant, nchunks*acclen) bool; False rows are missing
     (zero-filled, as make_continuous does for absent specnums).
+    max_jobs: compute only the first max_jobs jobs of the plan (and only the
+    chunks they read); None computes every job.
     Returns vis (M, M, nfine, njobs) complex128 and the fine band (q0, q1).
+
+    One input (antenna, pol) is carried at a time, so the working set is one
+    input's timestream plus one job's PFB, whatever the number of inputs.
     """
     nant = raw.shape[0]
     npol, M = 2, 2 * raw.shape[0]
@@ -217,32 +269,24 @@ def repfb_xcorr_avg(raw: np.ndarray, channels, acclen: int, nchunks: int, nblock
     win = sinc_hamming(ntap, lblock)
     q0, q1 = band_edges(channels, chanstart, chanend, osamp)
     jobs = plan_chunks(nchunks, acclen * 4096, nblock, lblock, ntap)
-    ts = np.zeros((M, nchunks * acclen * 4096))
+    if max_jobs is not None:
+        jobs = jobs[:max_jobs]
+    njobs = len(jobs)
+    # samples the jobs read (the last one zero-padded past the stream's end)
+    span = (njobs * nblock + ntap - 1) * lblock
+    lchunk = acclen * 4096
+    nch_used = min(nchunks, -(-span // lchunk))
+    xin = np.zeros((M, njobs, nblock, q1 - q0), np.complex128)
     for a in range(nant):
-        prev = [np.zeros((2 * cut, 2049), np.complex128) for _ in range(npol)]
-        for j in range(nchunks):
-            rows = np.arange(j * acclen, (j + 1) * acclen)
-            if bits == 4:
-                pols = unpack_4bit_np(raw[a], rows[0], rows[-1] + 1, sel)
-            else:
-                pols = unpack_1bit_channels(raw[a], rows[0], rows[-1] + 1, sel)
-            for p in range(npol):
-                spec = pols[p]
-                if spec_present is not None:
-                    keep = np.asarray(spec_present[a][rows], dtype=bool)
-                    placed = make_continuous(spec[keep], rows[keep], 0, chan_abs, acclen)
-                else:
-                    placed = make_continuous(spec, rows, 0, chan_abs, acclen)
-                x = np.concatenate([prev[p], placed], axis=0)
-                out = ipfb(x, filt)[cut:nslice - cut]
-                ts[2 * a + p, j * acclen * 4096:(j + 1) * acclen * 4096] = out.ravel()
-                prev[p] = placed[acclen - 2 * cut:]
-    span = (nblock + ntap - 1) * lblock
-    pad = np.zeros((M, len(jobs) * nblock * lblock + span))
-    pad[:, : ts.shape[1]] = ts[:, : pad.shape[1]]
-    vis = np.zeros((M, M, q1 - q0, len(jobs)), np.complex128)
-    for k in range(len(jobs)):
-        seg = pad[:, k * nblock * lblock: k * nblock * lblock + span]
-        xin = np.stack([pfb(seg[m], win, nchan=lblock // 2 + 1, ntap=ntap)[:, q0:q1] for m in range(M)])
-        vis[..., k] = xcorr_all_ant(xin, nant, npol, nblock, q1 - q0)
+        for p in range(npol):
+            ts = np.zeros(max(span, nch_used * lchunk))
+            ts[:nch_used * lchunk] = stream_timestream(raw, a, p, sel, chan_abs, acclen, nch_used, cut, filt,
+                                                       spec_present, bits)
+            for k in range(njobs):
+                seg = ts[k * nblock * lblock: k * nblock * lblock + (nblock + ntap - 1) * lblock]
+                xin[2 * a + p, k] = pfb(seg, win, nchan=lblock // 2 + 1, ntap=ntap)[:, q0:q1]
+            del ts
+    vis = np.zeros((M, M, q1 - q0, njobs), np.complex128)
+    for k in range(njobs):
+        vis[..., k] = xcorr_all_ant(xin[:, k], nant, npol, nblock, q1 - q0)
     return vis, (q0, q1)
