@@ -41,6 +41,7 @@ struct ab_stream {
   ab_ctx* ctx = nullptr;
   int nant = 0, M = 0, P = 4096, O = 1, ntap = 4;
   int64_t nchan_raw = 0, nsel = 0, acclen = 0, cut = 0, nslice = 0;
+  int64_t ld = 0;  // column stride of the [n][t] intermediate: nslice rounded up to 32 floats (128 B)
   int bits = 4;
   int64_t nblock = 0, njobs = 0, q0 = 0, q1 = 0, nq = 0;
   float thresh = 0.f;
@@ -94,7 +95,7 @@ static void stream_free(ab_stream* st) {
 static size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
 static void workspace_parts(const ab_stream* st, size_t part[3]) {
   const int64_t L = (int64_t)st->P * st->O;
-  part[0] = align256(sizeof(float) * (size_t)st->M * st->P * st->nslice);
+  part[0] = align256(sizeof(float) * (size_t)st->M * st->P * st->ld);
   part[1] = align256(sizeof(float) * (size_t)st->M * st->nb_max * L);
   part[2] = align256(sizeof(float2) * (size_t)st->M * st->nb_max * st->nq);
 }
@@ -143,6 +144,11 @@ extern "C" int ab_stream_create(ab_ctx* ctx, int64_t nant, int64_t nchan_raw, in
   st->acclen = acclen;
   st->cut = cut;
   st->nslice = acclen + 2 * cut;
+  // every column starts on a 128-byte boundary whatever nslice is (the
+  // reference's default cut = 10 gives nslice = acclen + 20), so the row
+  // stage's 32-byte column stores and the time stage's 16-byte staging copies
+  // stay aligned; rows [nslice, ld) are never written or read
+  st->ld = (st->nslice + 31) / 32 * 32;
   st->nblock = nblock;
   st->njobs = njobs;
   st->q0 = q0;
@@ -219,7 +225,7 @@ extern "C" int ab_stream_create(ab_ctx* ctx, int64_t nant, int64_t nchan_raw, in
   AB_ALLOC(st->d_abs, sizeof(int32_t) * nsel);
   AB_ALLOC(st->d_wtaps, sizeof(float) * ntap * P);
   AB_ALLOC(st->d_win, sizeof(float) * ntap * L);
-  for (int i = 0; i < (st->fused ? 1 : 2); i++) AB_ALLOC(st->interm[i], sizeof(float) * (size_t)M * P * st->nslice);
+  for (int i = 0; i < (st->fused ? 1 : 2); i++) AB_ALLOC(st->interm[i], sizeof(float) * (size_t)M * P * st->ld);
   if (st->fused) AB_ALLOC(st->state, sizeof(float) * (size_t)2 * M * P * 4 * osamp);
   AB_ALLOC(st->W, sizeof(float) * (size_t)M * st->nb_max * L);
   AB_ALLOC(st->Y, sizeof(float2) * (size_t)M * st->nb_max * st->nq);
@@ -366,7 +372,7 @@ static int stream_push(ab_stream* st, const uint8_t* raw, int64_t ant_stride, co
   AB_CHECK_ARG(chunk == st->chunks_done, "ab_stream_push: expected chunk %lld, got %lld", (long long)st->chunks_done,
                (long long)chunk);
   const int P = st->P, O = st->O, M = st->M;
-  const int64_t acclen = st->acclen, cut = st->cut, nslice = st->nslice;
+  const int64_t acclen = st->acclen, cut = st->cut, nslice = st->nslice, ld = st->ld;
   // the row stage reads spectra up to (chunk+1)*acclen - 1: through the map,
   // or as raw rows when there is none
   const int64_t need = (chunk + 1) * acclen, row_bytes = st->bits == 4 ? 2 * st->nchan_raw : st->nchan_raw / 2;
@@ -396,14 +402,14 @@ static int stream_push(ab_stream* st, const uint8_t* raw, int64_t ant_stride, co
                  st->d_cols, st->d_abs, (int)st->nsel, st->bits};
   {
     StageTimer t(st, s, 0);
-    AB_TRY(launch_row_stage_packed4(st->ctx, src, st->nant, (int)nslice, P, st->planP, st->twP, cur, nslice, s));
+    AB_TRY(launch_row_stage_packed4(st->ctx, src, st->nant, (int)nslice, P, st->planP, st->twP, cur, ld, s));
     t.done(1);
   }
   // 2. time stage (with the PFB fold fused in when osamp >= 4)
   if (st->fir_J > 0 || st->iir_W > 0) {
     StageTimer t(st, s, 1);
     const size_t half = (size_t)M * P * 4 * O;
-    FirArgs fa_fir{cur, nslice, P, M, (int)nslice, (int)cut, (int)acclen, st->fir_taps, st->fir_J,
+    FirArgs fa_fir{cur, ld, P, M, (int)nslice, (int)cut, (int)acclen, st->fir_taps, st->fir_J,
                    st->fir_row_tile, st->state + (chunk & 1) * half, st->state + ((chunk + 1) & 1) * half,
                    st->ctx->tw64, st->ctx->num_sms, st->iir_W};
     FoldArgs fa{O, st->ntap, (int)cut, (int)acclen, row0_all, nb_all, st->d_win, st->W, nullptr};
@@ -412,12 +418,12 @@ static int stream_push(ab_stream* st, const uint8_t* raw, int64_t ant_stride, co
   } else if (st->fused) {
     StageTimer t(st, s, 1);
     FoldArgs fa{O, st->ntap, (int)cut, (int)acclen, row0_all, nb_all, st->d_win, st->W, st->state};
-    AB_TRY(launch_time_fold(st->ctx, cur, nslice, M, P, (int)nslice, st->planM, st->twN, st->d_wtaps, st->ntap,
+    AB_TRY(launch_time_fold(st->ctx, cur, ld, M, P, (int)nslice, st->planM, st->twN, st->d_wtaps, st->ntap,
                             st->thresh, fa, st->ctx->tw64, s));
     t.done(1);
   } else {
     StageTimer t(st, s, 1);
-    AB_TRY(launch_time_stage(st->ctx, cur, nslice, M, P, (int)nslice, st->planM, st->twN, nullptr, st->d_wtaps,
+    AB_TRY(launch_time_stage(st->ctx, cur, ld, M, P, (int)nslice, st->planM, st->twN, nullptr, st->d_wtaps,
                              st->ntap, st->thresh, s));
     t.done(1);
   }
@@ -427,7 +433,7 @@ static int stream_push(ab_stream* st, const uint8_t* raw, int64_t ant_stride, co
     const int64_t nb = st->fused ? nb_all : std::min(nb_all - done, st->nb_max);
     if (!st->fused) {
       const int64_t row0 = row0_all + done * O;
-      TsSrc ts{cur, prev, nslice, cut, cut + acclen, acclen, 0};
+      TsSrc ts{cur, prev, ld, cut, cut + acclen, acclen, 0};
       StageTimer t(st, s, 2);
       AB_TRY(launch_pfb_stage_a(ts, M, P, O, st->ntap, row0, nb, st->d_win, st->W, st->ctx->tw64, s));
       t.done(1);

@@ -474,6 +474,10 @@ extern "C" int ab_avg_xcorr_all_ant(const float* x, int64_t nant, int64_t npol, 
 }
 
 namespace ab {
+// Largest channel count of one coarse-correlator call (grid x stays far below
+// its limit, and the scratch size below cannot wrap).
+constexpr int64_t kCoarseMaxCols = 1 << 20;
+
 int coarse_xcorr_run(ab_ctx* ctx, const uint8_t* raw, int64_t ant_stride, int64_t nant, int64_t nchan,
                      int64_t rowstart, int64_t nrows, const int32_t* rows, const int64_t* channels, int64_t ncols,
                      int64_t chunk_rows, long long* G, int64_t* out_re, int64_t* out_im, cudaStream_t s) {
@@ -533,11 +537,16 @@ int coarse_xcorr_run(ab_ctx* ctx, const uint8_t* raw, int64_t ant_stride, int64_
   return AB_OK;
 }
 
+// Bytes of int64 partial sums one call needs, or 0 when that count would not
+// fit in 62 bits (absurd channel or chunk counts); callers reject 0.
 size_t coarse_xcorr_scratch_bytes(int64_t nant, int64_t nrows, int64_t ncols, int64_t chunk_rows) {
   const int R = (int)(4 * nant);
   const int Rp = ((R + 15) / 16) * 16;
-  const int64_t nchunks = (nrows + chunk_rows - 1) / chunk_rows;
-  return sizeof(long long) * (size_t)(nchunks * ncols) * Rp * Rp;
+  if (nrows < 1 || chunk_rows < 1 || ncols < 1 || ncols > kCoarseMaxCols) return 0;
+  const unsigned long long nchunks = (unsigned long long)((nrows + chunk_rows - 1) / chunk_rows);
+  const unsigned long long per_chunk = sizeof(long long) * (unsigned long long)Rp * Rp * (unsigned long long)ncols;
+  if (nchunks > (1ull << 62) / per_chunk) return 0;
+  return (size_t)(per_chunk * nchunks);
 }
 }  // namespace ab
 
@@ -552,8 +561,11 @@ extern "C" int ab_xcorr_coarse_4bit(ab_ctx* ctx, const uint8_t* raw, int64_t ant
   AB_CHECK_ARG(ant_stride >= nspec * 2 * nchan || nant == 1, "ab_xcorr_coarse_4bit: antenna stride too small");
   if (chunk_rows <= 0 || chunk_rows > nrows) chunk_rows = nrows;
   AB_CHECK_ARG(chunk_rows <= (1ll << 24), "ab_xcorr_coarse_4bit: chunk_rows must be <= 2^24 (int32 partials)");
+  const size_t need = coarse_xcorr_scratch_bytes(nant, nrows, ncols, chunk_rows);
+  AB_CHECK_ARG(need > 0, "ab_xcorr_coarse_4bit: %lld channels in %lld chunks is too large (at most %lld channels)",
+               (long long)ncols, (long long)((nrows + chunk_rows - 1) / chunk_rows), (long long)kCoarseMaxCols);
   void* G = nullptr;
-  AB_TRY(get_scratch(ctx, kScratchXcorrG, coarse_xcorr_scratch_bytes(nant, nrows, ncols, chunk_rows), &G));
+  AB_TRY(get_scratch(ctx, kScratchXcorrG, need, &G));
   return coarse_xcorr_run(ctx, raw, ant_stride, nant, nchan, rowstart, nrows, rows, channels, ncols, chunk_rows,
                           (long long*)G, out_re, out_im, as_stream(stream));
 }
@@ -572,11 +584,13 @@ extern "C" int ab_xcorr_coarse_4bit(ab_ctx* ctx, const uint8_t* raw, int64_t ant
 // The buffer is a file-scope __device__ array of kNoAllocScratchBytes (16 MiB);
 // every GPU that loads this library holds it until the process exits.  In
 // host code the array's name is only a host-side stand-in, so its device
-// address is fetched once per device with cudaGetSymbolAddress the first time
-// the entry point runs on that device; make that first call before any stream
-// capture.  All calls share the one buffer: the entry point clears it at the
-// start of every call, and calls whose work overlaps on the GPU (different
-// streams, or several host threads on one device) race on it.
+// address is fetched with cudaGetSymbolAddress, with that device current, by
+// every call made outside stream capture; a call made while its stream is
+// being captured uses the address the last uncaptured call on that device
+// found, so the first call on a device must come before any stream capture.
+// All calls share the one buffer: the entry point clears it at the start of
+// every call, and calls whose work overlaps on the GPU (different streams, or
+// several host threads on one device) race on it.
 constexpr size_t kNoAllocScratchBytes = 16u << 20;
 static __device__ __align__(256) long long g_noalloc_scratch[kNoAllocScratchBytes / sizeof(long long)];
 
@@ -597,17 +611,22 @@ extern "C" int ab_xcorr_coarse_4bit_noalloc(const uint8_t* raw, int64_t ant_stri
   if (chunk_rows <= 0 || chunk_rows > nrows) chunk_rows = nrows;
   AB_CHECK_ARG(chunk_rows <= (1ll << 24), "ab_xcorr_coarse_4bit_noalloc: chunk_rows must be <= 2^24");
   const size_t need = coarse_xcorr_scratch_bytes(nant, nrows, ncols, chunk_rows);
-  AB_CHECK_ARG(need <= kNoAllocScratchBytes,
+  AB_CHECK_ARG(need > 0 && need <= kNoAllocScratchBytes,
                "ab_xcorr_coarse_4bit_noalloc: this call needs %zu bytes of scratch but the built-in buffer holds "
                "%zu; split it into calls with fewer channels or chunks, or use ab_xcorr_coarse_4bit",
                need, kNoAllocScratchBytes);
   int dev = 0;
   AB_CUDA(cudaGetDevice(&dev));
   AB_CHECK_ARG(dev >= 0 && dev < 128, "ab_xcorr_coarse_4bit_noalloc: device index %d out of range", dev);
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  AB_CUDA(cudaStreamIsCapturing(as_stream(stream), &cap));
   void* G = nullptr;
   {
     std::lock_guard<std::mutex> lk(g_noalloc_mu);
-    if (!g_noalloc_addr[dev]) {
+    if (cap == cudaStreamCaptureStatusNone) {
+      // Outside capture the address is looked up on every call: after a
+      // device reset, or with another context current on this device, the
+      // module (and the buffer) may sit somewhere else than last time.
       void* p = nullptr;
       cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
       if (e != cudaSuccess || !p) {
@@ -615,6 +634,9 @@ extern "C" int ab_xcorr_coarse_4bit_noalloc(const uint8_t* raw, int64_t ant_stri
         return AB_ERR_CUDA;
       }
       g_noalloc_addr[dev] = p;
+    } else if (!g_noalloc_addr[dev]) {
+      set_error("ab_xcorr_coarse_4bit_noalloc: the first call on device %d must come before any stream capture", dev);
+      return AB_ERR_ARG;
     }
     G = g_noalloc_addr[dev];
   }

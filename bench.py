@@ -509,20 +509,29 @@ def run_batch(args):
     print(json.dumps(out), flush=True)
 
 
-def _timed(torch, fn, steps, warmup, local):
-    """ms per call of fn() (CUDA events on the current stream, after warm-up)."""
+def _timed(torch, fn, steps, warmup, local, min_s=2.0):
+    """ms per call of fn() (CUDA events on the current stream, after warm-up).
+    Short calls are repeated until the timed region lasts at least min_s, so
+    that the clock sampler (every 200 ms) sees it; the calls actually timed
+    are in the returned clock record as `timed_calls`."""
     s = torch.cuda.current_stream()
     for _ in range(warmup):
         fn()
     torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    fn()
+    torch.cuda.synchronize()
+    one = max(time.perf_counter() - t0, 1e-6)
+    n = max(int(steps), int(np.ceil(min_s / one)))
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clk:
         e0.record(s)
-        for _ in range(steps):
+        for _ in range(n):
             fn()
         e1.record(s)
         torch.cuda.synchronize()
-    return e0.elapsed_time(e1) / steps, clk.summary()
+    summary = dict(clk.summary(), timed_calls=n)
+    return e0.elapsed_time(e1) / n, summary
 
 
 def _line(metric, value, unit, ms, args, workload, extra):

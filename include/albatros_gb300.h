@@ -233,10 +233,12 @@ int ab_xcorr_coarse_4bit(ab_ctx *ctx, const uint8_t *raw, int64_t ant_stride, in
  * the device, a loop where an allocation could stall or fail).  Its partial
  * sums live in a 16 MiB buffer built into the library (held on every device
  * that loads it until exit); calls needing more scratch than that, i.e.
- * nchunks * ncols * (16*ceil(nant/4))^2 * 8 bytes, return AB_ERR_ARG.  The
- * first call on a device looks up the buffer's device address and should come
- * before any stream capture.  All calls share the buffer (cleared at the start
- * of each call), so calls that overlap on the GPU race. */
+ * nchunks * ncols * (16*ceil(nant/4))^2 * 8 bytes, return AB_ERR_ARG.  Each
+ * call made outside stream capture looks up the buffer's device address; a
+ * call made during a capture reuses the last address found on that device, so
+ * the first call on a device must come before any stream capture.  All calls
+ * share the buffer (cleared at the start of each call), so calls that overlap
+ * on the GPU race. */
 int ab_xcorr_coarse_4bit_noalloc(const uint8_t *raw, int64_t ant_stride, int64_t nant, int64_t nspec, int64_t nchan,
                                  int64_t rowstart, int64_t nrows, const int32_t *rows, const int64_t *channels,
                                  int64_t ncols, int64_t chunk_rows, int64_t *out_re, int64_t *out_im, void *stream);

@@ -4,8 +4,9 @@
 - ``_ref/lib_unpacking.so`` and ``_ref/lib_correlations_cpu.so`` from the
   reference's own ``src/correlations/unpacking.c`` and
   ``src/correlations/correlations_cpu.c``, compiled where they lie, only when
-  the reference checkout exists at $ALBATROS_REFERENCE (default
-  /root/reference).  Outputs go to ``oracle/_ref/`` (git-ignored).
+  the reference checkout is found: at $ALBATROS_REFERENCE, else in a
+  directory ``reference`` beside this repository's checkout.  Outputs go to
+  ``oracle/_ref/`` (git-ignored).
 
 TEST INFRASTRUCTURE: the product path never loads these libraries.
 """
@@ -16,7 +17,7 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = os.environ.get("ALBATROS_REFERENCE", "/root/reference")
+REF = os.environ.get("ALBATROS_REFERENCE") or os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
 CFLAGS = ["-O3", "-std=c99", "-fPIC", "-shared", "-fopenmp"]
 
 

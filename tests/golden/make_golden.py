@@ -1,7 +1,7 @@
 """Generate the golden fixtures in tests/golden/ from the REFERENCE's own code.
 
-Run in a checkout that has the reference at $ALBATROS_REFERENCE (default
-/root/reference).  It
+Run with the reference checkout at $ALBATROS_REFERENCE (or in a directory
+``reference`` beside this repository's checkout).  It
   1. compiles the reference's C (src/correlations/unpacking.c,
      src/correlations/correlations_cpu.c) with oracle/build.py into oracle/_ref/
      and calls it through ctypes with the reference's own argument types
@@ -30,11 +30,12 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
-REF = os.environ.get("ALBATROS_REFERENCE", "/root/reference")
 sys.path.insert(0, ROOT)
 
 from oracle import build as obuild  # noqa: E402
 from tests.golden import gen  # noqa: E402
+
+REF = obuild.REF
 
 P, I, S = ctypes.c_void_p, ctypes.c_int, ctypes.c_short
 

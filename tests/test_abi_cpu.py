@@ -109,6 +109,11 @@ def test_every_entry_point_rejects_bad_arguments_on_host():
         ("ab_xcorr_coarse_4bit", None, 16, 100, 2, 100, 8, 0, 10, None, 16, 4, 0, 16, 16, None),
         ("ab_xcorr_coarse_4bit_noalloc", 16, 100, 2, 100, 8, 90, 20, None, 16, 4, 0, 16, 16, None),  # rows past nspec
         ("ab_xcorr_coarse_4bit_noalloc", 16, 100, 40, 100, 8, 0, 20, None, 16, 4, 0, 16, 16, None),  # 40 antennas
+        # channel or chunk counts whose scratch size would wrap a 64-bit product
+        ("ab_xcorr_coarse_4bit_noalloc", 16, 1 << 50, 32, 1 << 40, 8, 0, 1 << 40, None, 16, 1 << 40, 1, 16, 16,
+         None),
+        ("ab_xcorr_coarse_4bit_noalloc", 16, 1 << 50, 32, 1 << 40, 8, 0, 1 << 40, None, 16, 1 << 20, 1, 16, 16,
+         None),
         ("ab_avg_xcorr_4bit_pairs", None, 16, 16, 16, 4, 4, 16, 16, None),
         ("ab_avg_xcorr_1bit_pairs", None, 16, 16, 16, 4, 4, 8, 16, None),
         ("ab_stream_create", None, 2, 64, 4, 16, 16, 64, 32768, 80, 64, 4, 0.45, 512, 2, 0, 4096,

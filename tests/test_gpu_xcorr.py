@@ -1,5 +1,7 @@
 """GPU parity: correlators.  Integer paths bit-exact against the C oracle /
 the reference's golden sums; float paths within 1e-5 relative of FP64."""
+import os
+
 import numpy as np
 import pytest
 import torch
@@ -79,6 +81,41 @@ def test_coarse_xcorr_bit_exact(nant, nspec, nchan, chunk, mma_bits):
         er, ei = io.xcorr_all_ant_4bit(raw, r0, r1, ch, nchan, nthreads=8)
         np.testing.assert_array_equal(re[k], er)
         np.testing.assert_array_equal(im[k], ei)
+
+
+_full = {}
+
+
+def test_coarse_xcorr_many_antenna_full_size(mma_bits):
+    """The many-antenna coarse correlator workload at its full size: 16
+    antennas x 2 pols (all 528 input pairs), 256 channels, 2^18 spectra (2 GiB
+    of packets, every nibble value including 0x8), one average over all
+    spectra, bit-exact against the int64 oracle."""
+    from albatros_axion_detection_gb300.correlations import xcorr_coarse_4bit
+    nant, nchan, nspec = 16, 256, 1 << 18
+    if "raw" not in _full:
+        _full["raw"] = gen.raw_4bit_uniform(seed=418, nspec=nspec, nchan=nchan, nant=nant)
+        _full["ref"] = io.xcorr_all_ant_4bit(_full["raw"], 0, nspec, np.arange(nchan), nchan,
+                                             nthreads=os.cpu_count() or 1)
+    raw = _full["raw"]
+    er, ei = _full["ref"]
+    re, im = xcorr_coarse_4bit(cu(raw), 0, nspec, np.arange(nchan), nchan, average=False)
+    np.testing.assert_array_equal(re.cpu().numpy()[0], er)
+    np.testing.assert_array_equal(im.cpu().numpy()[0], ei)
+
+
+def test_coarse_xcorr_rejects_oversized_channel_counts():
+    """A channel count whose partial-sum scratch would overflow is refused on
+    the host with AB_ERR_ARG before anything runs."""
+    import ctypes
+    from albatros_axion_detection_gb300 import _lib
+    lib = _lib.load()
+    raw = cu(np.zeros((2, 16, 16), np.uint8))
+    ch = cu(np.zeros(4, np.int64))
+    out = cu(np.zeros(16, np.int64))
+    rc = lib.ab_xcorr_coarse_4bit(_lib.ctx(), raw.data_ptr(), 256, 2, 16, 8, 0, 16, None, ch.data_ptr(), 1 << 40,
+                                  16, out.data_ptr(), out.data_ptr(), None)
+    assert rc == -1 and b"too large" in lib.ab_last_error()
 
 
 def test_coarse_xcorr_worst_case_magnitudes(mma_bits):
