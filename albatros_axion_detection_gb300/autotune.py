@@ -138,6 +138,8 @@ def set_time_filter(mode: int = DEFAULT_MODE, row_tile: int = 0, device: Optiona
 OPT_ROW_FFTS_PER_CTA = 1
 OPT_COARSE_MMA_BITS = 3
 OPT_ROW_PREFETCH = 5
+OPT_COARSE_ENGINE = 6
+OPT_COARSE_TC_SLICE = 7
 DEFAULT_ROW_PREFETCH = 2
 
 
@@ -145,6 +147,19 @@ def set_coarse_mma_bits(bits: int, device: Optional[int] = None) -> None:
     """Operand type of the coarse correlator's tensor-core MMA: 16 (fp16,
     exact, the default) or 8 (int8)."""
     _lib.call("ab_ctx_set_option", _lib.ctx(device), OPT_COARSE_MMA_BITS, int(bits))
+
+
+def set_coarse_engine(engine: int, device: Optional[int] = None) -> None:
+    """Tensor-core path of the fp16 coarse correlator: 0 (default) tcgen05
+    from 9 antennas up and warp-level mma.sync below, 1 always mma.sync, 2
+    tcgen05 for any antenna count up to 32."""
+    _lib.call("ab_ctx_set_option", _lib.ctx(device), OPT_COARSE_ENGINE, int(engine))
+
+
+def set_coarse_tc_slice(samples: int, device: Optional[int] = None) -> None:
+    """Time samples one CTA of the tcgen05 coarse correlator sums (0: chosen
+    per call; else a multiple of 64 up to 131072)."""
+    _lib.call("ab_ctx_set_option", _lib.ctx(device), OPT_COARSE_TC_SLICE, int(samples))
 
 
 def set_row_prefetch(mode, device: Optional[int] = None) -> None:

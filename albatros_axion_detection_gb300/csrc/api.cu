@@ -307,6 +307,16 @@ int ab_ctx_set_option(ab_ctx* ctx, int32_t option, int32_t value) {
       AB_CHECK_ARG(value == 8 || value == 16, "ab_ctx_set_option: coarse MMA input bits must be 8 or 16");
       ctx->coarse_f16 = value == 16;
       return AB_OK;
+    case AB_OPT_COARSE_ENGINE:
+      AB_CHECK_ARG(value >= 0 && value <= 2,
+                   "ab_ctx_set_option: coarse engine must be 0 (auto), 1 (warp-level MMA) or 2 (tcgen05)");
+      ctx->coarse_engine = value;
+      return AB_OK;
+    case AB_OPT_COARSE_TC_SLICE:
+      AB_CHECK_ARG(value >= 0 && value % 64 == 0 && value <= (1 << 17),
+                   "ab_ctx_set_option: tensor-core slice must be 0 (auto) or a multiple of 64 up to 131072");
+      ctx->coarse_tc_slice = value;
+      return AB_OK;
     default:
       ab::set_error("ab_ctx_set_option: unknown option %d", option);
       return AB_ERR_ARG;

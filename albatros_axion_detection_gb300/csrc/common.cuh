@@ -82,6 +82,8 @@ struct ab_ctx {
   int fir_row_tile = 16;     // rows-per-thread class of the IIR / FIR time stage (16: 21 / 17 rows)
   int row_prefetch = 2;      // time-paired row stage: persistent + prefetch (1), + shared twiddles (2), one CTA per tile (0)
   bool coarse_f16 = true;    // coarse correlator on fp16 (exact) instead of int8 tensor-core MMA
+  int coarse_engine = 0;     // fp16 coarse correlator: 0 = tcgen05 from 9 antennas up, 1 = warp-level mma.sync, 2 = tcgen05
+  int coarse_tc_slice = 0;   // samples per CTA of the tcgen05 form (0: chosen per call)
   int row_ffts_per_cta = 8;  // row stage: 8 = time-paired spectra of one input per CTA;
                              // 4 or 2 = pol-paired spectra of one antenna per CTA
   // grow-only scratch buffers keyed by slot
@@ -110,5 +112,5 @@ int get_pair_table(ab_ctx* ctx, const FftPlan& p, const int2** out);
 int get_scratch(ab_ctx* ctx, int slot, size_t bytes, void** out);
 // Per-device constant tables of the FIR time stage (fir.cu).
 int fir_init_device();
-enum ScratchSlot { kScratchPfbW = 1, kScratchXcorrG = 2, kScratchChain = 3, kScratchYband = 4 };
+enum ScratchSlot { kScratchPfbW = 1, kScratchXcorrG = 2, kScratchChain = 3, kScratchYband = 4, kScratchFault = 5 };
 }  // namespace ab

@@ -389,11 +389,19 @@ __global__ void __launch_bounds__(kCcThreads)
   }
 }
 
+// fault: the tensor-core form's fault word (or null); when set, every output
+// of the call is INT64_MIN.
 __global__ void coarse_finalize_kernel(const long long* __restrict__ G, int Rp, int M, int ncols, int64_t nchunks,
-                                       int64_t* __restrict__ re, int64_t* __restrict__ im) {
+                                       int64_t* __restrict__ re, int64_t* __restrict__ im,
+                                       const int* __restrict__ fault) {
   int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   int64_t total = nchunks * M * M * ncols;
   if (idx >= total) return;
+  if (fault && *fault) {
+    re[idx] = INT64_MIN;
+    im[idx] = INT64_MIN;
+    return;
+  }
   int64_t k = idx % ncols;
   int64_t r = idx / ncols;
   int j = (int)(r % M);
@@ -474,6 +482,10 @@ extern "C" int ab_avg_xcorr_all_ant(const float* x, int64_t nant, int64_t npol, 
 }
 
 namespace ab {
+int launch_coarse_tc(ab_ctx* ctx, const uint8_t* raw, int64_t ant_stride, int64_t nant, int64_t nchan,
+                     int64_t rowstart, int64_t nrows, const int32_t* rows, const int64_t* channels, int64_t ncols,
+                     int64_t chunk_rows, int Rp, long long* G, int* fault, cudaStream_t s);
+
 // Largest channel count of one coarse-correlator call (grid x stays far below
 // its limit, and the scratch size below cannot wrap).
 constexpr int64_t kCoarseMaxCols = 1 << 20;
@@ -492,6 +504,24 @@ int coarse_xcorr_run(ab_ctx* ctx, const uint8_t* raw, int64_t ant_stride, int64_
   const int64_t spc = (chunk_rows + slice - 1) / slice;
   size_t gbytes = sizeof(long long) * (size_t)(nchunks * ncols) * Rp * Rp;
   AB_CUDA(cudaMemsetAsync(G, 0, gbytes, s));
+  const int M = (int)(2 * nant);
+  // tensor-core (tcgen05) form: by default from 9 antennas up (where its
+  // 128-row tiles are mostly filled), on request for any count up to 32;
+  // only through a context (the allocation-free entry point keeps the
+  // warp-level form)
+  const int engine = ctx ? ctx->coarse_engine : 1;
+  if (ctx && ctx->coarse_f16 && nant <= 32 && (engine == 2 || (engine == 0 && nant >= 9))) {
+    void* fw = nullptr;
+    AB_TRY(get_scratch(ctx, kScratchFault, 256, &fw));
+    AB_CUDA(cudaMemsetAsync(fw, 0, sizeof(int), s));
+    AB_TRY(launch_coarse_tc(ctx, raw, ant_stride, nant, nchan, rowstart, nrows, rows, channels, ncols, chunk_rows,
+                            Rp, G, (int*)fw, s));
+    const int64_t total = nchunks * M * M * ncols;
+    coarse_finalize_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(G, Rp, M, (int)ncols, nchunks, out_re,
+                                                                           out_im, (const int*)fw);
+    AB_LAUNCH_CHECK();
+    return AB_OK;
+  }
   size_t smem = (size_t)FC * Rp * kCcPitch;
   AB_CHECK_ARG(nchunks * spc <= 0x7fffffff, "coarse xcorr: too many slices");
   dim3 grid((unsigned)((ncols + FC - 1) / FC), (unsigned)(nchunks * spc));
@@ -529,10 +559,9 @@ int coarse_xcorr_run(ab_ctx* ctx, const uint8_t* raw, int64_t ant_stride, int64_
   }
 #undef AB_CC
   AB_LAUNCH_CHECK();
-  const int M = (int)(2 * nant);
   int64_t total = nchunks * M * M * ncols;
   coarse_finalize_kernel<<<(unsigned)((total + 255) / 256), 256, 0, s>>>(G, Rp, M, (int)ncols, nchunks, out_re,
-                                                                         out_im);
+                                                                         out_im, nullptr);
   AB_LAUNCH_CHECK();
   return AB_OK;
 }

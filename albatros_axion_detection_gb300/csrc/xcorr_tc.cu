@@ -1,0 +1,392 @@
+// xcorr_tc.cu -- the all-baseline coarse correlator on the fifth-generation
+// tensor cores (tcgen05.mma, accumulators in tensor memory).
+//
+// Same Gram matrix as the warp-level forms in xcorr.cu: per channel, the
+// matrix A has one row per (antenna, pol, re|im) and one column per time
+// sample, G = A A^T, Re V_ij = G[r_i, r_j] + G[m_i, m_j] and
+// Im V_ij = G[m_i, r_j] - G[r_i, m_j] (the X X^H of
+// albatros_analysis/src/correlations/correlations_gpu.py:95-121, replacing the
+// cuBLAS CGEMM of albatros_analysis/src/correlations/cgemm_batch.cu:8-53).
+//
+// Exactness.  The decoded nibbles are integers in [-7, 8] (0x8 decodes to +8,
+// as in albatros_analysis/src/correlations/unpacking.c:187-202), exact in
+// fp16; products are at most 64, and a CTA sums at most kTcMaxSlice = 2^17
+// samples, so every partial sum is an integer below 2^23 and the fp32
+// accumulation in tensor memory is exact in any order.  The partials are
+// converted to int64 exactly and added into the per-chunk sums with int64
+// atomics (order-independent, bit-reproducible).
+//
+// Tiles.  A 128-row operand tile holds CPT channels' rows (CPT = 2 with 64
+// rows a channel for up to 16 antennas, CPT = 1 with 128 rows for up to 32);
+// the rows of absent antennas stay zero.  One MMA of M = N = 128, K = 16 runs
+// the tile against itself, accumulating the 128 x 128 fp32 product in 128
+// tensor-memory columns; the channel blocks on its diagonal are the Gram
+// matrices.  A CTA owns kTcTiles tiles (4 * CPT channels, all 512 columns of
+// tensor memory) and a slice of time samples.
+//
+// Pipeline (one CTA per SM):
+//   * warps 0-7 produce: two groups of 4 warps take alternate stages of
+//     kTcKt = 64 samples; a thread loads 8 consecutive samples of one
+//     antenna (16 or 8 bytes each: every selected channel's two pols),
+//     decodes the nibbles to fp16 with integer tricks (below) and writes
+//     whole 16-byte rows of 8 samples into the stage's K-major tiles in the
+//     128-byte swizzled layout; then fence.proxy.async and an mbarrier arrive;
+//   * warp 8 allocates the tensor memory, and its lane 0 waits for each full
+//     stage, issues 4 tiles x 4 k-steps of tcgen05.mma and commits to the
+//     stage's "empty" barrier, which frees the stage for the producers;
+//   * after the last stage a commit to the "done" barrier releases warps 0-3,
+//     which read their 32 tensor-memory lanes each (tcgen05.ld) and add the
+//     Gram entries into the int64 sums.
+// Every mbarrier wait is bounded (about 2 s of wall time); a thread whose wait
+// runs out sets the call's fault word, stops issuing work and drains, the
+// tensor memory is freed on every path, and the finalize kernel then writes
+// INT64_MIN to every output of the call (so a fault cannot pass for data).
+#include <cuda_fp16.h>
+
+#include "common.cuh"
+
+namespace ab {
+
+constexpr int kTcKt = 64;                          // samples per stage
+constexpr int kTcStages = 3;                       // stage ring
+constexpr int kTcTiles = 4;                        // 128-row tiles per CTA (4 x 128 TMEM columns)
+constexpr int kTcTileBytes = 128 * kTcKt * 2;      // 16 KB of fp16 per tile
+constexpr int kTcStageBytes = kTcTiles * kTcTileBytes;
+constexpr int kTcProducers = 256;                  // warps 0-7
+constexpr int kTcThreads = kTcProducers + 32;      // + the MMA / tensor-memory warp
+constexpr int kTcGroup = kTcProducers / 2;         // producer threads per stage
+constexpr int64_t kTcMaxSlice = 1 << 17;           // samples a CTA may sum (exactness bound)
+constexpr size_t kTcSmemBytes = (size_t)kTcStages * kTcStageBytes + 1024 /* alignment */ + 128 /* barriers */;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(bar) : "memory");
+}
+// Wait for the completion of the barrier phase with the given parity; false
+// when about 2 s pass first.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  const uint64_t t0 = globaltimer_ns();
+  for (;;) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (ok) return true;
+    if (globaltimer_ns() - t0 > 2000000000ull) return false;
+  }
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// Shared-memory matrix descriptor of a K-major operand in the 128-byte
+// swizzled layout: rows of 128 bytes (64 fp16 samples), 8-row atoms of 1024
+// bytes (stride-dimension offset), the leading-dimension offset unused (16
+// bytes), descriptor version 1, swizzle mode 2 (128 B).
+__device__ __forceinline__ uint64_t sw128_kmajor_desc(uint32_t saddr) {
+  return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
+         ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+
+// Instruction descriptor of kind::f16: fp32 accumulators, fp16 A and B, both
+// K-major, M = 128, N = 128.
+constexpr uint32_t kTcIdesc = (1u << 4) | ((128u >> 3) << 17) | ((128u >> 4) << 24);
+
+__device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(kTcIdesc), "r"(accumulate)
+      : "memory");
+}
+__device__ __forceinline__ void tc_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+// 32 consecutive fp32 columns of this warp's 32 tensor-memory lanes.
+__device__ __forceinline__ void tc_ld32(uint32_t taddr, float (&v)[32]) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+      "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
+}
+
+// Nibble-wise (v + 7) mod 16 of the 8 nibbles of w (no carries between
+// nibbles): the low 3 bits plus 7 carry into bit 3, which is then flipped by
+// the nibble's own bit 3.  The decoded level is then n - 7 for n = (v+7)&15
+// (v > 8 -> v - 16, else v).
+__device__ __forceinline__ uint32_t nib_plus7(uint32_t w) {
+  return ((w & 0x77777777u) + 0x77777777u) ^ (w & 0x88888888u);
+}
+// fp16 pair (n_lo - 7, n_hi - 7) from 4-bit fields n in the low bits of each
+// 16-bit half: 0x6400 | n is the fp16 value 1024 + n, and 1031 = 0x6407.
+__device__ __forceinline__ uint32_t nib_to_h2(uint32_t n2) {
+  uint32_t r;
+  const uint32_t x = (n2 & 0x000F000Fu) | 0x64006400u;
+  asm("sub.rn.f16x2 %0, %1, %2;" : "=r"(r) : "r"(x), "r"(0x64076407u));
+  return r;
+}
+
+// Byte offset of (row, 16-byte chunk c) in a 128-row K-major tile of 128-byte
+// rows with the 128-byte swizzle (chunk index XOR row mod 8).
+__device__ __forceinline__ uint32_t sw128_offset(int row, int c) {
+  return (uint32_t)(row * 128 + (((c ^ row) & 7) << 4));
+}
+
+template <int CPT>  // channels per 128-row tile: 2 (nant <= 16) or 1 (nant <= 32)
+__global__ void __launch_bounds__(kTcThreads, 1)
+    coarse_xcorr_tc_kernel(const uint8_t* __restrict__ raw, int64_t ant_stride, int64_t row_bytes, int nant,
+                           int64_t rowstart, int64_t nrows, const int32_t* __restrict__ rows,
+                           const int64_t* __restrict__ channels, int ncols, int64_t chunk_rows, int64_t slice,
+                           int64_t slices_per_chunk, int Rp, long long* __restrict__ G, int* __restrict__ fault) {
+  constexpr int CPC = kTcTiles * CPT;   // channels per CTA
+  constexpr int BPT = 2 * CPC;          // packet bytes per (antenna, sample): CPC channels x 2 pols
+  constexpr int WPT = BPT / 4;          // 32-bit words per (antenna, sample)
+  constexpr int ROWS = 128 / CPT;       // tile rows per channel
+  constexpr int NA = ROWS / 4;          // antennas a channel's rows can hold
+  extern __shared__ uint8_t smem_raw[];
+  // 1024-byte aligned stage ring (the swizzle atoms), then the barriers
+  const uint32_t raw_s = smem_u32(smem_raw);
+  const uint32_t pad = (1024u - (raw_s & 1023u)) & 1023u;
+  uint8_t* stages = smem_raw + pad;
+  const uint32_t stages_s = raw_s + pad;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(stages + kTcStages * kTcStageBytes);
+  const uint32_t bar_s = stages_s + kTcStages * kTcStageBytes;
+  auto full_bar = [&](int i) { return bar_s + 8u * (uint32_t)i; };
+  auto empty_bar = [&](int i) { return bar_s + 8u * (uint32_t)(kTcStages + i); };
+  const uint32_t done_bar = bar_s + 8u * (2 * kTcStages);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * kTcStages + 1);
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int c0 = blockIdx.x * CPC;
+  const int64_t chunk = blockIdx.y / slices_per_chunk;
+  const int64_t sl = blockIdx.y % slices_per_chunk;
+  const int64_t k_begin = chunk * chunk_rows + sl * slice;
+  const int64_t chunk_end = min((chunk + 1) * chunk_rows, nrows);
+  const int64_t k_end = min(k_begin + slice, chunk_end);
+  const int nst = k_end > k_begin ? (int)((k_end - k_begin + kTcKt - 1) / kTcKt) : 0;
+
+  // zero the stage ring once: rows of absent antennas and channels stay zero
+  for (int i = tid; i < kTcStages * kTcStageBytes / 16; i += kTcThreads)
+    reinterpret_cast<uint4*>(stages)[i] = make_uint4(0u, 0u, 0u, 0u);
+  if (tid == 0) {
+    for (int i = 0; i < kTcStages; i++) {
+      mbar_init(full_bar(i), kTcGroup);
+      mbar_init(empty_bar(i), 1);
+    }
+    mbar_init(done_bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == kTcProducers / 32) {  // the MMA warp owns the tensor memory
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(kTcTiles * 128));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // zeroed tiles visible to the tensor cores
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp < kTcProducers / 32) {
+    // ---------------- producers ----------------
+    const int g = tid / kTcGroup, pt = tid % kTcGroup;
+    // 16- or 8-byte packet loads need the CTA's channels contiguous and aligned
+    bool vec = ((uintptr_t)raw % 16 == 0) && ant_stride % 16 == 0 && row_bytes % 16 == 0 && c0 + CPC <= ncols;
+    if (vec) {
+      const int64_t ch0 = channels[c0];
+      vec = (2 * ch0) % BPT == 0;
+#pragma unroll
+      for (int j = 1; j < CPC; j++) vec = vec && channels[c0 + j] == ch0 + j;
+    }
+    bool ok = true;
+    for (int s = g; s < nst && ok; s += 2) {
+      const int slot = s % kTcStages, use = s / kTcStages;
+      if (use > 0 && !mbar_wait(empty_bar(slot), (uint32_t)((use - 1) & 1))) {
+        atomicExch(fault, 1);
+        ok = false;
+        break;
+      }
+      uint8_t* stage = stages + slot * kTcStageBytes;
+      const int64_t kt = k_begin + (int64_t)s * kTcKt;
+      for (int item = pt; item < NA * 8; item += kTcGroup) {
+        const int ant = item >> 3, kc = item & 7;
+        if (ant >= nant) continue;  // its rows stay zero
+        uint32_t w[8][WPT];
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+          const int64_t k = kt + 8 * kc + i;
+#pragma unroll
+          for (int q = 0; q < WPT; q++) w[i][q] = 0u;
+          if (k < k_end) {
+            const int64_t r = rows ? (int64_t)rows[(int64_t)ant * nrows + k] : rowstart + k;
+            const uint8_t* src = raw + (int64_t)ant * ant_stride + r * row_bytes;
+            if (vec) {
+              const uint8_t* p = src + 2 * channels[c0];
+              if constexpr (WPT == 4) {
+                const uint4 v = __ldg(reinterpret_cast<const uint4*>(p));
+                w[i][0] = v.x;
+                w[i][1] = v.y;
+                w[i][2] = v.z;
+                w[i][3] = v.w;
+              } else {
+                const uint2 v = __ldg(reinterpret_cast<const uint2*>(p));
+                w[i][0] = v.x;
+                w[i][1] = v.y;
+              }
+            } else {
+#pragma unroll
+              for (int j = 0; j < CPC; j++) {
+                uint32_t b2 = 0u;  // absent channel: nibble 0 decodes to 0
+                if (c0 + j < ncols) {
+                  const uint8_t* p = src + 2 * channels[c0 + j];
+                  b2 = (uint32_t)__ldg(p) | ((uint32_t)__ldg(p + 1) << 8);
+                }
+                w[i][j >> 1] |= b2 << (16 * (j & 1));
+              }
+            }
+          }
+#pragma unroll
+          for (int q = 0; q < WPT; q++) w[i][q] = nib_plus7(w[i][q]);
+        }
+        // byte b = 2 j + pol of channel j: high nibble -> row (.., re), low -> (.., im)
+#pragma unroll
+        for (int b = 0; b < BPT; b++) {
+          const int j = b >> 1, pol = b & 1;
+          const int tile = j / CPT, h = j % CPT;
+          const int row_re = h * ROWS + 4 * ant + 2 * pol;
+          const uint32_t sel = (uint32_t)(b & 3) * 0x1111u + 0x4400u;  // byte b%4 of each word -> bytes 0|1 and 2|3
+          uint32_t re[4], im[4];
+#pragma unroll
+          for (int m = 0; m < 4; m++) {
+            const uint32_t p = __byte_perm(w[2 * m][b >> 2], w[2 * m + 1][b >> 2], sel);
+            im[m] = nib_to_h2(p);
+            re[m] = nib_to_h2(p >> 4);
+          }
+          uint8_t* tb = stage + tile * kTcTileBytes;
+          *reinterpret_cast<uint4*>(tb + sw128_offset(row_re, kc)) = make_uint4(re[0], re[1], re[2], re[3]);
+          *reinterpret_cast<uint4*>(tb + sw128_offset(row_re + 1, kc)) = make_uint4(im[0], im[1], im[2], im[3]);
+        }
+      }
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      mbar_arrive(full_bar(slot));
+    }
+  } else if (lane == 0) {
+    // ---------------- MMA issuer ----------------
+    for (int s = 0; s < nst; s++) {
+      const int slot = s % kTcStages, use = s / kTcStages;
+      if (!mbar_wait(full_bar(slot), (uint32_t)(use & 1))) {
+        atomicExch(fault, 1);
+        break;
+      }
+      tc_fence_after();
+      const uint32_t st = stages_s + slot * kTcStageBytes;
+#pragma unroll
+      for (int t = 0; t < kTcTiles; t++) {
+#pragma unroll
+        for (int kk = 0; kk < kTcKt / 16; kk++) {
+          const uint64_t d = sw128_kmajor_desc(st + t * kTcTileBytes + kk * 32);
+          tc_mma(tmem + 128u * t, d, d, (s > 0 || kk > 0) ? 1u : 0u);
+        }
+      }
+      tc_commit(empty_bar(slot));
+    }
+    tc_commit(done_bar);  // arrives once every MMA issued above has completed
+  }
+
+  // ---------------- epilogue: warps 0-3 read lanes 32w .. 32w+31 ----------------
+  if (warp < 4) {
+    const bool done = nst > 0 && mbar_wait(done_bar, 0u);
+    if (nst > 0 && !done) atomicExch(fault, 1);
+    tc_fence_after();
+    if (done) {
+      const int row = 32 * warp + lane;  // tensor-memory lane = row of the tile
+      const int h = row / ROWS, rr = row % ROWS;
+      const int R = 4 * nant;
+#pragma unroll 1
+      for (int t = 0; t < kTcTiles; t++) {
+        const int ch = c0 + t * CPT + h;
+#pragma unroll 1
+        for (int cb = 0; cb < ROWS; cb += 32) {
+          float v[32];
+          // every lane of the warp takes part in the load, whatever its row
+          tc_ld32(tmem + ((uint32_t)(32 * warp) << 16) + 128u * t + (uint32_t)(h * ROWS + cb), v);
+          if (ch < ncols && rr < R) {
+            long long* Gr = G + (((int64_t)chunk * ncols + ch) * Rp + rr) * Rp;
+#pragma unroll
+            for (int c = 0; c < 32; c++)
+              if (cb + c < R) atomicAdd((unsigned long long*)&Gr[cb + c], (unsigned long long)__float2ll_rn(v[c]));
+          }
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == kTcProducers / 32) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcTiles * 128));
+  }
+}
+
+// Launch the tensor-core form for 1 <= nant <= 32 into G (zeroed by the
+// caller, stride Rp >= 4*nant); *fault must be zero before the launch.
+int launch_coarse_tc(ab_ctx* ctx, const uint8_t* raw, int64_t ant_stride, int64_t nant, int64_t nchan,
+                     int64_t rowstart, int64_t nrows, const int32_t* rows, const int64_t* channels, int64_t ncols,
+                     int64_t chunk_rows, int Rp, long long* G, int* fault, cudaStream_t s) {
+  AB_CHECK_ARG(nant >= 1 && nant <= 32 && 4 * nant <= Rp, "coarse xcorr (tensor cores): nant %lld unsupported",
+               (long long)nant);
+  AB_CHECK_ARG(kTcSmemBytes <= ctx->smem_optin, "coarse xcorr (tensor cores): %zu bytes of shared memory needed",
+               kTcSmemBytes);
+  const int cpt = nant <= 16 ? 2 : 1;
+  const int64_t cpc = (int64_t)kTcTiles * cpt;
+  const int64_t groups = (ncols + cpc - 1) / cpc;
+  const int64_t nchunks = (nrows + chunk_rows - 1) / chunk_rows;
+  // about four CTAs per SM in total, slices of whole stages, at most kTcMaxSlice samples
+  int64_t per = std::max<int64_t>(1, (4 * (int64_t)ctx->num_sms + groups * nchunks - 1) / (groups * nchunks));
+  int64_t slice = (chunk_rows + per - 1) / per;
+  slice = std::min<int64_t>(std::max<int64_t>((slice + kTcKt - 1) / kTcKt * kTcKt, kTcKt), kTcMaxSlice);
+  if (ctx->coarse_tc_slice > 0) slice = ctx->coarse_tc_slice;
+  const int64_t spc = (chunk_rows + slice - 1) / slice;
+  AB_CHECK_ARG(groups <= 0x7fffffff && nchunks * spc <= 65535,
+               "coarse xcorr (tensor cores): %lld chunks x %lld slices exceed the grid limit; use larger chunks",
+               (long long)nchunks, (long long)spc);
+  dim3 grid((unsigned)groups, (unsigned)(nchunks * spc));
+  if (cpt == 2) {
+    AB_CUDA(cudaFuncSetAttribute(coarse_xcorr_tc_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)kTcSmemBytes));
+    coarse_xcorr_tc_kernel<2><<<grid, kTcThreads, kTcSmemBytes, s>>>(raw, ant_stride, 2 * nchan, (int)nant, rowstart,
+                                                                     nrows, rows, channels, (int)ncols, chunk_rows,
+                                                                     slice, spc, Rp, G, fault);
+  } else {
+    AB_CUDA(cudaFuncSetAttribute(coarse_xcorr_tc_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)kTcSmemBytes));
+    coarse_xcorr_tc_kernel<1><<<grid, kTcThreads, kTcSmemBytes, s>>>(raw, ant_stride, 2 * nchan, (int)nant, rowstart,
+                                                                     nrows, rows, channels, (int)ncols, chunk_rows,
+                                                                     slice, spc, Rp, G, fault);
+  }
+  AB_LAUNCH_CHECK();
+  return AB_OK;
+}
+
+}  // namespace ab

@@ -543,8 +543,9 @@ def _line(metric, value, unit, ms, args, workload, extra):
 
 
 def run_coarse(args, nant, nchan, nspec, chunk, workload):
-    """Exact all-baseline coarse correlation of 4-bit packets (tensor-core MMA
-    on fp16 operands, or int8 with --mma-bits 8; int64 sums): configurations
+    """Exact all-baseline coarse correlation of 4-bit packets (fp16 operands
+    on the tcgen05 tensor cores from 9 antennas up, warp-level mma.sync
+    below, or int8 mma.sync with --mma-bits 8; int64 sums): configurations
     'plain unpack + xcorr' and 'many-antenna coarse correlator'."""
     import torch
     from albatros_axion_detection_gb300 import correlations
@@ -589,7 +590,9 @@ def run_coarse(args, nant, nchan, nspec, chunk, workload):
            "e2e": {"value": spectra / (ms_e2e / 1e3), "unit": "spectra/s", "ms_per_step": ms_e2e,
                    "h2d_bytes_per_step": int(bytes_in), "d2h_bytes_per_step": int(out_re.numel() * 16)},
            "roofline": {"bound": "hbm",
-                        "kernel": "coarse_xcorr_kernel" if args.mma_bits == 8 else "coarse_xcorr_f16_kernel",
+                        "kernel": ("coarse_xcorr_kernel (int8 mma.sync)" if args.mma_bits == 8 else
+                                   "coarse_xcorr_tc_kernel (tcgen05)" if 9 <= nant <= 32 else
+                                   "coarse_xcorr_f16_kernel (fp16 mma.sync)"),
                         "achieved": achieved, "peak": peak,
                         "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
                         "int_macs_per_s_unique_pairs": macs / (ms / 1e3)},

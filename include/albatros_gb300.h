@@ -84,6 +84,16 @@ int ab_ctx_set_time_filter(ab_ctx *ctx, int32_t mode, int32_t row_tile);
  * 4-byte multiples); 2 (default) does the same with the FFT twiddles copied
  * into shared memory once per CTA; 0 launches one CTA per tile. */
 #define AB_OPT_ROW_PREFETCH 5
+/* AB_OPT_COARSE_ENGINE: tensor-core path of the fp16 coarse correlator.
+ * 0 (default): fifth-generation tensor cores (tcgen05.mma, accumulators in
+ * tensor memory) for 9 to 32 antennas, warp-level mma.sync below; 1: always
+ * warp-level mma.sync; 2: tcgen05 for any count up to 32.  Both are exact. */
+#define AB_OPT_COARSE_ENGINE 6
+/* AB_OPT_COARSE_TC_SLICE: time samples one CTA of the tcgen05 form sums
+ * before adding into the int64 totals: 0 (default) chooses per call (about
+ * four CTAs per SM), else a multiple of 64 up to 131072 (the largest for
+ * which every fp32 partial sum stays an exact integer). */
+#define AB_OPT_COARSE_TC_SLICE 7
 int ab_ctx_set_option(ab_ctx *ctx, int32_t option, int32_t value);
 
 /* ---- unpacking ----------------------------------------------------------

@@ -118,6 +118,68 @@ def test_coarse_xcorr_rejects_oversized_channel_counts():
     assert rc == -1 and b"too large" in lib.ab_last_error()
 
 
+@pytest.fixture
+def tc_engine():
+    """Force the tcgen05 form of the coarse correlator for any antenna count."""
+    from albatros_axion_detection_gb300 import autotune
+    autotune.set_coarse_mma_bits(16)
+    autotune.set_coarse_engine(2)
+    yield
+    autotune.set_coarse_engine(0)
+    autotune.set_coarse_tc_slice(0)
+
+
+@pytest.mark.parametrize("nant,nspec,nchan,chunk,ch", [
+    (16, 4096, 256, None, "all"),       # 2 channels a tile, 32 channel groups, contiguous 16-byte loads
+    (32, 1000, 12, 300, "all"),         # 1 channel a tile (128 rows), ragged chunks and slices
+    (2, 2 ** 14, 64, 2 ** 12, "step3"),  # scattered channels: byte loads; most rows zero
+    (13, 777, 20, None, "all"),         # ragged channel group (20 = 2 x 8 + 4), odd sample count
+    (1, 333, 5, 100, "all"),
+])
+def test_coarse_xcorr_tcgen05_bit_exact(tc_engine, nant, nspec, nchan, chunk, ch):
+    from albatros_axion_detection_gb300.correlations import xcorr_coarse_4bit
+    raw = gen.raw_4bit_uniform(seed=7 * nant + nchan, nspec=nspec, nchan=nchan, nant=nant)
+    chans = np.arange(nchan) if ch == "all" else np.arange(0, nchan, 3)
+    re, im = xcorr_coarse_4bit(cu(raw), 0, nspec, chans, nchan, chunk=chunk, average=False)
+    re, im = re.cpu().numpy(), im.cpu().numpy()
+    c = nspec if chunk is None else chunk
+    for k in range(re.shape[0]):
+        r0, r1 = k * c, min((k + 1) * c, nspec)
+        er, ei = io.xcorr_all_ant_4bit(raw, r0, r1, chans, nchan, nthreads=8)
+        np.testing.assert_array_equal(re[k], er)
+        np.testing.assert_array_equal(im[k], ei)
+
+
+def test_coarse_xcorr_tcgen05_longest_slice_exact(tc_engine):
+    """All nibbles 0x8 (+8) over one CTA slice of 2^17 samples, the longest the
+    tcgen05 form allows: every fp32 partial sum reaches 64 * 2^17 = 2^23 and
+    must stay exact in tensor memory."""
+    from albatros_axion_detection_gb300 import autotune
+    from albatros_axion_detection_gb300.correlations import xcorr_coarse_4bit
+    autotune.set_coarse_tc_slice(1 << 17)
+    nspec = 1 << 17
+    raw = np.full((2, nspec, 8), 0x88, np.uint8)
+    re, im = xcorr_coarse_4bit(cu(raw), 0, nspec, np.arange(4), 4, average=False)
+    assert np.all(re.cpu().numpy() == nspec * 128) and np.all(im.cpu().numpy() == 0)
+    # a mixed pattern at the same length: bit-exact against the int64 oracle
+    raw = gen.raw_4bit_uniform(seed=17, nspec=nspec, nchan=4, nant=2)
+    re, im = xcorr_coarse_4bit(cu(raw), 0, nspec, np.arange(4), 4, average=False)
+    er, ei = io.xcorr_all_ant_4bit(raw, 0, nspec, np.arange(4), 4)
+    np.testing.assert_array_equal(re.cpu().numpy()[0], er)
+    np.testing.assert_array_equal(im.cpu().numpy()[0], ei)
+
+
+def test_coarse_xcorr_tcgen05_row_lists(tc_engine):
+    from albatros_axion_detection_gb300.correlations import xcorr_coarse_4bit
+    raw = gen.raw_4bit(seed=3, nspec=700, nchan=32, nant=2)
+    rows = np.stack([np.arange(0, 600), np.arange(100, 700)]).astype(np.int32)
+    re, im = xcorr_coarse_4bit(cu(raw), 0, 0, np.arange(32), 32, rows=rows, average=False)
+    shifted = np.stack([raw[0, 0:600], raw[1, 100:700]])
+    er, ei = io.xcorr_all_ant_4bit(shifted, 0, 600, np.arange(32), 32)
+    np.testing.assert_array_equal(re.cpu().numpy()[0], er)
+    np.testing.assert_array_equal(im.cpu().numpy()[0], ei)
+
+
 def test_coarse_xcorr_worst_case_magnitudes(mma_bits):
     """All nibbles 0x8 (+8): the largest products, exact in the int32 / fp32
     partial sums (4096 samples x 64 per CTA slice)."""
