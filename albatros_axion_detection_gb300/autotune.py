@@ -140,6 +140,7 @@ OPT_COARSE_MMA_BITS = 3
 OPT_ROW_PREFETCH = 5
 OPT_COARSE_ENGINE = 6
 OPT_COARSE_TC_SLICE = 7
+OPT_PFB_TMA = 9
 DEFAULT_ROW_PREFETCH = 2
 
 
@@ -160,6 +161,12 @@ def set_coarse_tc_slice(samples: int, device: Optional[int] = None) -> None:
     """Time samples one CTA of the tcgen05 coarse correlator sums (0: chosen
     per call; else a multiple of 64 up to 131072)."""
     _lib.call("ab_ctx_set_option", _lib.ctx(device), OPT_COARSE_TC_SLICE, int(samples))
+
+
+def set_pfb_tma(on: int, device: Optional[int] = None) -> None:
+    """Streaming PFB band DFT: persistent CTAs with TMA-staged W tiles (1,
+    default) or one CTA per tile with plain loads (0); same arithmetic."""
+    _lib.call("ab_ctx_set_option", _lib.ctx(device), OPT_PFB_TMA, int(on))
 
 
 def set_row_prefetch(mode, device: Optional[int] = None) -> None:

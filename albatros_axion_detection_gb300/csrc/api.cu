@@ -3,9 +3,49 @@
 #include <stdarg.h>
 #include <string.h>
 
+#include <cudaTypedefs.h>
+
+#include "async.cuh"
 #include "common.cuh"
 
 namespace ab {
+
+// The driver's tensor-map encoder, looked up once through the runtime.
+static PFN_cuTensorMapEncodeTiled_v12000 tmap_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  });
+  return fn;
+}
+
+int encode_tmap(CUtensorMap* map, CUtensorMapDataType dtype, int rank, const void* base, const uint64_t* dims,
+                const uint64_t* strides, const uint32_t* box) {
+  auto fn = tmap_encoder();
+  if (!fn) {
+    set_error("tensor map: the driver's cuTensorMapEncodeTiled is not available");
+    return AB_ERR_UNSUPPORTED;
+  }
+  cuuint64_t gd[3], gs[2];
+  cuuint32_t bx[3], es[3] = {1, 1, 1};
+  for (int i = 0; i < rank; i++) {
+    gd[i] = dims[i];
+    bx[i] = box[i];
+  }
+  for (int i = 0; i + 1 < rank; i++) gs[i] = strides[i];
+  CUresult r = fn(map, dtype, (cuuint32_t)rank, const_cast<void*>(base), gd, gs, bx, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                  CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    set_error("tensor map: cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return AB_ERR_ARG;
+  }
+  return AB_OK;
+}
 
 static thread_local char g_err[512] = "";
 
@@ -311,6 +351,10 @@ int ab_ctx_set_option(ab_ctx* ctx, int32_t option, int32_t value) {
       AB_CHECK_ARG(value >= 0 && value <= 2,
                    "ab_ctx_set_option: coarse engine must be 0 (auto), 1 (warp-level MMA) or 2 (tcgen05)");
       ctx->coarse_engine = value;
+      return AB_OK;
+    case AB_OPT_PFB_TMA:
+      AB_CHECK_ARG(value == 0 || value == 1, "ab_ctx_set_option: PFB TMA staging must be 0 or 1");
+      ctx->pfb_tma = value;
       return AB_OK;
     case AB_OPT_COARSE_TC_SLICE:
       AB_CHECK_ARG(value >= 0 && value % 64 == 0 && value <= (1 << 17),

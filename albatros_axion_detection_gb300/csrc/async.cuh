@@ -1,0 +1,81 @@
+// async.cuh -- asynchronous copies and their barriers: mbarrier wait with a
+// wall-time bound, TMA (cp.async.bulk.tensor) tile loads, and the host-side
+// encoding of the tensor maps they read.  Shared by the PFB band DFT
+// (pfb.cu) and the tcgen05 coarse correlator (xcorr_tc.cu).
+#pragma once
+#include <cuda.h>  // CUtensorMap and its enums (types only; the encoder comes through the runtime)
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace ab {
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_init_fence() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(bar) : "memory");
+}
+// Arrive and announce `bytes` of asynchronous copies that complete on `bar`.
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(bar),
+               "r"(bytes)
+               : "memory");
+}
+// Wait for the completion of the barrier phase with the given parity; false
+// when about 2 s of wall time pass first.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  const uint64_t t0 = globaltimer_ns();
+  for (;;) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (ok) return true;
+    if (globaltimer_ns() - t0 > 2000000000ull) return false;
+  }
+}
+
+// Order this thread's earlier generic-proxy shared-memory accesses before
+// later asynchronous-proxy ones (TMA, tensor cores).
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// One box of a 2-D tiled tensor map into shared memory at dst (128-byte
+// aligned), completing on the mbarrier bar.  x is the innermost coordinate
+// (elements); x * element size must be a multiple of 16 bytes.
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::
+          "r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
+      : "memory");
+}
+// Same for a 3-D map (x innermost, then y, then z).
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map, int x, int y, int z, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+      "[%5];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(bar)
+      : "memory");
+}
+
+// Host: encode a tiled tensor map of `rank` (2 or 3) dimensions over
+// `base`: dims[0] innermost (contiguous), strides[i] the byte stride of
+// dimension i+1, box[] the tile, no swizzle, no interleave, 128-byte L2
+// promotion, zero fill outside the tensor.  The driver's encoder is reached
+// through the runtime (no link against the driver library).  Returns an
+// AB_* status.
+int encode_tmap(CUtensorMap* map, CUtensorMapDataType dtype, int rank, const void* base, const uint64_t* dims,
+                const uint64_t* strides, const uint32_t* box);
+
+}  // namespace ab

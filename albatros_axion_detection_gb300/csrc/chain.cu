@@ -32,7 +32,7 @@
 
 namespace ab {
 int launch_xcorr_accum(const float2* Y, int M, int64_t nb, int64_t F, int64_t b_lo, int64_t b_hi, float2* vis,
-                       float scale, cudaStream_t s);
+                       float scale, cudaStream_t s, const int* fault);
 }
 
 using namespace ab;
@@ -60,6 +60,7 @@ struct ab_stream {
   float* W = nullptr;
   float2* Y = nullptr;
   float2* vis = nullptr;
+  int* d_fault = nullptr;    // set by a stage whose asynchronous copies did not arrive; vis is then NaN
   bool owns_scratch = true;  // interm[0], W, Y allocated here (not a shared workspace)
   int64_t nb_max = 0;
   int64_t chunks_done = 0;  // next chunk expected
@@ -87,6 +88,7 @@ static void stream_free(ab_stream* st) {
   cudaFree(st->interm[1]);
   cudaFree(st->state);
   cudaFree(st->vis);
+  cudaFree(st->d_fault);
 }
 
 // Per-push scratch of a fused stream, as carved from one workspace: the IPFB
@@ -230,6 +232,7 @@ extern "C" int ab_stream_create(ab_ctx* ctx, int64_t nant, int64_t nchan_raw, in
   AB_ALLOC(st->W, sizeof(float) * (size_t)M * st->nb_max * L);
   AB_ALLOC(st->Y, sizeof(float2) * (size_t)M * st->nb_max * st->nq);
   AB_ALLOC(st->vis, sizeof(float2) * (size_t)std::max<int64_t>(njobs, 1) * M * M * st->nq);
+  AB_ALLOC(st->d_fault, sizeof(int));
   std::vector<int32_t> hc(nsel), ha(nsel);
   for (int64_t k = 0; k < nsel; k++) {
     hc[k] = (int32_t)chan_cols[k];
@@ -245,6 +248,7 @@ extern "C" int ab_stream_create(ab_ctx* ctx, int64_t nant, int64_t nchan_raw, in
             cudaMemcpy(st->d_wtaps, wf.data(), sizeof(float) * wf.size(), cudaMemcpyHostToDevice) == cudaSuccess &&
             cudaMemcpy(st->d_win, wl.data(), sizeof(float) * wl.size(), cudaMemcpyHostToDevice) == cudaSuccess &&
             cudaMemset(st->vis, 0, sizeof(float2) * (size_t)std::max<int64_t>(njobs, 1) * M * M * st->nq) == cudaSuccess &&
+            cudaMemset(st->d_fault, 0, sizeof(int)) == cudaSuccess &&
             (!st->fused || cudaMemset(st->state, 0, sizeof(float) * (size_t)2 * M * P * 4 * osamp) == cudaSuccess);
   if (!ok) {
     set_error("ab_stream_create: upload failed");
@@ -272,6 +276,7 @@ extern "C" int ab_stream_reset(ab_stream* st, void* stream) {
                           as_stream(stream)));
   if (st->fused)
     AB_CUDA(cudaMemsetAsync(st->state, 0, sizeof(float) * (size_t)2 * st->M * st->P * 4 * st->O, as_stream(stream)));
+  AB_CUDA(cudaMemsetAsync(st->d_fault, 0, sizeof(int), as_stream(stream)));
   return AB_OK;
 }
 
@@ -441,7 +446,7 @@ static int stream_push(ab_stream* st, const uint8_t* raw, int64_t ant_stride, co
     {
       StageTimer t(st, s, 3);
       AB_TRY(launch_pfb_stage_b(st->ctx, st->W, M, P, O, nb, st->planP, st->twL, (int)(st->q0 / O), (int)(st->q1 / O),
-                                st->Y, s));
+                                st->Y, s, st->d_fault));
       t.done(1);
     }
     // correlate, split at job boundaries
@@ -453,7 +458,7 @@ static int stream_push(ab_stream* st, const uint8_t* raw, int64_t ant_stride, co
       int64_t job = b / st->nblock;
       int64_t jend = std::min(bend, (job + 1) * st->nblock);
       AB_TRY(launch_xcorr_accum(st->Y, M, nb, st->nq, b - bfirst, jend - bfirst,
-                                st->vis + job * (int64_t)M * M * st->nq, 1.0f / (float)st->nblock, s));
+                                st->vis + job * (int64_t)M * M * st->nq, 1.0f / (float)st->nblock, s, st->d_fault));
       nx++;
       b = jend;
     }

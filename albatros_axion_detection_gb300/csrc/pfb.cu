@@ -2,8 +2,10 @@
 //   y[b, k] = sum_{i<ntap} ts[(b+i) L + k] win[i L + k];  out[b] = rfft(y[b])
 // computed as stage A (tap fold + O-point real DFT over t', k = n + P t')
 // and stage B (twiddle + P-point DFT over n), see pfb.cuh.
+#include <algorithm>
 #include <type_traits>
 
+#include "async.cuh"
 #include "fft_static.cuh"
 #include "pfb.cuh"
 
@@ -519,6 +521,133 @@ __global__ void __launch_bounds__(kBandThreads, 3)
   }
 }
 
+
+// Persistent TMA form of the two-slot band DFT.  One CTA of kBtThreads per SM
+// walks the (slot pair, block, input) tiles.  A tile's W records (4096 sample
+// phases x the 16 bytes its two slots share) arrive as 16 TMA boxes (4 floats
+// x 256 phases each) in a 64 KB landing tile and complete on one mbarrier;
+// once they are twiddled into the two FFT buffers the landing tile is free,
+// and the next tile's boxes are issued into it at once, so they arrive while
+// this tile's radix-16 passes and band outputs run.  The two slots' passes run
+// side by side, one per half of the CTA.  The arithmetic is that of
+// pfb_stage_band2_kernel.  A wait that runs out (about 2 s) sets *fault and
+// stops the CTA; the fine correlator then writes NaN into the visibilities.
+constexpr int kBtThreads = 512;
+
+__host__ __device__ inline size_t stage_band_tma_smem() {
+  return 1024 + (size_t)4096 * 16 + sizeof(float2) * (2 * (size_t)padded_len(4096) + 3 * 64 + 16 + 32) + 64;
+}
+
+__global__ void __launch_bounds__(kBtThreads, 1)
+    pfb_stage_band_tma_kernel(const __grid_constant__ CUtensorMap wmap, int O, int64_t nb, int ninputs,
+                              const float2* __restrict__ twL, const float2* __restrict__ tws, int u0, int u1,
+                              float2* __restrict__ out, int* __restrict__ fault) {
+  constexpr int P = 4096;
+  extern __shared__ uint8_t smb[];
+  const uint32_t raw_s = smem_u32(smb);
+  const uint32_t pad = (1024u - (raw_s & 1023u)) & 1023u;
+  float4* stage = reinterpret_cast<float4*>(smb + pad);  // [4096]: the pair's 4 floats of W per sample phase
+  const uint32_t stage_s = raw_s + pad;
+  float2* bufA = reinterpret_cast<float2*>(smb + pad + 4096 * 16);
+  float2* bufB = bufA + padded_len(P);
+  float2* t3 = bufB + padded_len(P);  // [64] w^(4096 i), [64] w^(64 i), [64] w^i
+  float2* w16 = t3 + 192;
+  float2* qtw = w16 + 16;             // [2][16] w_L^(256 s q) for the tile's two slots
+  uint64_t* barp = reinterpret_cast<uint64_t*>(qtw + 32);
+  int* abort_flag = reinterpret_cast<int*>(barp + 1);
+  const uint32_t bar = smem_u32(barp);
+  const int GW = O < 8 ? O : 8, NG = O / GW, NJ = O / 4;
+  const int L = P * O;
+  const int tid = threadIdx.x, half = tid >> 8, ht = tid & 255;
+  const int64_t ntile = (int64_t)NJ * nb * ninputs;
+  const int nu = u1 - u0;
+  if (tid < 192) {
+    const int d = tid >> 6, i = tid & 63;
+    const int64_t e = d == 0 ? (int64_t)i * 4096 : d == 1 ? (int64_t)i * 64 : i;
+    t3[tid] = e < L ? __ldg(&twL[e]) : make_float2(1.f, 0.f);
+  }
+  if (tid < 16) w16[tid] = __ldg(&twL[(int64_t)tid * (L / 16)]);
+  if (tid == 0) {
+    *abort_flag = 0;
+    mbar_init(bar, 1);
+    mbar_init_fence();
+  }
+  __syncthreads();
+  // the 16 boxes of tile t: x = the pair's first float in its 8-float group,
+  // y = the W row (((in nb + b) NG + g) P + n) of sample phase n = 256 r
+  auto issue = [&](int64_t t) {
+    const int j = (int)(t % NJ);
+    const int64_t rest = t / NJ, b = rest % nb, in = rest / nb;
+    const int g = (4 * j) / GW, e0 = (4 * j) % GW;
+    const int64_t row0 = ((in * nb + b) * NG + g) * P;
+    fence_proxy_async();
+    mbar_arrive_expect_tx(bar, 4096 * 16);
+#pragma unroll 1
+    for (int r = 0; r < 16; r++) tma_load_2d(stage_s + r * 256 * 16, &wmap, e0, (int)(row0 + 256 * r), bar);
+  };
+  if (tid == 0 && blockIdx.x < ntile) issue(blockIdx.x);
+  uint32_t phase = 0;
+  for (int64_t t = blockIdx.x; t < ntile; t += gridDim.x, phase ^= 1) {
+    const int j = (int)(t % NJ);
+    const int64_t rest = t / NJ, b = rest % nb, in = rest / nb;
+    const int sA = 2 * j, sB = 2 * j + 1;
+    if (tid < 32) {
+      const int s = tid < 16 ? sA : sB, q = tid & 15;
+      qtw[tid] = __ldg(&twL[((int64_t)s * 256 * q) % L]);
+    }
+    if (tid == 0 && !mbar_wait(bar, phase)) {
+      atomicExch(fault, 1);
+      *abort_flag = 1;
+    }
+    __syncthreads();
+    if (*abort_flag) break;
+    float2* ob = out + ((int64_t)in * nb + b) * ((int64_t)nu * O);
+    // twiddle both slots into their buffers: phases n = ht + 256 q, q in this half's 8
+    const float2 bA = tw3(t3, (int)(((int64_t)sA * ht) % L)), bB = tw3(t3, (int)(((int64_t)sB * ht) % L));
+    float wv[8];  // slot O/2 (the second real value of slot 0's record) when j == 0
+#pragma unroll
+    for (int qq = 0; qq < 8; qq++) {
+      const int q = 8 * half + qq, n = ht + 256 * q;
+      const float4 v = stage[n];
+      float2 xa = j == 0 ? make_float2(v.x, 0.f) : make_float2(v.x, v.y);  // slot 0: the real W_0
+      if (sA) xa = cmul(cmul(xa, bA), qtw[q]);
+      bufA[pidx(n)] = xa;
+      bufB[pidx(n)] = cmul(cmul(make_float2(v.z, v.w), bB), qtw[16 + q]);
+      wv[qq] = v.y;
+    }
+    __syncthreads();  // the landing tile is consumed: fetch the next tile into it
+    if (tid == 0 && t + gridDim.x < ntile) issue(t + gridDim.x);
+    float2* buf = half ? bufB : bufA;
+    spass<16, 256, 4096, 256, false>(buf, tws + Plan4096::tw_off(0), ht);
+    __syncthreads();
+    spass<16, 16, 4096, 256, false>(buf, tws + Plan4096::tw_off(1), ht);
+    __syncthreads();
+    if (half == 0) {
+      band_outputs(bufA, w16, u0, nu, false, sA, O, ob, ht);
+      if (sA != 0) band_outputs(bufA, w16, u0, nu, true, O - sA, O, ob, ht);
+    } else {
+      band_outputs(bufB, w16, u0, nu, false, sB, O, ob, ht);
+      band_outputs(bufB, w16, u0, nu, true, O - sB, O, ob, ht);
+    }
+    if (j == 0) {  // W_{O/2}: the pair holding slot 0 takes a third transform
+      const int sH = O / 2;
+      __syncthreads();
+#pragma unroll
+      for (int qq = 0; qq < 8; qq++) {
+        const int n = ht + 256 * (8 * half + qq);
+        bufA[pidx(n)] = cmul(make_float2(wv[qq], 0.f), tw3(t3, (int)(((int64_t)sH * n) % L)));
+      }
+      __syncthreads();
+      if (half == 0) spass<16, 256, 4096, 256, false>(bufA, tws + Plan4096::tw_off(0), ht);
+      __syncthreads();
+      if (half == 0) spass<16, 16, 4096, 256, false>(bufA, tws + Plan4096::tw_off(1), ht);
+      __syncthreads();
+      if (half == 0) band_outputs(bufA, w16, u0, nu, false, sH, O, ob, ht);
+    }
+    __syncthreads();  // buffers and slot twiddles are rewritten by the next tile
+  }
+}
+
 int launch_pfb_stage_a(const TsSrc& src, int ninputs, int P, int O, int ntap, int64_t row0, int64_t nb,
                        const float* win, float* W, const float2* tw64, cudaStream_t s) {
   AB_CHECK_ARG(P % kFoldCols == 0, "pfb: lblock/osamp %d must be a multiple of %d", P, kFoldCols);
@@ -555,13 +684,28 @@ int launch_pfb_stage_a(const TsSrc& src, int ninputs, int P, int O, int ntap, in
 }
 
 int launch_pfb_stage_b(ab_ctx* ctx, const float* W, int ninputs, int P, int O, int64_t nb, const FftPlan& planP,
-                       const float2* twL, int u0, int u1, float2* out, cudaStream_t s) {
+                       const float2* twL, int u0, int u1, float2* out, cudaStream_t s, int* fault) {
   if (nb <= 0) return AB_OK;
   const int GW = O < 8 ? O : 8;
   size_t smem = sizeof(float) * (size_t)P * GW + sizeof(float2) * ((size_t)padded_len(P) + smem_tw_len(P * O));
   AB_CHECK_ARG(smem <= 220 * 1024, "pfb: stage B needs %zu bytes of shared memory", smem);
   dim3 grid((unsigned)nb, (unsigned)(O / GW), (unsigned)ninputs);
-  if (P == Plan4096::N && O >= 4 && O <= 64 && nb <= 65535 && u1 >= 0 && ((uintptr_t)W & 15) == 0) {
+  const int64_t wrows = (int64_t)ninputs * nb * (O / GW) * P;
+  if (fault && ctx->pfb_tma && P == Plan4096::N && O >= 4 && O <= 64 && u1 >= 0 && ((uintptr_t)W & 15) == 0 &&
+      wrows < (1ll << 31) && stage_band_tma_smem() <= ctx->smem_optin) {
+    // W as a 2-D tensor: rows of GW floats (32 or 16 bytes), boxes of 4 floats x 256 rows
+    CUtensorMap map;
+    const uint64_t dims[2] = {(uint64_t)GW, (uint64_t)wrows}, strides[1] = {(uint64_t)GW * sizeof(float)};
+    const uint32_t box[2] = {4, 256};
+    AB_TRY(encode_tmap(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, W, dims, strides, box));
+    const float2* tws;
+    AB_TRY(get_twiddle_stream(ctx, P, {16, 16, 16}, &tws));
+    const size_t sm = stage_band_tma_smem();
+    AB_CUDA(cudaFuncSetAttribute(pfb_stage_band_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    const int64_t ntile = (int64_t)(O / 4) * nb * ninputs;
+    const unsigned g = (unsigned)std::min<int64_t>(ntile, std::max(ctx->num_sms, 1));
+    pfb_stage_band_tma_kernel<<<g, kBtThreads, sm, s>>>(map, O, nb, ninputs, twL, tws, u0, u1, out, fault);
+  } else if (P == Plan4096::N && O >= 4 && O <= 64 && nb <= 65535 && u1 >= 0 && ((uintptr_t)W & 15) == 0) {
     const float2* tws;
     AB_TRY(get_twiddle_stream(ctx, P, {16, 16, 16}, &tws));
     size_t sm = stage_band2_smem();
@@ -641,7 +785,7 @@ static int pfb_common(ab_ctx* ctx, const float* ts, int64_t nsamp, const float* 
   TsSrc src{ts, nullptr, 0, 0, 0, nsamp / P, 1};
   cudaStream_t s = as_stream(stream);
   AB_TRY(launch_pfb_stage_a(src, 1, P, O, (int)ntap, 0, nblock, win, (float*)Wv, ctx->tw64, s));
-  AB_TRY(launch_pfb_stage_b(ctx, (const float*)Wv, 1, P, O, nblock, planP, twL, u0, u1, (float2*)out, s));
+  AB_TRY(launch_pfb_stage_b(ctx, (const float*)Wv, 1, P, O, nblock, planP, twL, u0, u1, (float2*)out, s, nullptr));
   return AB_OK;
 }
 

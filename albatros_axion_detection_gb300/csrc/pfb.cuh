@@ -36,7 +36,9 @@ int launch_pfb_stage_a(const TsSrc& src, int ninputs, int P, int O, int ntap, in
 
 // Stage B.  band: u in [u0, u1), out[(in*nb + b)*(u1-u0)*O + (u-u0)*O + s];
 // full (u1 < 0): out[(in*nb + b)*(L/2+1) + q] for q <= L/2.
+// fault: a device word set when an asynchronous copy of the TMA form does not
+// arrive in time (the TMA form runs only when fault is given).
 int launch_pfb_stage_b(ab_ctx* ctx, const float* W, int ninputs, int P, int O, int64_t nb, const FftPlan& planP,
-                       const float2* twL, int u0, int u1, float2* out, cudaStream_t s);
+                       const float2* twL, int u0, int u1, float2* out, cudaStream_t s, int* fault = nullptr);
 
 }  // namespace ab

@@ -80,8 +80,10 @@ __global__ void __launch_bounds__(kXcThreads)
 // ---------------------------------------------------------------------------
 // Streaming chain accumulation: Y[in][b][f] (c64); for blocks [b_lo, b_hi)
 // vis[(i*M + j)*F + f] += scale * sum_b Y_i conj(Y_j), lower triangle mirrored.
+// fault (or null): set by an earlier stage whose asynchronous copies did not
+// arrive; the visibilities touched are then NaN.
 __global__ void xcorr_accum_kernel(const float2* __restrict__ Y, int M, int64_t nb, int64_t F, int64_t b_lo,
-                                   int64_t b_hi, float2* __restrict__ vis, float scale) {
+                                   int64_t b_hi, float2* __restrict__ vis, float scale, const int* __restrict__ fault) {
   const int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (f >= F) return;
   // pair index p -> (i, j), i <= j
@@ -100,6 +102,7 @@ __global__ void xcorr_accum_kernel(const float2* __restrict__ Y, int M, int64_t 
     acc.y = fmaf(a.y, c.x, fmaf(-a.x, c.y, acc.y));
   }
   acc = cscale(acc, scale);
+  if (fault && *fault) acc = make_float2(__int_as_float(0x7fc00000), __int_as_float(0x7fc00000));
   float2* v = vis + ((int64_t)i * M + j) * F + f;
   *v = cadd(*v, acc);
   if (i != j) {
@@ -117,7 +120,7 @@ constexpr int kXaF = 32, kXaG = 8;
 template <int M>
 __global__ void __launch_bounds__(kXaF * kXaG)
     xcorr_accum_small_kernel(const float2* __restrict__ Y, int64_t nb, int64_t F, int64_t b_lo, int64_t b_hi,
-                             float2* __restrict__ vis, float scale) {
+                             float2* __restrict__ vis, float scale, const int* __restrict__ fault) {
   constexpr int NP = M * (M + 1) / 2;
   __shared__ float2 part[kXaG][NP][kXaF];
   const int fl = threadIdx.x % kXaF, g = threadIdx.x / kXaF;
@@ -145,10 +148,12 @@ __global__ void __launch_bounds__(kXaF * kXaG)
   for (int p = 0; p < NP; p++) part[g][p][fl] = acc[p];
   __syncthreads();
   if (f >= F) return;
+  const bool bad = fault && *fault;
   for (int p = g; p < NP; p += kXaG) {
     float2 t = part[0][p][fl];
     for (int q = 1; q < kXaG; q++) t = cadd(t, part[q][p][fl]);
     t = cscale(t, scale);
+    if (bad) t = make_float2(__int_as_float(0x7fc00000), __int_as_float(0x7fc00000));
     int i = 0, r = p;
     while (r >= M - i) {
       r -= M - i;
@@ -165,16 +170,16 @@ __global__ void __launch_bounds__(kXaF * kXaG)
 }
 
 int launch_xcorr_accum(const float2* Y, int M, int64_t nb, int64_t F, int64_t b_lo, int64_t b_hi, float2* vis,
-                       float scale, cudaStream_t s) {
+                       float scale, cudaStream_t s, const int* fault) {
   if (b_hi <= b_lo) return AB_OK;
   const dim3 gs((unsigned)((F + kXaF - 1) / kXaF));
   switch (M) {
-    case 2: xcorr_accum_small_kernel<2><<<gs, kXaF * kXaG, 0, s>>>(Y, nb, F, b_lo, b_hi, vis, scale); break;
-    case 4: xcorr_accum_small_kernel<4><<<gs, kXaF * kXaG, 0, s>>>(Y, nb, F, b_lo, b_hi, vis, scale); break;
-    case 6: xcorr_accum_small_kernel<6><<<gs, kXaF * kXaG, 0, s>>>(Y, nb, F, b_lo, b_hi, vis, scale); break;
+    case 2: xcorr_accum_small_kernel<2><<<gs, kXaF * kXaG, 0, s>>>(Y, nb, F, b_lo, b_hi, vis, scale, fault); break;
+    case 4: xcorr_accum_small_kernel<4><<<gs, kXaF * kXaG, 0, s>>>(Y, nb, F, b_lo, b_hi, vis, scale, fault); break;
+    case 6: xcorr_accum_small_kernel<6><<<gs, kXaF * kXaG, 0, s>>>(Y, nb, F, b_lo, b_hi, vis, scale, fault); break;
     default: {
       dim3 grid((unsigned)((F + 127) / 128), (unsigned)(M * (M + 1) / 2));
-      xcorr_accum_kernel<<<grid, 128, 0, s>>>(Y, M, nb, F, b_lo, b_hi, vis, scale);
+      xcorr_accum_kernel<<<grid, 128, 0, s>>>(Y, M, nb, F, b_lo, b_hi, vis, scale, fault);
     }
   }
   AB_LAUNCH_CHECK();

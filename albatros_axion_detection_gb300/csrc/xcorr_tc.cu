@@ -43,6 +43,7 @@
 // INT64_MIN to every output of the call (so a fault cannot pass for data).
 #include <cuda_fp16.h>
 
+#include "async.cuh"
 #include "common.cuh"
 
 namespace ab {
@@ -57,36 +58,6 @@ constexpr int kTcThreads = kTcProducers + 32;      // + the MMA / tensor-memory 
 constexpr int kTcGroup = kTcProducers / 2;         // producer threads per stage
 constexpr int64_t kTcMaxSlice = 1 << 17;           // samples a CTA may sum (exactness bound)
 constexpr size_t kTcSmemBytes = (size_t)kTcStages * kTcStageBytes + 1024 /* alignment */ + 128 /* barriers */;
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ uint64_t globaltimer_ns() {
-  uint64_t t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
-
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
-  asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(bar) : "memory");
-}
-// Wait for the completion of the barrier phase with the given parity; false
-// when about 2 s pass first.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
-  const uint64_t t0 = globaltimer_ns();
-  for (;;) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    if (ok) return true;
-    if (globaltimer_ns() - t0 > 2000000000ull) return false;
-  }
-}
 
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
@@ -195,7 +166,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       mbar_init(empty_bar(i), 1);
     }
     mbar_init(done_bar, 1);
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    mbar_init_fence();
   }
   if (warp == kTcProducers / 32) {  // the MMA warp owns the tensor memory
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),

@@ -203,6 +203,9 @@ def run_ours(args):
     if args.row_prefetch >= 0:
         from albatros_axion_detection_gb300 import autotune
         autotune.set_row_prefetch(args.row_prefetch)
+    if args.pfb_tma >= 0:
+        from albatros_axion_detection_gb300 import autotune
+        autotune.set_pfb_tma(args.pfb_tma)
     if args.time_filter != "default" or args.row_tile:
         from albatros_axion_detection_gb300 import autotune
         mode = {"iir": 0, "fir": 3, "fft": 1}.get(args.time_filter, autotune.DEFAULT_MODE)
@@ -699,6 +702,8 @@ def main():
                     help="stream: IPFB time stage form (default: the library's choice)")
     ap.add_argument("--row-tile", type=int, default=0, help="stream: IIR / FIR row tile (16 or 32)")
     ap.add_argument("--row-ffts", type=int, default=0, help="stream: spectra per row-stage CTA (8, 4 or 2)")
+    ap.add_argument("--pfb-tma", type=int, default=-1,
+                    help="stream: PFB band DFT with TMA-staged tiles (1, default) or plain loads (0)")
     ap.add_argument("--row-prefetch", type=int, default=-1,
                     help="stream: row stage 0 = one CTA per tile, 1 = persistent prefetching, "
                          "2 (default) = + shared twiddles")
