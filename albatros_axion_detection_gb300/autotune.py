@@ -164,8 +164,9 @@ def set_coarse_tc_slice(samples: int, device: Optional[int] = None) -> None:
 
 
 def set_pfb_tma(on: int, device: Optional[int] = None) -> None:
-    """Streaming PFB band DFT: persistent CTAs with TMA-staged W tiles (1,
-    default) or one CTA per tile with plain loads (0); same arithmetic."""
+    """Streaming PFB band DFT: plain loads (0, default), W tiles staged by
+    TMA into each CTA's FFT buffers (1), or persistent CTAs fetching the next
+    tile with TMA (2); the same arithmetic."""
     _lib.call("ab_ctx_set_option", _lib.ctx(device), OPT_PFB_TMA, int(on))
 
 

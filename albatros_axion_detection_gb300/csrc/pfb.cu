@@ -648,6 +648,112 @@ __global__ void __launch_bounds__(kBtThreads, 1)
   }
 }
 
+
+// TMA form with three CTAs per SM: one CTA per tile as pfb_stage_band2_kernel,
+// whose 16 TMA boxes land in the space of its two FFT buffers (64 KB of the
+// 69.6 KB); each thread reads its 16 records from there into registers, and
+// after a barrier writes the twiddled values over them.  The other two CTAs
+// of the SM transform while a CTA's boxes are in flight.  A wait that runs
+// out (about 2 s) sets *fault; the CTA then writes nothing.
+__host__ __device__ inline size_t stage_band2_tma_smem() { return 1024 + stage_band2_smem() + 16; }
+
+__global__ void __launch_bounds__(kBandThreads, 3)
+    pfb_stage_band2_tma_kernel(const __grid_constant__ CUtensorMap wmap, const float* __restrict__ W, int O,
+                               int64_t nb, const float2* __restrict__ twL, const float2* __restrict__ tws, int u0,
+                               int u1, float2* __restrict__ out, int* __restrict__ fault) {
+  constexpr int P = 4096, PER = P / kBandThreads;
+  extern __shared__ uint8_t smb2[];
+  const uint32_t raw_s = smem_u32(smb2);
+  const uint32_t pad = (1024u - (raw_s & 1023u)) & 1023u;
+  float2* bufA = reinterpret_cast<float2*>(smb2 + pad);
+  float2* bufB = bufA + padded_len(P);
+  const float4* stage = reinterpret_cast<const float4*>(bufA);  // landing tile, [4096] float4 over bufA/bufB
+  const uint32_t stage_s = raw_s + pad;
+  float2* t3 = bufB + padded_len(P);
+  float2* w16 = t3 + 192;
+  float2* qtw = w16 + 16;
+  uint64_t* barp = reinterpret_cast<uint64_t*>(qtw + 32);
+  int* ok_flag = reinterpret_cast<int*>(barp + 1);
+  const uint32_t bar = smem_u32(barp);
+  const int GW = O < 8 ? O : 8, NG = O / GW;
+  const int j = blockIdx.x;
+  const int64_t b = blockIdx.y;
+  const int in = blockIdx.z;
+  const int L = P * O;
+  const int tid = threadIdx.x;
+  const int c0 = 2 * j;
+  const int sA = c0, sB = c0 + 1;
+  const int g = (2 * c0) / GW, e0 = (2 * c0) % GW;
+  if (tid == 0) {
+    mbar_init(bar, 1);
+    mbar_init_fence();
+    mbar_arrive_expect_tx(bar, 4096 * 16);
+    const int64_t row0 = (((int64_t)in * nb + b) * NG + g) * P;
+#pragma unroll 1
+    for (int r = 0; r < 16; r++) tma_load_2d(stage_s + r * 256 * 16, &wmap, e0, (int)(row0 + 256 * r), bar);
+  }
+  if (tid < 192) {
+    const int d = tid >> 6, i = tid & 63;
+    const int64_t e = d == 0 ? (int64_t)i * 4096 : d == 1 ? (int64_t)i * 64 : i;
+    t3[tid] = e < L ? __ldg(&twL[e]) : make_float2(1.f, 0.f);
+  }
+  if (tid < 16) w16[tid] = __ldg(&twL[(int64_t)tid * (L / 16)]);
+  if (tid < 32) {
+    const int s = tid < 16 ? sA : sB, q = tid & 15;
+    qtw[tid] = __ldg(&twL[((int64_t)s * kBandThreads * q) % L]);
+  }
+  const int nu = u1 - u0;
+  float2* ob = out + ((int64_t)in * nb + b) * ((int64_t)nu * O);
+  if (tid == 0) {
+    const bool ok = mbar_wait(bar, 0);
+    if (!ok) atomicExch(fault, 1);
+    *ok_flag = ok;
+  }
+  __syncthreads();
+  if (!*ok_flag) return;
+  float4 v[PER];
+#pragma unroll
+  for (int q = 0; q < PER; q++) v[q] = stage[tid + q * kBandThreads];
+  __syncthreads();  // the landing tile is read: the buffers are written over it
+  const float2 bA = tw3(t3, (int)(((int64_t)sA * tid) % L)), bB = tw3(t3, (int)(((int64_t)sB * tid) % L));
+#pragma unroll
+  for (int q = 0; q < PER; q++) {
+    const int n = tid + q * kBandThreads;
+    float2 xa = j == 0 ? make_float2(v[q].x, 0.f) : make_float2(v[q].x, v[q].y);
+    if (sA) xa = cmul(cmul(xa, bA), qtw[q]);
+    bufA[pidx(n)] = xa;
+    bufB[pidx(n)] = cmul(cmul(make_float2(v[q].z, v[q].w), bB), qtw[16 + q]);
+  }
+  __syncthreads();
+  spass<16, 256, 4096, kBandThreads, false>(bufA, tws + Plan4096::tw_off(0), tid);
+  spass<16, 256, 4096, kBandThreads, false>(bufB, tws + Plan4096::tw_off(0), tid);
+  __syncthreads();
+  spass<16, 16, 4096, kBandThreads, false>(bufA, tws + Plan4096::tw_off(1), tid);
+  spass<16, 16, 4096, kBandThreads, false>(bufB, tws + Plan4096::tw_off(1), tid);
+  __syncthreads();
+  band_outputs(bufA, w16, u0, nu, false, sA, O, ob, tid);
+  if (sA != 0) band_outputs(bufA, w16, u0, nu, true, O - sA, O, ob, tid);
+  band_outputs(bufB, w16, u0, nu, false, sB, O, ob, tid);
+  band_outputs(bufB, w16, u0, nu, true, O - sB, O, ob, tid);
+  if (j == 0) {  // W_{O/2}, the second real value of slot 0
+    const int sH = O / 2;
+    __syncthreads();
+    const float* src = W + ((((int64_t)in * nb + b) * NG + g) * P) * GW + e0;  // slot 0's record (re-read)
+#pragma unroll 4
+    for (int q = 0; q < PER; q++) {
+      const int n = tid + q * kBandThreads;
+      const float wv = __ldg(src + (size_t)n * GW + 1);
+      bufA[pidx(n)] = cmul(make_float2(wv, 0.f), tw3(t3, (int)(((int64_t)sH * n) % L)));
+    }
+    __syncthreads();
+    spass<16, 256, 4096, kBandThreads, false>(bufA, tws + Plan4096::tw_off(0), tid);
+    __syncthreads();
+    spass<16, 16, 4096, kBandThreads, false>(bufA, tws + Plan4096::tw_off(1), tid);
+    __syncthreads();
+    band_outputs(bufA, w16, u0, nu, false, sH, O, ob, tid);
+  }
+}
+
 int launch_pfb_stage_a(const TsSrc& src, int ninputs, int P, int O, int ntap, int64_t row0, int64_t nb,
                        const float* win, float* W, const float2* tw64, cudaStream_t s) {
   AB_CHECK_ARG(P % kFoldCols == 0, "pfb: lblock/osamp %d must be a multiple of %d", P, kFoldCols);
@@ -692,7 +798,7 @@ int launch_pfb_stage_b(ab_ctx* ctx, const float* W, int ninputs, int P, int O, i
   dim3 grid((unsigned)nb, (unsigned)(O / GW), (unsigned)ninputs);
   const int64_t wrows = (int64_t)ninputs * nb * (O / GW) * P;
   if (fault && ctx->pfb_tma && P == Plan4096::N && O >= 4 && O <= 64 && u1 >= 0 && ((uintptr_t)W & 15) == 0 &&
-      wrows < (1ll << 31) && stage_band_tma_smem() <= ctx->smem_optin) {
+      wrows < (1ll << 31) && nb <= 65535 && stage_band_tma_smem() <= ctx->smem_optin) {
     // W as a 2-D tensor: rows of GW floats (32 or 16 bytes), boxes of 4 floats x 256 rows
     CUtensorMap map;
     const uint64_t dims[2] = {(uint64_t)GW, (uint64_t)wrows}, strides[1] = {(uint64_t)GW * sizeof(float)};
@@ -700,11 +806,18 @@ int launch_pfb_stage_b(ab_ctx* ctx, const float* W, int ninputs, int P, int O, i
     AB_TRY(encode_tmap(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, W, dims, strides, box));
     const float2* tws;
     AB_TRY(get_twiddle_stream(ctx, P, {16, 16, 16}, &tws));
-    const size_t sm = stage_band_tma_smem();
-    AB_CUDA(cudaFuncSetAttribute(pfb_stage_band_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    const int64_t ntile = (int64_t)(O / 4) * nb * ninputs;
-    const unsigned g = (unsigned)std::min<int64_t>(ntile, std::max(ctx->num_sms, 1));
-    pfb_stage_band_tma_kernel<<<g, kBtThreads, sm, s>>>(map, O, nb, ninputs, twL, tws, u0, u1, out, fault);
+    if (ctx->pfb_tma == 2) {
+      const size_t sm = stage_band_tma_smem();
+      AB_CUDA(cudaFuncSetAttribute(pfb_stage_band_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+      const int64_t ntile = (int64_t)(O / 4) * nb * ninputs;
+      const unsigned g = (unsigned)std::min<int64_t>(ntile, std::max(ctx->num_sms, 1));
+      pfb_stage_band_tma_kernel<<<g, kBtThreads, sm, s>>>(map, O, nb, ninputs, twL, tws, u0, u1, out, fault);
+    } else {
+      const size_t sm = stage_band2_tma_smem();
+      AB_CUDA(cudaFuncSetAttribute(pfb_stage_band2_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+      dim3 g2((unsigned)(O / 4), (unsigned)nb, (unsigned)ninputs);
+      pfb_stage_band2_tma_kernel<<<g2, kBandThreads, sm, s>>>(map, W, O, nb, twL, tws, u0, u1, out, fault);
+    }
   } else if (P == Plan4096::N && O >= 4 && O <= 64 && nb <= 65535 && u1 >= 0 && ((uintptr_t)W & 15) == 0) {
     const float2* tws;
     AB_TRY(get_twiddle_stream(ctx, P, {16, 16, 16}, &tws));

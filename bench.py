@@ -703,7 +703,8 @@ def main():
     ap.add_argument("--row-tile", type=int, default=0, help="stream: IIR / FIR row tile (16 or 32)")
     ap.add_argument("--row-ffts", type=int, default=0, help="stream: spectra per row-stage CTA (8, 4 or 2)")
     ap.add_argument("--pfb-tma", type=int, default=-1,
-                    help="stream: PFB band DFT with TMA-staged tiles (1, default) or plain loads (0)")
+                    help="stream: PFB band DFT tile fetch: 0 plain loads (default), 1 TMA into the FFT buffers, "
+                         "2 persistent CTAs with TMA prefetch")
     ap.add_argument("--row-prefetch", type=int, default=-1,
                     help="stream: row stage 0 = one CTA per tile, 1 = persistent prefetching, "
                          "2 (default) = + shared twiddles")

@@ -94,11 +94,12 @@ int ab_ctx_set_time_filter(ab_ctx *ctx, int32_t mode, int32_t row_tile);
  * four CTAs per SM), else a multiple of 64 up to 131072 (the largest for
  * which every fp32 partial sum stays an exact integer). */
 #define AB_OPT_COARSE_TC_SLICE 7
-/* AB_OPT_PFB_TMA: 1 (default) runs the streaming chain's PFB band DFT as
- * persistent CTAs that stage each tile's W records with TMA tensor copies
- * (cp.async.bulk.tensor), fetching the next tile while the current one is
- * transformed; 0 runs one CTA per tile with plain loads.  The arithmetic is
- * the same.  Read at each push. */
+/* AB_OPT_PFB_TMA: how the streaming chain's PFB band DFT fetches a tile's W
+ * records: 0 (default) plain 16-byte loads into registers, one CTA per tile,
+ * three per SM; 1 TMA tensor copies (cp.async.bulk.tensor) landing in the
+ * CTA's FFT buffers, three CTAs per SM; 2 persistent CTAs (one per SM) that
+ * fetch the next tile with TMA while transforming the current one.  The
+ * arithmetic is the same (bitwise the same output).  Read at each push. */
 #define AB_OPT_PFB_TMA 9
 int ab_ctx_set_option(ab_ctx *ctx, int32_t option, int32_t value);
 

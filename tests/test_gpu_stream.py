@@ -199,21 +199,23 @@ def test_run_from_host_overlapped_copies_equal_device_run():
     (1, 4, 512, 16, 4),     # one slot pair (the W_{O/2} transform in every tile)
 ])
 def test_pfb_band_tma_bitwise_equal(nant, osamp, acclen, nblock, nchunks):
-    """The band DFT with W tiles staged by TMA (persistent CTAs, the next tile
-    fetched while the current one is transformed) gives bitwise the same
-    visibilities as one CTA per tile with plain loads, and both match the
+    """The band DFT with W tiles staged by TMA (1: one CTA per tile landing
+    the tile in its FFT buffers; 2: persistent CTAs fetching the next tile
+    while the current one is transformed) gives bitwise the same
+    visibilities as one CTA per tile with plain loads (0), and all match the
     FP64 oracle."""
     from albatros_axion_detection_gb300 import autotune
     raw = gen.raw_4bit(seed=osamp * nant + acclen, nspec=nchunks * acclen, nchan=8, nant=nant)
     channels = np.arange(300, 308)
     kw = dict(acclen=acclen, nchunks=nchunks, nblock=nblock, chanstart=0, chanend=8, osamp=osamp, cut=32)
     out = {}
-    for tma in (1, 0):
+    for tma in (1, 2, 0):
         autotune.set_pfb_tma(tma)
         try:
             out[tma], _ = run(raw, channels, **kw)
         finally:
-            autotune.set_pfb_tma(1)
+            autotune.set_pfb_tma(0)
     assert np.array_equal(np.asarray(out[1]), np.asarray(out[0]))
+    assert np.array_equal(np.asarray(out[2]), np.asarray(out[0]))
     ref, _ = po.repfb_xcorr_avg(raw, channels, **kw)
     check(np.asarray(out[1]), ref)
