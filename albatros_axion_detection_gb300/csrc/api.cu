@@ -60,6 +60,7 @@ bool make_plan(int n, FftPlan* p) {
   if (n < 1) return false;
   p->n = n;
   p->npass = 0;
+  p->gscratch = nullptr;
   int m = n;
   const int order[] = {8, 4, 2, 7, 5, 3};
   // Prefer radix 8; a single leftover factor 2 or 4 is taken as radix 2/4.
@@ -79,8 +80,40 @@ bool make_plan(int n, FftPlan* p) {
   return true;
 }
 
+bool make_plan_any(int n, FftPlan* p) {
+  if (make_plan(n, p)) return true;
+  if (n < 1) return false;
+  p->npass = 0;
+  p->gscratch = nullptr;
+  int m = n;
+  const int order[] = {8, 4, 2, 7, 5, 3};
+  for (int r : order)
+    while (m % r == 0) {
+      if (p->npass >= kMaxPasses) return false;
+      p->radix[p->npass++] = r;
+      m /= r;
+    }
+  for (int f = 11; (int64_t)f * f <= m; f += 2)  // the remaining prime factors, direct DFT passes
+    while (m % f == 0) {
+      if (p->npass >= kMaxPasses) return false;
+      p->radix[p->npass++] = f;
+      m /= f;
+    }
+  if (m > 1) {
+    if (p->npass >= kMaxPasses) return false;
+    p->radix[p->npass++] = m;
+  }
+  int prod = 1;
+  for (int q = 0; q < p->npass; q++) {
+    prod *= p->radix[q];
+    p->span[q] = n / prod;
+  }
+  return true;
+}
+
 bool make_plan_from(int n, const std::vector<int>& radices, FftPlan* p) {
   if ((int)radices.size() > kMaxPasses) return false;
+  p->gscratch = nullptr;
   p->n = n;
   p->npass = (int)radices.size();
   int prod = 1;

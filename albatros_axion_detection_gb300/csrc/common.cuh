@@ -57,6 +57,17 @@ inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s
 // Factorise n into supported radices (8, 4, 2, 7, 5, 3). Returns false if n
 // has another prime factor.
 bool make_plan(int n, FftPlan* p);
+// Any length: the factors 2, 3, 4, 5, 7, 8 as register passes, every other
+// prime factor as a direct DFT pass (needs FftPlan::gscratch at launch).
+bool make_plan_any(int n, FftPlan* p);
+// True when the plan has a direct DFT pass.
+inline bool plan_has_generic(const FftPlan& p) {
+  for (int q = 0; q < p.npass; q++) {
+    const int r = p.radix[q];
+    if (r != 2 && r != 3 && r != 4 && r != 5 && r != 7 && r != 8) return true;
+  }
+  return false;
+}
 
 }  // namespace ab
 
@@ -113,5 +124,6 @@ int get_pair_table(ab_ctx* ctx, const FftPlan& p, const int2** out);
 int get_scratch(ab_ctx* ctx, int slot, size_t bytes, void** out);
 // Per-device constant tables of the FIR time stage (fir.cu).
 int fir_init_device();
-enum ScratchSlot { kScratchPfbW = 1, kScratchXcorrG = 2, kScratchChain = 3, kScratchYband = 4, kScratchFault = 5 };
+enum ScratchSlot { kScratchPfbW = 1, kScratchXcorrG = 2, kScratchChain = 3, kScratchYband = 4, kScratchFault = 5,
+                  kScratchDftPass = 6 };
 }  // namespace ab

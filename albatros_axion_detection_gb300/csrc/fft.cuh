@@ -29,6 +29,11 @@ struct FftPlan {
   int npass;
   int radix[kMaxPasses];  // R_p
   int span[kMaxPasses];   // S_p = n / (R_1 .. R_p)
+  // Radices other than 2, 3, 4, 5, 7, 8 (prime factors the register
+  // butterflies do not cover) run as direct DFT passes, whose outputs go
+  // through this global scratch: n complex per CTA, CTA (x, y) at
+  // gscratch + (y * gridDim.x + x) * n.  Null for plans without them.
+  float2* gscratch;
 };
 
 // 32-byte store of 8 floats (one whole sector), p 32-byte aligned
@@ -244,8 +249,47 @@ __device__ __forceinline__ void dit_pass(float2* buf, int n, int S, const TW& tw
   }
 }
 
+// One pass of any radix R as a direct DFT (the prime factors without a
+// register butterfly).  Output k of butterfly (blk, j) is
+//   DIF: W_RS^(j k) sum_r x_r W_R^(r k)      DIT: sum_r conj(W_RS^(j r)) x_r conj(W_R)^(r k)
+// with every twiddle an exact table entry (index (r k) mod R advanced by
+// integer steps, no recurrences); the R terms are summed in blocks of 32
+// before being added, which keeps fp32 rounding near that of an FFT.  All
+// threads share the outputs; they go to the CTA's global scratch and are
+// copied back after a barrier.  The caller syncs after the pass.
 template <bool INV, class TW>
-__device__ __forceinline__ void run_pass(int R, float2* buf, int n, int S, const TW& tw, int T, int tid, int nthr) {
+__device__ __noinline__ void generic_pass(float2* buf, int n, int R, int S, const TW& tw, int T, float2* scratch,
+                                          int tid, int nthr) {
+  const int tstep = T / (R * S), rstep = T / R;
+  for (int o = tid; o < n; o += nthr) {
+    const int bf = o / R, k = o - bf * R;
+    const int blk = bf / S, j = bf - blk * S;
+    const int base = blk * R * S + j;
+    float2 acc = make_float2(0.f, 0.f), part = make_float2(0.f, 0.f);
+    int e = 0;  // (r k) mod R
+    for (int r = 0; r < R; r++) {
+      float2 x = buf[pidx(base + r * S)];
+      if (INV && j) x = cmulc(x, tw(j * r * tstep));
+      const float2 w = tw(e * rstep);
+      part = INV ? cadd(part, cmulc(x, w)) : cadd(part, cmul(x, w));
+      e += k;
+      if (e >= R) e -= R;
+      if ((r & 31) == 31) {
+        acc = cadd(acc, part);
+        part = make_float2(0.f, 0.f);
+      }
+    }
+    acc = cadd(acc, part);
+    if (!INV && j) acc = cmul(acc, tw(j * k * tstep));
+    scratch[base + k * S] = acc;
+  }
+  __syncthreads();
+  for (int i = tid; i < n; i += nthr) buf[pidx(i)] = scratch[i];
+}
+
+template <bool INV, class TW>
+__device__ __forceinline__ void run_pass(int R, float2* buf, int n, int S, const TW& tw, int T, int tid, int nthr,
+                                         float2* gscratch = nullptr) {
   switch (R) {
     case 2: INV ? dit_pass<2>(buf, n, S, tw, T, tid, nthr) : dif_pass<2>(buf, n, S, tw, T, tid, nthr); break;
     case 3: INV ? dit_pass<3>(buf, n, S, tw, T, tid, nthr) : dif_pass<3>(buf, n, S, tw, T, tid, nthr); break;
@@ -253,7 +297,10 @@ __device__ __forceinline__ void run_pass(int R, float2* buf, int n, int S, const
     case 5: INV ? dit_pass<5>(buf, n, S, tw, T, tid, nthr) : dif_pass<5>(buf, n, S, tw, T, tid, nthr); break;
     case 7: INV ? dit_pass<7>(buf, n, S, tw, T, tid, nthr) : dif_pass<7>(buf, n, S, tw, T, tid, nthr); break;
     case 8: INV ? dit_pass<8>(buf, n, S, tw, T, tid, nthr) : dif_pass<8>(buf, n, S, tw, T, tid, nthr); break;
-    default: break;
+    default:
+      if (gscratch) generic_pass<INV>(buf, n, R, S, tw, T, gscratch + (size_t)(blockIdx.y * gridDim.x + blockIdx.x) * n,
+                                      tid, nthr);
+      break;
   }
 }
 
@@ -262,7 +309,7 @@ __device__ __forceinline__ void run_pass(int R, float2* buf, int n, int S, const
 template <class TW>
 __device__ __forceinline__ void dif_forward(float2* buf, const FftPlan& p, const TW& tw, int T, int tid, int nthr) {
   for (int q = 0; q < p.npass; q++) {
-    run_pass<false>(p.radix[q], buf, p.n, p.span[q], tw, T, tid, nthr);
+    run_pass<false>(p.radix[q], buf, p.n, p.span[q], tw, T, tid, nthr, p.gscratch);
     __syncthreads();
   }
 }
@@ -271,7 +318,7 @@ __device__ __forceinline__ void dif_forward(float2* buf, const FftPlan& p, const
 template <class TW>
 __device__ __forceinline__ void dit_inverse(float2* buf, const FftPlan& p, const TW& tw, int T, int tid, int nthr) {
   for (int q = p.npass - 1; q >= 0; q--) {
-    run_pass<true>(p.radix[q], buf, p.n, p.span[q], tw, T, tid, nthr);
+    run_pass<true>(p.radix[q], buf, p.n, p.span[q], tw, T, tid, nthr, p.gscratch);
     __syncthreads();
   }
 }

@@ -891,9 +891,14 @@ extern "C" int ab_ipfb(ab_ctx* ctx, const float* dat, const float* filt, float* 
     set_error("ab_ipfb: lblock %d does not factor into 2,3,5,7", P);
     return AB_ERR_UNSUPPORTED;
   }
-  if (!ctx_plan(ctx, (int)(nslice / 2), &planM)) {
-    set_error("ab_ipfb: nslice/2 = %lld does not factor into 2,3,5,7", (long long)(nslice / 2));
+  if (!ctx_plan(ctx, (int)(nslice / 2), &planM) && !make_plan_any((int)(nslice / 2), &planM)) {
+    set_error("ab_ipfb: no FFT plan for nslice/2 = %lld", (long long)(nslice / 2));
     return AB_ERR_UNSUPPORTED;
+  }
+  if (plan_has_generic(planM)) {  // prime factors above 7: direct DFT passes through a scratch column per CTA
+    void* g = nullptr;
+    AB_TRY(get_scratch(ctx, kScratchDftPass, sizeof(float2) * (size_t)P * (size_t)planM.n, &g));
+    planM.gscratch = (float2*)g;
   }
   const float2 *twP, *twN;
   AB_TRY(get_twiddles(ctx, P, &twP));

@@ -5,8 +5,11 @@ albatros_analysis/src/utils/pfb_utils.py (sinc_hamming :4-7), computed by the
 CUDA kernels of csrc/ipfb.cu and csrc/pfb.cu.
 
 The FFTs are this library's own shared-memory mixed-radix transforms
-(radices 2, 3, 4, 5, 7, 8): IPFB lengths need nslice/2 and lblock to factor
-into 2, 3, 5, 7; PFB lengths must be powers of two (lblock = 4096*osamp).
+(register butterflies of radix 2, 3, 4, 5, 7, 8; any other prime factor of
+an IPFB length runs as a direct DFT pass, correct for any even nslice but
+slow for large primes: 0.2 s for nslice 32788 = 4 * 7 * 1171 against 1.4 ms
+for 32928 = 2^5 * 3 * 7^3 on one GB300); lblock must factor into 2, 3, 5, 7;
+PFB lengths must be powers of two (lblock = 4096*osamp).
 """
 from __future__ import annotations
 

@@ -98,3 +98,59 @@ def test_autotuner_orders_are_valid_plans():
     for n in (16464, 16384, 4096 * 3):
         for order in autotune.candidate_orders(n, limit=24):
             assert int(np.prod(order)) == n and set(order) <= {2, 3, 4, 5, 7, 8}
+
+
+def plan_any(n):
+    """make_plan_any (csrc/api.cu): radices 8, 4, 2, 7, 5, 3 as far as they
+    divide n, then each remaining prime factor as one direct DFT pass."""
+    radices, m = [], n
+    for r in (8, 4, 2, 7, 5, 3):
+        while m % r == 0:
+            radices.append(r)
+            m //= r
+    f = 11
+    while f * f <= m:
+        while m % f == 0:
+            radices.append(f)
+            m //= f
+        f += 2
+    if m > 1:
+        radices.append(m)
+    return radices
+
+
+@pytest.mark.parametrize("n", [16394, 2 * 13 * 11, 4 * 1009, 3 * 11 * 11, 1009])
+def test_any_length_plans_with_direct_dft_passes(n):
+    """nslice/2 of the reference's default cut (16394 = 2 * 7 * 1171) and
+    other lengths with prime factors above 7: the plan multiplies to n, its
+    direct DFT passes land frequencies in the same digit-reversed positions,
+    and forward -> pointwise -> inverse is circular filtering."""
+    radices = plan_any(n)
+    assert int(np.prod(radices)) == n and len(radices) <= 12
+    rng = np.random.default_rng(n)
+    x = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    X = dif_forward(x, radices)
+    pos = positions(n, radices)
+    assert np.array_equal(np.sort(pos), np.arange(n))
+    np.testing.assert_allclose(X[pos], np.fft.fft(x), atol=1e-8 * np.sqrt(n))
+    H = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    Hpos = np.empty(n, complex)
+    Hpos[pos] = H
+    y = dit_inverse(X * Hpos, radices) / n
+    np.testing.assert_allclose(y, np.fft.ifft(np.fft.fft(x) * H), atol=1e-9)
+
+
+@pytest.mark.parametrize("R,S,T", [(1171, 1, 32788), (1171, 2, 32788), (13, 22, 572)])
+def test_direct_pass_twiddle_indices(R, S, T):
+    """generic_pass (csrc/fft.cuh): stepping e += k (mod R) gives (r k) mod R,
+    and every table index j k (T / (R S)), e (T / R) stays below T."""
+    assert T % (R * S) == 0
+    tstep, rstep = T // (R * S), T // R
+    for k in (0, 1, R // 2, R - 1):
+        e = 0
+        for r in range(R):
+            assert e == (r * k) % R and e * rstep < T
+            e += k
+            if e >= R:
+                e -= R
+    assert (S - 1) * (R - 1) * tstep < T

@@ -98,11 +98,12 @@ def test_headline_other_time_stages(raw, mode, cut):
     assert max(errs) < 1e-5
 
 
-def test_headline_ipfb_timestream(raw):
+@pytest.mark.parametrize("cut", [10, 80])
+def test_headline_ipfb_timestream(raw, cut):
     """cupy_ipfb on the first chunk's rows (2*cut zero rows, then 2^15 placed
-    rows) at nslice 32928, against the FP64 IPFB with the FP64 filter."""
+    rows) at nslice 32788 (the reference's default cut) and 32928, against the
+    FP64 IPFB with the FP64 filter."""
     from albatros_axion_detection_gb300 import pfb_gpu_utils as pg
-    cut = 80
     nslice = ACCLEN + 2 * cut
     sel = np.arange(NCH)
     spec = po.unpack_4bit_np(raw[0], 0, ACCLEN, sel)[0]

@@ -54,12 +54,26 @@ def test_ipfb_vs_oracle(nslice):
     assert rel(got, exp) < TOL_FFT
 
 
-def test_ipfb_rejects_unsupported_length():
+@pytest.mark.parametrize("nslice", [22, 1044, 2018, 8212, 32788])
+def test_ipfb_any_length_vs_oracle(nslice):
+    """Lengths whose nslice/2 has a prime factor above 7 (11; 29; 1009; 2053;
+    1171, the reference's default cut on 2^15 spectra) run their time-axis
+    transforms with direct DFT passes for those factors, like cuFFT runs any
+    length for the reference."""
+    from albatros_axion_detection_gb300 import pfb_gpu_utils as pu
+    dat = gen.ipfb_input(seed=nslice, nslice=nslice)
+    filt = pu.build_filter(nslice, 0.45)
+    got = pu.cupy_ipfb(cu(dat), filt).cpu().numpy()
+    exp = po.ipfb(dat.astype(np.complex128), filt.cpu().numpy().astype(np.complex128))
+    assert rel(got, exp) < TOL_FFT
+
+
+def test_ipfb_rejects_odd_length():
     from albatros_axion_detection_gb300 import pfb_gpu_utils as pu
     from albatros_axion_detection_gb300._lib import AlbatrosError
-    dat = gen.ipfb_input(seed=1, nslice=22)  # 11 is not a supported radix
-    with pytest.raises(AlbatrosError):
-        pu.cupy_ipfb(cu(dat), torch.zeros((4096, 12), dtype=torch.complex64, device="cuda"))
+    dat = gen.ipfb_input(seed=1, nslice=21)
+    with pytest.raises((ValueError, AlbatrosError)):
+        pu.cupy_ipfb(cu(dat), torch.zeros((4096, 11), dtype=torch.complex64, device="cuda"))
 
 
 def test_pfb_golden(golden_pfb):
