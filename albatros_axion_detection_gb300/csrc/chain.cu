@@ -220,8 +220,10 @@ extern "C" int ab_stream_create(ab_ctx* ctx, int64_t nant, int64_t nchan_raw, in
       if (c > total + 2) break;
     }
     st->nb_max = std::max<int64_t>(mx, acclen / osamp + 1);
-    // the final push may flush up to a whole job plus the taps beyond the data
-    st->nb_max = std::max<int64_t>(st->nb_max, acclen / osamp + nblock + ntap + 1);
+    // the final push also completes the blocks that straddle the end of the
+    // data (their taps read zeros past it); blocks that start past the end
+    // are all zeros and are not produced (they add nothing to the jobs)
+    st->nb_max = std::max<int64_t>(st->nb_max, acclen / osamp + ntap + 1);
   }
   AB_ALLOC(st->d_cols, sizeof(int32_t) * nsel);
   AB_ALLOC(st->d_abs, sizeof(int32_t) * nsel);
@@ -368,9 +370,11 @@ struct StageTimer {
   }
 };
 
-// Push chunk `chunk`.  final != 0 marks the last chunk of the stream: every
-// remaining block of the planned jobs is then produced with zeros past the end
-// (the reference's zero-padded last job, helper_gpu_stream_clean.py:163-167).
+// Push chunk `chunk`.  final != 0 marks the last chunk of the stream: the
+// remaining blocks of the planned jobs that hold data are then produced with
+// zeros past the end (the reference's zero-padded last job,
+// helper_gpu_stream_clean.py:163-167); the all-zero blocks after them add
+// nothing to the visibilities and are not computed.
 static int stream_push(ab_stream* st, const uint8_t* raw, int64_t ant_stride, const int32_t* spec_map,
                        int64_t map_stride, int64_t chunk, bool final, cudaStream_t s) {
   AB_CHECK_ARG(raw, "ab_stream_push: NULL raw pointer");
@@ -394,7 +398,11 @@ static int stream_push(ab_stream* st, const uint8_t* raw, int64_t ant_stride, co
   const int64_t total_blocks = st->njobs * st->nblock;
   const int64_t rows_avail = (chunk + 1) * acclen;
   int64_t b_end = rows_avail / O - st->ntap + 1;  // exclusive
-  if (final) b_end = total_blocks;
+  // the final push completes every planned block that holds data: the
+  // reference zero-pads the last job (helper_gpu_stream_clean.py:163-167);
+  // blocks starting at or past the end of the data are zeros throughout, so
+  // they contribute nothing to their job's visibilities and are skipped
+  if (final) b_end = std::min<int64_t>(total_blocks, (rows_avail + O - 1) / O);
   if (b_end > total_blocks) b_end = total_blocks;
   if (b_end < st->blocks_done) b_end = st->blocks_done;
   const int64_t nb_all = b_end - st->blocks_done;

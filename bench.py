@@ -491,7 +491,8 @@ def run_batch(args):
         "config": {"workload": BATCH_WORKLOAD, "spectra_per_step": spectra, "files": len(files), "lanes": len(bc.lanes),
                    "parallelism": f"replicas x{world}",
                    "tuned_time_stage": {f"acclen{k[0]}_cut{k[1]}_osamp{k[2]}": v for k, v in bc.tuned.items()},
-                   "setup_s": t_setup, "l2": "inputs larger than L2"},
+                   "setup_s": t_setup, "l2": "inputs larger than L2",
+                   "workspace_gb_per_lane": [round(w.numel() / 1e9, 3) for w in bc.workspaces if w is not None]},
         "e2e": {"value": world * spectra / (ms_e2e / 1e3), "unit": "spectra/s", "ms_per_step": ms_e2e,
                 "h2d_bytes_per_step": bc.h2d_bytes, "d2h_bytes_per_step": bc.d2h_bytes},
         "gpu_launches": int(bc.launches_per_run() * args.steps),

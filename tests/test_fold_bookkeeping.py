@@ -11,7 +11,9 @@ Checks, for every push of every geometry:
     tail (first segment), a row the item computed, or the zero padding after
     the stream's end (last segment of the final push);
   * the tail kept for the next chunk is made of rows the item holds;
-  * blocks of a push that is not the final one only read rows that exist.
+  * blocks of a push that is not the final one only read rows that exist;
+  * no push produces more blocks than the stream's W buffer holds (the final
+    push skips the all-zero blocks that start past the end of the data).
 The fine blocks follow the reference's PFB buffer (ntap = 4 blocks of osamp
 rows each; albatros_analysis/scripts/xcorr/helper_gpu_stream_clean.py:71-167).
 """
@@ -56,10 +58,11 @@ def check_stream(U, D, O, acclen, nchunks, total_blocks):
     for c in range(nchunks):
         final = c == nchunks - 1
         b_end = (c + 1) * acclen // O - NTAP + 1
-        if final:
-            b_end = total_blocks
+        if final:  # blocks starting at or past the end of the data are all zeros: not produced
+            b_end = min(total_blocks, -(-(c + 1) * acclen // O))
         b_end = max(min(b_end, total_blocks), blocks_done)
         nb = b_end - blocks_done
+        assert nb <= acclen // O + NTAP + 1  # the stream's W buffer (nb_max in ab_stream_create)
         row0 = blocks_done * O - c * acclen  # local row of the first block
         assert c == 0 or row0 >= -4 * O
         owner = np.zeros(nb, np.int64)
