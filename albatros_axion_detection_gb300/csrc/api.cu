@@ -61,6 +61,7 @@ bool make_plan(int n, FftPlan* p) {
   p->n = n;
   p->npass = 0;
   p->gscratch = nullptr;
+  p->bs = BluesteinPass{};
   int m = n;
   const int order[] = {8, 4, 2, 7, 5, 3};
   // Prefer radix 8; a single leftover factor 2 or 4 is taken as radix 2/4.
@@ -114,6 +115,7 @@ bool make_plan_any(int n, FftPlan* p) {
 bool make_plan_from(int n, const std::vector<int>& radices, FftPlan* p) {
   if ((int)radices.size() > kMaxPasses) return false;
   p->gscratch = nullptr;
+  p->bs = BluesteinPass{};
   p->n = n;
   p->npass = (int)radices.size();
   int prod = 1;
@@ -171,6 +173,88 @@ int get_pair_table(ab_ctx* ctx, const FftPlan& p, const int2** out) {
   AB_CUDA(cudaMemcpy(d, h.data(), sizeof(int2) * h.size(), cudaMemcpyHostToDevice));
   ctx->pair_tables[key] = d;
   *out = d;
+  return AB_OK;
+}
+
+int plan_pos(const FftPlan& p, int f) { return host_pos(p, f); }
+
+int get_bluestein(ab_ctx* ctx, int R, BluesteinPass* out) {
+  {
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    auto it = ctx->bluestein.find(R);
+    if (it != ctx->bluestein.end()) {
+      *out = it->second;
+      return AB_OK;
+    }
+  }
+  BluesteinPass bs{};
+  bs.R = R;
+  FftPlan lp;
+  int L = 2 * R - 1;
+  while (!make_plan(L, &lp)) L++;  // the smallest 7-smooth length >= 2R - 1
+  bs.L = L;
+  bs.npass = lp.npass;
+  for (int q = 0; q < kMaxPasses; q++) {
+    bs.radix[q] = q < lp.npass ? lp.radix[q] : 0;
+    bs.span[q] = q < lp.npass ? lp.span[q] : 0;
+  }
+  const double pi = 3.14159265358979323846;
+  // chirp c_e = exp(-i pi e / R), e < 2R
+  std::vector<float2> ch((size_t)2 * R);
+  for (int e = 0; e < 2 * R; e++) ch[e] = make_float2((float)cos(pi * e / R), (float)-sin(pi * e / R));
+  // b[m] = conj(c_(m^2 mod 2R)) for |m| < R, wrapped to length L; its DFT / L
+  std::vector<double> br((size_t)L, 0.0), bi((size_t)L, 0.0);
+  for (int m = 0; m < R; m++) {
+    const int64_t e = ((int64_t)m * m) % (2 * R);
+    const double c = cos(pi * (double)e / R), sn = sin(pi * (double)e / R);
+    br[m] = c;
+    bi[m] = sn;
+    if (m > 0) {
+      br[L - m] = c;
+      bi[L - m] = sn;
+    }
+  }
+  std::vector<double> cl((size_t)L), sl((size_t)L);
+  for (int e = 0; e < L; e++) {
+    cl[e] = cos(2.0 * pi * e / L);
+    sl[e] = sin(2.0 * pi * e / L);
+  }
+  std::vector<float2> filt((size_t)L);
+  for (int f = 0; f < L; f++) {
+    double xr = 0.0, xi = 0.0;
+    int64_t e = 0;
+    for (int m = 0; m < L; m++) {  // sum_m b[m] exp(-2 pi i f m / L)
+      xr += br[m] * cl[e] + bi[m] * sl[e];
+      xi += bi[m] * cl[e] - br[m] * sl[e];
+      e += f;
+      if (e >= L) e -= L;
+    }
+    filt[(size_t)host_pos(lp, f)] = make_float2((float)(xr / L), (float)(xi / L));
+  }
+  const float2* twL = nullptr;
+  AB_TRY(get_twiddles(ctx, L, &twL));
+  float2 *dch = nullptr, *dfl = nullptr;
+  if (cudaMalloc(&dch, sizeof(float2) * ch.size()) != cudaSuccess ||
+      cudaMalloc(&dfl, sizeof(float2) * filt.size()) != cudaSuccess) {
+    cudaFree(dch);
+    set_error("Bluestein tables: device allocation failed");
+    return AB_ERR_NOMEM;
+  }
+  AB_CUDA(cudaMemcpy(dch, ch.data(), sizeof(float2) * ch.size(), cudaMemcpyHostToDevice));
+  AB_CUDA(cudaMemcpy(dfl, filt.data(), sizeof(float2) * filt.size(), cudaMemcpyHostToDevice));
+  bs.chirp = dch;
+  bs.filt = dfl;
+  bs.twL = twL;
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  auto it = ctx->bluestein.find(R);
+  if (it != ctx->bluestein.end()) {  // another thread built it meanwhile
+    cudaFree(dch);
+    cudaFree(dfl);
+    *out = it->second;
+    return AB_OK;
+  }
+  ctx->bluestein[R] = bs;
+  *out = bs;
   return AB_OK;
 }
 
@@ -406,6 +490,10 @@ int ab_ctx_destroy(ab_ctx* ctx) {
   for (auto& kv : ctx->twiddles) cudaFree(kv.second);
   for (auto& kv : ctx->streams) cudaFree(kv.second);
   for (auto& kv : ctx->pair_tables) cudaFree(kv.second);
+  for (auto& kv : ctx->bluestein) {
+    cudaFree(const_cast<float2*>(kv.second.chirp));
+    cudaFree(const_cast<float2*>(kv.second.filt));
+  }
   for (auto& kv : ctx->fir_taps) cudaFree((void*)kv.second.second);
   for (auto& kv : ctx->scratch)
     if (kv.second.first) cudaFree(kv.second.first);

@@ -60,6 +60,12 @@ bool make_plan(int n, FftPlan* p);
 // Any length: the factors 2, 3, 4, 5, 7, 8 as register passes, every other
 // prime factor as a direct DFT pass (needs FftPlan::gscratch at launch).
 bool make_plan_any(int n, FftPlan* p);
+// The Bluestein pass of prime radix R (cached per context): convolution
+// length L (the smallest 7-smooth length >= 2R - 1), L's plan, the chirp,
+// the filter spectrum (FP64 on the host, rounded once) and L's twiddles.
+int get_bluestein(ab_ctx* ctx, int R, BluesteinPass* out);
+// Storage position of frequency f after the forward passes of plan p.
+int plan_pos(const FftPlan& p, int f);
 // True when the plan has a direct DFT pass.
 inline bool plan_has_generic(const FftPlan& p) {
   for (int q = 0; q < p.npass; q++) {
@@ -81,6 +87,7 @@ struct ab_ctx {
   std::map<int64_t, float2*> twiddles;
   std::map<std::vector<int>, float2*> streams;
   std::map<std::vector<int>, int2*> pair_tables;
+  std::map<int, ab::BluesteinPass> bluestein;  // keyed by the prime radix
   // FFT plans chosen by the autotuner: length -> radix order (forces the
   // runtime-plan kernels for that length)
   std::map<int, std::vector<int>> plan_override;

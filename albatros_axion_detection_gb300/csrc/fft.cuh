@@ -24,6 +24,20 @@ namespace ab {
 
 constexpr int kMaxPasses = 12;
 
+// A prime radix R run by Bluestein's method: the length-R DFT as a chirp
+// multiply, a circular convolution of length L (7-smooth, L >= 2R - 1) by
+// this library's FFT in shared memory, and a chirp multiply back:
+//   X_k = c_k sum_r (x_r c_r) conj(c_(k-r)),  c_m = exp(-i pi m^2 / R).
+struct BluesteinPass {
+  int R, L;                   // the prime radix (0: none) and the convolution length
+  int npass;                  // L's plan
+  int radix[kMaxPasses];
+  int span[kMaxPasses];
+  const float2* chirp;        // c_(e) for e in [0, 2R): exp(-i pi e / R), indexed by m^2 mod 2R
+  const float2* filt;         // FFT_L of conj(c) wrapped to length L, / L, at L's storage positions
+  const float2* twL;          // exp(-2 pi i e / L), e < L
+};
+
 struct FftPlan {
   int n;                  // transform length (complex points)
   int npass;
@@ -34,6 +48,9 @@ struct FftPlan {
   // through this global scratch: n complex per CTA, CTA (x, y) at
   // gscratch + (y * gridDim.x + x) * n.  Null for plans without them.
   float2* gscratch;
+  // The prime radix bs.R (if any) runs as a Bluestein pass in a shared
+  // scratch of padded_len(bs.L) float2 (the caller's sscratch).
+  BluesteinPass bs;
 };
 
 // 32-byte store of 8 floats (one whole sector), p 32-byte aligned
@@ -287,9 +304,67 @@ __device__ __noinline__ void generic_pass(float2* buf, int n, int R, int S, cons
   for (int i = tid; i < n; i += nthr) buf[pidx(i)] = scratch[i];
 }
 
-template <bool INV, class TW>
+// Twiddle source reading a global table directly.
+struct GlobalTw {
+  const float2* t;
+  __device__ __forceinline__ float2 operator()(int e) const { return __ldg(&t[e]); }
+};
+
+template <bool INV, class TW, bool GEN = true>
 __device__ __forceinline__ void run_pass(int R, float2* buf, int n, int S, const TW& tw, int T, int tid, int nthr,
-                                         float2* gscratch = nullptr) {
+                                         float2* gscratch = nullptr, const BluesteinPass* bs = nullptr,
+                                         float2* sscratch = nullptr);
+
+// A pass of the prime radix bs.R by Bluestein's method, butterfly by
+// butterfly with all threads, through the shared scratch sc (padded_len(L)).
+// DIF: y_k = W_RS^(j k) DFT(x)_k; DIT: y = IDFT(x_r conj(W_RS^(j r))), the
+// inverse as conj(DFT(conj(.))).  Every chirp and twiddle is an exact table
+// entry (chirp index m^2 mod 2R in integers).
+template <bool INV, class TW>
+__device__ __noinline__ void bluestein_pass(float2* buf, int n, int S, const TW& tw, int T, const BluesteinPass& bs,
+                                            float2* sc, int tid, int nthr) {
+  const int R = bs.R, L = bs.L, tstep = T / (R * S);
+  const GlobalTw twl{bs.twL};
+  const int nbf = n / R;
+  for (int bf = 0; bf < nbf; bf++) {
+    const int blk = bf / S, j = bf - blk * S;
+    const int base = blk * R * S + j;
+    for (int r = tid; r < L; r += nthr) {
+      float2 a = make_float2(0.f, 0.f);
+      if (r < R) {
+        float2 x = buf[pidx(base + r * S)];
+        if (INV) {
+          if (j) x = cmulc(x, tw(j * r * tstep));
+          x = cconj(x);
+        }
+        a = cmul(x, __ldg(&bs.chirp[(int)(((int64_t)r * r) % (2 * R))]));
+      }
+      sc[pidx(r)] = a;
+    }
+    __syncthreads();
+    for (int q = 0; q < bs.npass; q++) {  // L's passes use register butterflies only (L is 7-smooth)
+      run_pass<false, GlobalTw, false>(bs.radix[q], sc, L, bs.span[q], twl, L, tid, nthr);
+      __syncthreads();
+    }
+    for (int i = tid; i < L; i += nthr) sc[pidx(i)] = cmul(sc[pidx(i)], __ldg(&bs.filt[i]));
+    __syncthreads();
+    for (int q = bs.npass - 1; q >= 0; q--) {
+      run_pass<true, GlobalTw, false>(bs.radix[q], sc, L, bs.span[q], twl, L, tid, nthr);
+      __syncthreads();
+    }
+    for (int k = tid; k < R; k += nthr) {
+      float2 y = cmul(sc[pidx(k)], __ldg(&bs.chirp[(int)(((int64_t)k * k) % (2 * R))]));
+      if (INV) y = cconj(y);
+      else if (j) y = cmul(y, tw(j * k * tstep));
+      buf[pidx(base + k * S)] = y;
+    }
+    __syncthreads();
+  }
+}
+
+template <bool INV, class TW, bool GEN>
+__device__ __forceinline__ void run_pass(int R, float2* buf, int n, int S, const TW& tw, int T, int tid, int nthr,
+                                         float2* gscratch, const BluesteinPass* bs, float2* sscratch) {
   switch (R) {
     case 2: INV ? dit_pass<2>(buf, n, S, tw, T, tid, nthr) : dif_pass<2>(buf, n, S, tw, T, tid, nthr); break;
     case 3: INV ? dit_pass<3>(buf, n, S, tw, T, tid, nthr) : dif_pass<3>(buf, n, S, tw, T, tid, nthr); break;
@@ -298,8 +373,13 @@ __device__ __forceinline__ void run_pass(int R, float2* buf, int n, int S, const
     case 7: INV ? dit_pass<7>(buf, n, S, tw, T, tid, nthr) : dif_pass<7>(buf, n, S, tw, T, tid, nthr); break;
     case 8: INV ? dit_pass<8>(buf, n, S, tw, T, tid, nthr) : dif_pass<8>(buf, n, S, tw, T, tid, nthr); break;
     default:
-      if (gscratch) generic_pass<INV>(buf, n, R, S, tw, T, gscratch + (size_t)(blockIdx.y * gridDim.x + blockIdx.x) * n,
-                                      tid, nthr);
+      if constexpr (GEN) {
+        if (bs && sscratch && bs->R == R)
+          bluestein_pass<INV>(buf, n, S, tw, T, *bs, sscratch, tid, nthr);
+        else if (gscratch)
+          generic_pass<INV>(buf, n, R, S, tw, T, gscratch + (size_t)(blockIdx.y * gridDim.x + blockIdx.x) * n, tid,
+                            nthr);
+      }
       break;
   }
 }
@@ -307,18 +387,20 @@ __device__ __forceinline__ void run_pass(int R, float2* buf, int n, int S, const
 // Forward transform of the padded buffer, natural -> digit-reversed.
 // The caller syncs before; this syncs after every pass.
 template <class TW>
-__device__ __forceinline__ void dif_forward(float2* buf, const FftPlan& p, const TW& tw, int T, int tid, int nthr) {
+__device__ __forceinline__ void dif_forward(float2* buf, const FftPlan& p, const TW& tw, int T, int tid, int nthr,
+                                            float2* sscratch = nullptr) {
   for (int q = 0; q < p.npass; q++) {
-    run_pass<false>(p.radix[q], buf, p.n, p.span[q], tw, T, tid, nthr, p.gscratch);
+    run_pass<false>(p.radix[q], buf, p.n, p.span[q], tw, T, tid, nthr, p.gscratch, &p.bs, sscratch);
     __syncthreads();
   }
 }
 
 // Inverse (unnormalised) transform, digit-reversed -> natural.
 template <class TW>
-__device__ __forceinline__ void dit_inverse(float2* buf, const FftPlan& p, const TW& tw, int T, int tid, int nthr) {
+__device__ __forceinline__ void dit_inverse(float2* buf, const FftPlan& p, const TW& tw, int T, int tid, int nthr,
+                                            float2* sscratch = nullptr) {
   for (int q = p.npass - 1; q >= 0; q--) {
-    run_pass<true>(p.radix[q], buf, p.n, p.span[q], tw, T, tid, nthr, p.gscratch);
+    run_pass<true>(p.radix[q], buf, p.n, p.span[q], tw, T, tid, nthr, p.gscratch, &p.bs, sscratch);
     __syncthreads();
   }
 }

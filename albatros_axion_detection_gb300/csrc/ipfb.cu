@@ -15,6 +15,8 @@
 #include <type_traits>
 
 #include "fft_static.cuh"
+#include <algorithm>
+
 #include "fold.cuh"
 #include "ipfb.cuh"
 
@@ -94,14 +96,14 @@ struct NoPlan {};
 // generic runtime plan (two-level shared-memory table `tw`).
 template <class PL, int NTHR>
 __device__ __forceinline__ void fft_inv(float2* buf, const FftPlan& plan, const SmemTw& tw, int T,
-                                        const float2* tws, int tid) {
-  if constexpr (std::is_same<PL, NoPlan>::value) dit_inverse(buf, plan, tw, T, tid, NTHR);
+                                        const float2* tws, int tid, float2* sscratch = nullptr) {
+  if constexpr (std::is_same<PL, NoPlan>::value) dit_inverse(buf, plan, tw, T, tid, NTHR, sscratch);
   else sdit<PL, NTHR>(buf, tws, tid);
 }
 template <class PL, int NTHR>
 __device__ __forceinline__ void fft_fwd(float2* buf, const FftPlan& plan, const SmemTw& tw, int T,
-                                        const float2* tws, int tid) {
-  if constexpr (std::is_same<PL, NoPlan>::value) dif_forward(buf, plan, tw, T, tid, NTHR);
+                                        const float2* tws, int tid, float2* sscratch = nullptr) {
+  if constexpr (std::is_same<PL, NoPlan>::value) dif_forward(buf, plan, tw, T, tid, NTHR, sscratch);
   else sdif<PL, NTHR>(buf, tws, tid);
 }
 template <class PL>
@@ -272,8 +274,10 @@ __global__ void __launch_bounds__(NTHR)
 #pragma unroll
     for (int t = 0; t < 8; t++) w[t] = t < ntap ? __ldg(&wtaps[(int64_t)t * P + n]) : 0.f;
   }
+  // a Bluestein pass's scratch follows the twiddle tables (plans of ab_ipfb only)
+  float2* bscr = plan.bs.R ? buf + padded_len(M) + smem_tw_len(N) : nullptr;
   __syncthreads();
-  fft_fwd<PL, NTHR>(buf, plan, tw, N, tws, tid);
+  fft_fwd<PL, NTHR>(buf, plan, tw, N, tws, tid, bscr);
 
   const float scale = 0.5f / (float)N;  // irfft 1/N and the untangle's 1/2
   const float t2 = thresh * thresh;
@@ -337,7 +341,7 @@ __global__ void __launch_bounds__(NTHR)
     if (pc != pk) buf[pc] = cadd(cconj(Et), make_float2(Ot.y, Ot.x));  // conj(Et) + i conj(Ot)
   }
   __syncthreads();
-  fft_inv<PL, NTHR>(buf, plan, tw, N, tws, tid);
+  fft_inv<PL, NTHR>(buf, plan, tw, N, tws, tid, bscr);
   if constexpr (FOLDG == 0) {
     float2* out2 = reinterpret_cast<float2*>(col);
     for (int m = tid; m < M; m += NTHR) out2[m] = buf[pidx(m)];
@@ -721,7 +725,7 @@ static int launch_time_t(ab_ctx* /*ctx*/, float* buf, int64_t ld, int ninputs, i
 int launch_time_stage(ab_ctx* ctx, float* buf, int64_t ld, int ninputs, int P, int N, const FftPlan& planM,
                       const float2* twN, const float2* table, const float* wtaps, int ntap, float thresh,
                       cudaStream_t s) {
-  size_t smem = time_smem_bytes(N);
+  size_t smem = time_smem_bytes(N) + (planM.bs.R ? sizeof(float2) * (size_t)padded_len(planM.bs.L) : 0);
   AB_CHECK_ARG(smem <= ctx->smem_optin, "time stage: nslice %d needs %zu bytes of shared memory (max %zu)", N, smem,
                ctx->smem_optin);
   AB_CHECK_ARG(table || (wtaps && ntap >= 1 && ntap <= 8), "time stage: need a filter table or 1..8 window taps");
@@ -895,10 +899,27 @@ extern "C" int ab_ipfb(ab_ctx* ctx, const float* dat, const float* filt, float* 
     set_error("ab_ipfb: no FFT plan for nslice/2 = %lld", (long long)(nslice / 2));
     return AB_ERR_UNSUPPORTED;
   }
-  if (plan_has_generic(planM)) {  // prime factors above 7: direct DFT passes through a scratch column per CTA
-    void* g = nullptr;
-    AB_TRY(get_scratch(ctx, kScratchDftPass, sizeof(float2) * (size_t)P * (size_t)planM.n, &g));
-    planM.gscratch = (float2*)g;
+  if (plan_has_generic(planM)) {
+    // prime factors above 7: the largest by Bluestein's method when its
+    // convolution fits in shared memory beside the column, the others (and
+    // that one otherwise) as direct DFT passes through a scratch column per CTA
+    int rmax = 0;
+    for (int q = 0; q < planM.npass; q++) rmax = std::max(rmax, planM.radix[q]);
+    if (rmax >= 32) {
+      BluesteinPass bs{};
+      AB_TRY(get_bluestein(ctx, rmax, &bs));
+      if (time_smem_bytes((int)nslice) + sizeof(float2) * (size_t)padded_len(bs.L) <= ctx->smem_optin) planM.bs = bs;
+    }
+    bool direct = false;
+    for (int q = 0; q < planM.npass; q++) {
+      const int r = planM.radix[q];
+      direct |= r != 2 && r != 3 && r != 4 && r != 5 && r != 7 && r != 8 && r != planM.bs.R;
+    }
+    if (direct) {
+      void* g = nullptr;
+      AB_TRY(get_scratch(ctx, kScratchDftPass, sizeof(float2) * (size_t)P * (size_t)planM.n, &g));
+      planM.gscratch = (float2*)g;
+    }
   }
   const float2 *twP, *twN;
   AB_TRY(get_twiddles(ctx, P, &twP));

@@ -4,12 +4,15 @@ cupy_ipfb :56-91, cupy_pfb :105-121, get_matft :123-137) and
 albatros_analysis/src/utils/pfb_utils.py (sinc_hamming :4-7), computed by the
 CUDA kernels of csrc/ipfb.cu and csrc/pfb.cu.
 
-The FFTs are this library's own shared-memory mixed-radix transforms
-(register butterflies of radix 2, 3, 4, 5, 7, 8; any other prime factor of
-an IPFB length runs as a direct DFT pass, correct for any even nslice but
-slow for large primes: 0.2 s for nslice 32788 = 4 * 7 * 1171 against 1.4 ms
-for 32928 = 2^5 * 3 * 7^3 on one GB300); lblock must factor into 2, 3, 5, 7;
-PFB lengths must be powers of two (lblock = 4096*osamp).
+The FFTs are this library's own shared-memory mixed-radix transforms:
+register butterflies of radix 2, 3, 4, 5, 7, 8; any other prime factor of an
+IPFB length runs by Bluestein's method (a chirp convolution through a
+7-smooth FFT in shared memory; smaller primes and the rare ones too long for
+shared memory as direct DFT passes), so cupy_ipfb runs any even nslice, like
+the reference's cuFFT: 10.6 ms for nslice 32788 = 4 * 7 * 1171 (the
+reference's default cut on 2^15 spectra) against 1.4 ms for 32928 =
+2^5 * 3 * 7^3 on one GB300.  lblock must factor into 2, 3, 5, 7; PFB lengths
+must be powers of two (lblock = 4096*osamp).
 """
 from __future__ import annotations
 

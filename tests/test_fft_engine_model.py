@@ -154,3 +154,39 @@ def test_direct_pass_twiddle_indices(R, S, T):
             if e >= R:
                 e -= R
     assert (S - 1) * (R - 1) * tstep < T
+
+
+def smooth_at_least(n):
+    """The smallest length >= n whose prime factors are 2, 3, 5, 7."""
+    while True:
+        m = n
+        for r in (2, 3, 5, 7):
+            while m % r == 0:
+                m //= r
+        if m == 1:
+            return n
+        n += 1
+
+
+@pytest.mark.parametrize("R", [1171, 1009, 2053, 37])
+def test_bluestein_pass_restatement(R):
+    """bluestein_pass (csrc/fft.cuh) with the tables of get_bluestein
+    (csrc/api.cu): a = x c (c_m = exp(-i pi (m^2 mod 2R) / R)), circular
+    convolution of length L (7-smooth, >= 2R - 1) with conj(c) wrapped around,
+    times c again, is the length-R DFT; the inverse as conj(DFT(conj x))."""
+    L = smooth_at_least(2 * R - 1)
+    m = np.arange(R)
+    c = np.exp(-1j * np.pi * ((m * m) % (2 * R)) / R)
+    b = np.zeros(L, complex)
+    b[:R] = np.conj(c)
+    b[L - R + 1:] = np.conj(c[1:][::-1])
+    filt = np.fft.fft(b) / L
+    rng = np.random.default_rng(R)
+    x = rng.standard_normal(R) + 1j * rng.standard_normal(R)
+    a = np.zeros(L, complex)
+    a[:R] = x * c
+    conv = np.fft.ifft(np.fft.fft(a) * filt) * L  # the engine's unnormalised inverse, filter carries 1/L
+    np.testing.assert_allclose(conv[:R] * c, np.fft.fft(x), atol=1e-9 * np.sqrt(R))
+    a[:R] = np.conj(x) * c
+    conv = np.fft.ifft(np.fft.fft(a) * filt) * L
+    np.testing.assert_allclose(np.conj(conv[:R] * c), R * np.fft.ifft(x), atol=1e-9 * np.sqrt(R))
