@@ -141,6 +141,7 @@ OPT_ROW_PREFETCH = 5
 OPT_COARSE_ENGINE = 6
 OPT_COARSE_TC_SLICE = 7
 OPT_PFB_TMA = 9
+OPT_FAULT_TEST = 10
 DEFAULT_ROW_PREFETCH = 2
 
 

@@ -39,8 +39,11 @@
 //     Gram entries into the int64 sums.
 // Every mbarrier wait is bounded (about 2 s of wall time); a thread whose wait
 // runs out sets the call's fault word, stops issuing work and drains, the
-// tensor memory is freed on every path, and the finalize kernel then writes
-// INT64_MIN to every output of the call (so a fault cannot pass for data).
+// tensor memory is freed on every path, CTAs starting after it do nothing,
+// and the finalize kernel then writes INT64_MIN to every output of the call
+// (so a fault cannot pass for data).  AB_OPT_FAULT_TEST makes the next call's
+// producers withhold their first stage, so that path can be tested without
+// a fault.
 #include <cuda_fp16.h>
 
 #include "async.cuh"
@@ -129,7 +132,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     coarse_xcorr_tc_kernel(const uint8_t* __restrict__ raw, int64_t ant_stride, int64_t row_bytes, int nant,
                            int64_t rowstart, int64_t nrows, const int32_t* __restrict__ rows,
                            const int64_t* __restrict__ channels, int ncols, int64_t chunk_rows, int64_t slice,
-                           int64_t slices_per_chunk, int Rp, long long* __restrict__ G, int* __restrict__ fault) {
+                           int64_t slices_per_chunk, int Rp, long long* __restrict__ G, int* __restrict__ fault,
+                           int withhold) {
   constexpr int CPC = kTcTiles * CPT;   // channels per CTA
   constexpr int BPT = 2 * CPC;          // packet bytes per (antenna, sample): CPC channels x 2 pols
   constexpr int WPT = BPT / 4;          // 32-bit words per (antenna, sample)
@@ -156,6 +160,13 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   const int64_t chunk_end = min((chunk + 1) * chunk_rows, nrows);
   const int64_t k_end = min(k_begin + slice, chunk_end);
   const int nst = k_end > k_begin ? (int)((k_end - k_begin + kTcKt - 1) / kTcKt) : 0;
+
+  // a call whose fault word is already set (an earlier CTA's wait ran out)
+  // does no more work: its outputs become INT64_MIN anyway
+  __shared__ int skip;
+  if (tid == 0) skip = *reinterpret_cast<volatile int*>(fault);
+  __syncthreads();
+  if (skip) return;
 
   // zero the stage ring once: rows of absent antennas and channels stay zero
   for (int i = tid; i < kTcStages * kTcStageBytes / 16; i += kTcThreads)
@@ -260,7 +271,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         }
       }
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      mbar_arrive(full_bar(slot));
+      if (!(withhold && s == 0)) mbar_arrive(full_bar(slot));  // withhold: failure-path test, the MMA wait runs out
     }
   } else if (lane == 0) {
     // ---------------- MMA issuer ----------------
@@ -343,18 +354,24 @@ int launch_coarse_tc(ab_ctx* ctx, const uint8_t* raw, int64_t ant_stride, int64_
                "coarse xcorr (tensor cores): %lld chunks x %lld slices exceed the grid limit; use larger chunks",
                (long long)nchunks, (long long)spc);
   dim3 grid((unsigned)groups, (unsigned)(nchunks * spc));
+  int withhold = 0;
+  {
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    withhold = ctx->test_withhold_stage;
+    ctx->test_withhold_stage = 0;  // one call only
+  }
   if (cpt == 2) {
     AB_CUDA(cudaFuncSetAttribute(coarse_xcorr_tc_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)kTcSmemBytes));
     coarse_xcorr_tc_kernel<2><<<grid, kTcThreads, kTcSmemBytes, s>>>(raw, ant_stride, 2 * nchan, (int)nant, rowstart,
                                                                      nrows, rows, channels, (int)ncols, chunk_rows,
-                                                                     slice, spc, Rp, G, fault);
+                                                                     slice, spc, Rp, G, fault, withhold);
   } else {
     AB_CUDA(cudaFuncSetAttribute(coarse_xcorr_tc_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)kTcSmemBytes));
     coarse_xcorr_tc_kernel<1><<<grid, kTcThreads, kTcSmemBytes, s>>>(raw, ant_stride, 2 * nchan, (int)nant, rowstart,
                                                                      nrows, rows, channels, (int)ncols, chunk_rows,
-                                                                     slice, spc, Rp, G, fault);
+                                                                     slice, spc, Rp, G, fault, withhold);
   }
   AB_LAUNCH_CHECK();
   return AB_OK;

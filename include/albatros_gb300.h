@@ -101,6 +101,12 @@ int ab_ctx_set_time_filter(ab_ctx *ctx, int32_t mode, int32_t row_tile);
  * fetch the next tile with TMA while transforming the current one.  The
  * arithmetic is the same (bitwise the same output).  Read at each push. */
 #define AB_OPT_PFB_TMA 9
+/* AB_OPT_FAULT_TEST: 1 makes the next call of the tcgen05 coarse correlator
+ * test its failure path without any fault: its producers withhold their
+ * first stage, so the MMA thread's bounded wait (about 2 s) runs out, the
+ * call's outputs are all INT64_MIN, and the tensor memory is freed.  The
+ * setting applies to one call. */
+#define AB_OPT_FAULT_TEST 10
 int ab_ctx_set_option(ab_ctx *ctx, int32_t option, int32_t value);
 
 /* ---- unpacking ----------------------------------------------------------

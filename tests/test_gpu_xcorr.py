@@ -180,6 +180,28 @@ def test_coarse_xcorr_tcgen05_row_lists(tc_engine):
     np.testing.assert_array_equal(im.cpu().numpy()[0], ei)
 
 
+def test_coarse_xcorr_tcgen05_wait_timeout_reports_fault(tc_engine):
+    """Failure path of the tcgen05 correlator's bounded waits, without a GPU
+    fault: the producers withhold their first stage (nothing ever signals it),
+    the MMA thread's wait runs out after about 2 s, and the call returns with
+    every output INT64_MIN; the tensor memory was freed, so the next call is
+    exact again."""
+    import time
+    from albatros_axion_detection_gb300 import _lib, autotune
+    from albatros_axion_detection_gb300.correlations import xcorr_coarse_4bit
+    raw = gen.raw_4bit_uniform(seed=99, nspec=4096, nchan=16, nant=12)
+    _lib.call("ab_ctx_set_option", _lib.ctx(), autotune.OPT_FAULT_TEST, 1)
+    t0 = time.time()
+    re, im = xcorr_coarse_4bit(cu(raw), 0, 4096, np.arange(16), 16, average=False)
+    re, im = re.cpu().numpy(), im.cpu().numpy()
+    assert time.time() - t0 < 30
+    assert np.all(re == np.iinfo(np.int64).min) and np.all(im == np.iinfo(np.int64).min)
+    re, im = xcorr_coarse_4bit(cu(raw), 0, 4096, np.arange(16), 16, average=False)
+    er, ei = io.xcorr_all_ant_4bit(raw, 0, 4096, np.arange(16), 16)
+    np.testing.assert_array_equal(re.cpu().numpy()[0], er)
+    np.testing.assert_array_equal(im.cpu().numpy()[0], ei)
+
+
 def test_coarse_xcorr_worst_case_magnitudes(mma_bits):
     """All nibbles 0x8 (+8): the largest products, exact in the int32 / fp32
     partial sums (4096 samples x 64 per CTA slice)."""
