@@ -2,8 +2,9 @@
 
 The IPFB time-axis deconvolution has three forms in the library.  The IIR and
 FIR forms (the default wherever the reference's Wiener filter decays fast
-enough; IIR first) have one tunable tile: the kept rows per thread (16 or 32), which sets
-the rows a CTA filters and how many CTAs share an SM.  The FFT form runs one real FFT of
+enough; IIR first) have one tunable tile: the kept rows per thread (16, 32 or,
+for the IIR form, 64), which sets the rows a CTA filters and how many CTAs
+share an SM.  The FFT form runs one real FFT of
 nslice = acclen + 2*cut points per coarse sample phase (a complex FFT of
 n = nslice/2 points) and its inverse; two lengths have compile-time plans
 (n = 16464 for acclen 2^15, cut 80, and n = 16384), every other length runs
@@ -127,7 +128,7 @@ def set_time_filter(mode: int = DEFAULT_MODE, row_tile: int = 0, device: Optiona
     """Time stage of streams created from now on: mode 0 = IIR where the
     filter factors and decays fast enough, else FIR where it is accurate,
     else FFT (the default); 1 = FFT only; 2 = FFT where its length factors,
-    else IIR or FIR; 3 = FIR, else FFT.  row_tile 16/32 (0 keeps it)."""
+    else IIR or FIR; 3 = FIR, else FFT.  row_tile 16/32/64 (0 keeps it)."""
     _lib.call("ab_ctx_set_time_filter", _lib.ctx(device), int(mode), int(row_tile))
     _filter_setting["mode"] = int(mode)
     if row_tile:
@@ -270,7 +271,7 @@ def tune_time_fft(acclen: int, cut: int, osamp: int = 64, *, use_cache: bool = T
 def tune_time_stage(acclen: int, cut: int, osamp: int = 64, *, use_cache: bool = True, limit: int = 24,
                     verbose: bool = False) -> Dict[str, object]:
     """Choose the time stage for (acclen, cut, osamp): the IIR or FIR form with
-    either row tile, or the FFT form with its tuned radix order, whichever is
+    each of its row tiles, or the FFT form with its tuned radix order, whichever is
     fastest on this device.  Returns {"mode", "row_tile", "radices", "ms",
     "form"}; ``apply`` installs it."""
     _lib.require_cuda()
@@ -282,7 +283,7 @@ def tune_time_stage(acclen: int, cut: int, osamp: int = 64, *, use_cache: bool =
         return hit
     cands = []
     for mode, kind in ((0, "iir"), (3, "fir")):
-        for tile in (32, 16):
+        for tile in ((64, 32, 16) if kind == "iir" else (32, 16)):  # FIR runs tile 64 as 32
             ms, form = _time_chain(acclen, cut, osamp, mode=mode, row_tile=tile)
             if form[0] != kind:
                 break  # this form does not apply to the filter

@@ -440,7 +440,8 @@ int ab_ctx_set_time_filter(ab_ctx* ctx, int32_t mode, int32_t row_tile) {
   AB_CHECK_ARG(ctx, "ab_ctx_set_time_filter: NULL context");
   AB_CHECK_ARG(mode >= 0 && mode <= 3,
                "ab_ctx_set_time_filter: mode must be 0 (IIR/FIR first), 1 (FFT only), 2 (FFT first) or 3 (FIR)");
-  AB_CHECK_ARG(row_tile == 0 || row_tile == 16 || row_tile == 32, "ab_ctx_set_time_filter: row_tile must be 0, 16 or 32");
+  AB_CHECK_ARG(row_tile == 0 || row_tile == 16 || row_tile == 32 || row_tile == 64,
+               "ab_ctx_set_time_filter: row_tile must be 0, 16, 32 or 64");
   std::lock_guard<std::mutex> lk(ctx->mu);
   ctx->time_filter_mode = mode;
   if (row_tile) ctx->fir_row_tile = row_tile;

@@ -236,9 +236,10 @@ int get_fir_taps(ab_ctx* ctx, int P, int N, int ntap, float thresh, int* J_out, 
 // state is carried over at least IW rows, after which 1/A's impulse response
 // is below 1e-10 of its peak, and the rest of its effect is dropped.
 // Per-column IIR coefficients: g w0..g w3, a1..a3, 0, then 1/A's impulse
-// response h[U-5..U-1] for the two row tiles' U (state advance over one
+// response h[U-5..U-1] for the three row tiles' U (state advance over one
 // thread's rows), each padded to 8 floats.
-constexpr int kIirU32 = 41, kIirU16 = 21, kIirCoef = 24;
+constexpr int kIirU64 = 67, kIirU32 = 41, kIirU16 = 21, kIirCoef = 32;
+__host__ __device__ constexpr int iir_hh_offset(int U) { return U == kIirU64 ? 24 : U == kIirU32 ? 8 : 16; }
 
 static bool iir_factor(const double* w, double t, double coef[kIirCoef], int* carry) {
   const int m = 3;
@@ -316,8 +317,9 @@ static bool iir_factor(const double* w, double t, double coef[kIirCoef], int* ca
   coef[6] = a3;
   for (int k = 7; k < kIirCoef; k++) coef[k] = 0.0;
   for (int i = 0; i < 5; i++) {
-    coef[8 + i] = h[kIirU32 - 5 + i];
-    coef[16 + i] = h[kIirU16 - 5 + i];
+    coef[iir_hh_offset(kIirU32) + i] = h[kIirU32 - 5 + i];
+    coef[iir_hh_offset(kIirU16) + i] = h[kIirU16 - 5 + i];
+    coef[iir_hh_offset(kIirU64) + i] = h[kIirU64 - 5 + i];
   }
   return true;
 }
@@ -393,7 +395,7 @@ int get_iir_coeffs(ab_ctx* ctx, int P, int ntap, float thresh, int* W_out, const
 // O/2 points plus the real-input untangle), then writes the O packed floats
 // of W with 32-byte stores.
 constexpr int kFirThreads = 256;
-constexpr int kYPad = 3;  // pad floats per O rows of the y buffer (yidx)
+constexpr int kYPad = 2;  // pad floats per O rows of the y buffer (yidx); even, for the fold's pair loads
 
 __constant__ float2 c_fir_tw[64];  // exp(-2 pi i k / 64)
 
@@ -550,11 +552,15 @@ __device__ __forceinline__ void prefetch_item_extras(float* st_taps, int K, int 
 
 // y rows are padded kYPad floats per O rows, with the pads at the fine
 // blocks' first rows (y row phi + k*O): a block's 4*O rows then sit at
-// base + c + kYPad*(c/O) for compile-time c; blocks O + kYPad floats apart
-// fall in distinct banks (one lane per block), and the filter's stores of
-// lanes U rows apart meet at most 2-way conflicts at osamp 64 for U = 21 and
-// 41 (at most 4-way at the other osamp values; a 1-float pad gives 3-way at
-// U = 41, 11-way at U = 21).  (Two lanes per block, each
+// base + c + kYPad*(c/O) for compile-time c.  The kernels index the y
+// buffer from a base shifted by phi & 1 floats, so every block starts on an
+// 8-byte boundary and the fold reads rows in pairs; blocks O + 2 floats (an
+// odd number of 8-byte units) apart fall in distinct banks (one lane per
+// block), and the filter's stores of lanes U rows apart meet at most 2-way
+// conflicts at osamp 64 for U = 21 and 41 (a 1-float pad gives 3-way at
+// U = 41, 11-way at U = 21).  Pair loads halve the fold's shared loads
+// against a 3-float pad read one float at a time, with the same FMAs in the
+// same order.  (Two lanes per block, each
 // taking half the FFT, removed the fold's idle threads but met 2-way
 // conflicts on every y load and cost more than it saved.)
 template <int O>
@@ -566,81 +572,96 @@ __device__ __forceinline__ int y_phase(const FirItem& it, const FoldArgs& fa) {
   return (((4 * O - it.s0 + (int)fa.row0) % O) + O) % O;
 }
 
-// Fold + real DFT of the fine blocks whose last row lies in [s0, s0 + S)
-// (the last segment: >= s0), from the item's y rows (y row q = kept row
-// q - 4*O + s0), one block per thread; then the last segment keeps the
-// chunk's last 4*O rows as the next chunk's tail.
+// Fine blocks an item folds: those whose last row lies in [s0, s0 + S) (the
+// last segment: >= s0), as [b0, b1).
 template <int O>
-__device__ __forceinline__ void fold_item_blocks(const float* ys, int phi, const float4* wt, const FirItem& it,
-                                                 const FoldArgs& fa, int P, int S, int acclen,
-                                                 float* __restrict__ state_out, int tid) {
-  constexpr int NC = O / 2, LOGNC = ilog2(NC);
-  constexpr int GW = O < 8 ? O : 8;
+__device__ __forceinline__ void fold_block_range(const FirItem& it, const FoldArgs& fa, int S, int* b0, int* b1) {
   const int row0 = (int)fa.row0, nb = (int)fa.nb;
   auto first_block_ending_at_or_after = [&](int r) -> int {  // min b with row0 + b*O + 4O - 1 >= r
     const int num = r - 4 * O + 1 - row0;
     const int b = num <= 0 ? 0 : (num + O - 1) / O;
     return min(b, nb);
   };
-  const int b0 = it.first ? 0 : first_block_ending_at_or_after(it.s0);
-  const int b1 = it.last ? nb : first_block_ending_at_or_after(it.s0 + S);
-  float* wout = fa.W + (int64_t)it.in * fa.nb * ((int64_t)O * P) + (int64_t)it.n * GW;
-  for (int b = b0 + tid; b < b1; b += kFirThreads) {
-    const int rfirst = row0 + b * O;
-    float* wb = wout + (int64_t)b * ((int64_t)O * P);
-    if (rfirst >= it.s1) {  // entirely past the end of the stream
-#pragma unroll
-      for (int p = 0; p < O; p += GW) {
-        float* dst = wb + (int64_t)(p / GW) * P * GW;
-        if constexpr (GW == 8) st_global_v8(dst, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f);
-        else *reinterpret_cast<float4*>(dst) = make_float4(0.f, 0.f, 0.f, 0.f);
-      }
-      continue;
-    }
-    const int q0 = 4 * O - it.s0 + rfirst;  // y row of the block's first row (= phi mod O)
-    const float* yb = ys + yidx<O>(q0, phi);  // rows q0 + c at yb[c + kYPad*(c/O)]
-    float2 a[NC];
-#pragma unroll
-    for (int m = 0; m < NC; m++) {
-      float zz[2];
-#pragma unroll
-      for (int e = 0; e < 2; e++) {
-        const int tp = 2 * m + e;
-        const float4 w4 = wt[tp];
-        zz[e] = fmaf(w4.x, yb[tp], fmaf(w4.y, yb[tp + (O + kYPad)],
-                                        fmaf(w4.z, yb[tp + 2 * (O + kYPad)], w4.w * yb[tp + 3 * (O + kYPad)])));
-      }
-      a[m] = make_float2(zz[0], zz[1]);
-    }
-    reg_fft_dif<NC>(a);
-    // untangle the real input: W_k = (Z_k + conj Z_{NC-k})/2 + w^k (Z_k - conj Z_{NC-k})/(2i);
-    // packed floats p = 2k, 2k+1 ((W_0, W_{O/2}) at p = 0, 1), one group of
-    // GW floats per store (a whole 32-byte sector when GW = 8)
+  *b0 = it.first ? 0 : first_block_ending_at_or_after(it.s0);
+  *b1 = it.last ? nb : first_block_ending_at_or_after(it.s0 + S);
+}
+
+// Fold + real DFT of fine block b of an item from its y rows (y row q = kept
+// row q - 4*O + s0), by one thread: the 4 taps fold into O samples, whose
+// real DFT is a compile-time radix-2 FFT of O/2 points plus the real-input
+// untangle, written as O packed floats of W with 32-byte stores.
+template <int O>
+__device__ __forceinline__ void fold_one_block(const float* ys, int phi, const float4* wt, const FirItem& it,
+                                               const FoldArgs& fa, int P, int b) {
+  constexpr int NC = O / 2, LOGNC = ilog2(NC);
+  constexpr int GW = O < 8 ? O : 8;
+  const int rfirst = (int)fa.row0 + b * O;
+  float* wb = fa.W + (int64_t)it.in * fa.nb * ((int64_t)O * P) + (int64_t)it.n * GW + (int64_t)b * ((int64_t)O * P);
+  if (rfirst >= it.s1) {  // entirely past the end of the stream
 #pragma unroll
     for (int p = 0; p < O; p += GW) {
-      float2 o[GW / 2];
-#pragma unroll
-      for (int h = 0; h < GW / 2; h++) {
-        const int k = p / 2 + h;
-        if (k == 0) {
-          o[h] = make_float2(a[0].x + a[0].y, a[0].x - a[0].y);
-        } else {
-          const float2 z = a[bitrev(k, LOGNC)], c = cconj(a[bitrev(NC - k, LOGNC)]);
-          const float2 E = cscale(cadd(z, c), 0.5f);
-          const float2 Dd = csub(z, c);
-          const float2 Od = make_float2(0.5f * Dd.y, -0.5f * Dd.x);
-          o[h] = cadd(E, cmul(c_fir_tw[k * (64 / O)], Od));
-        }
-      }
       float* dst = wb + (int64_t)(p / GW) * P * GW;
-      if constexpr (GW == 8) st_global_v8(dst, o[0].x, o[0].y, o[1].x, o[1].y, o[2].x, o[2].y, o[3].x, o[3].y);
-      else *reinterpret_cast<float4*>(dst) = make_float4(o[0].x, o[0].y, o[1].x, o[1].y);
+      if constexpr (GW == 8) st_global_v8(dst, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f);
+      else *reinterpret_cast<float4*>(dst) = make_float4(0.f, 0.f, 0.f, 0.f);
     }
+    return;
   }
-  if (it.last) {
-    float* st = state_out + ((int64_t)it.in * P + it.n) * (4 * O);
-    for (int i = tid; i < 4 * O; i += kFirThreads) st[i] = ys[yidx<O>(4 * O - it.s0 + (acclen - 4 * O + i), phi)];
+  const int q0 = 4 * O - it.s0 + rfirst;  // y row of the block's first row (= phi mod O)
+  // rows q0 + c at yb[c + kYPad*(c/O)]; yb is 8-byte aligned (ys is shifted
+  // by phi & 1), so the rows 2m, 2m+1 of each tap come as one float2
+  const float2* yb = reinterpret_cast<const float2*>(ys + yidx<O>(q0, phi));
+  float2 a[NC];
+#pragma unroll
+  for (int m = 0; m < NC; m++) {
+    const float2 y0 = yb[m], y1 = yb[m + (O + kYPad) / 2], y2 = yb[m + (O + kYPad)],
+                 y3 = yb[m + 3 * (O + kYPad) / 2];
+    const float4 wa = wt[2 * m], wb4 = wt[2 * m + 1];
+    a[m] = make_float2(fmaf(wa.x, y0.x, fmaf(wa.y, y1.x, fmaf(wa.z, y2.x, wa.w * y3.x))),
+                       fmaf(wb4.x, y0.y, fmaf(wb4.y, y1.y, fmaf(wb4.z, y2.y, wb4.w * y3.y))));
   }
+  reg_fft_dif<NC>(a);
+  // untangle the real input: W_k = (Z_k + conj Z_{NC-k})/2 + w^k (Z_k - conj Z_{NC-k})/(2i);
+  // packed floats p = 2k, 2k+1 ((W_0, W_{O/2}) at p = 0, 1), one group of
+  // GW floats per store (a whole 32-byte sector when GW = 8)
+#pragma unroll
+  for (int p = 0; p < O; p += GW) {
+    float2 o[GW / 2];
+#pragma unroll
+    for (int h = 0; h < GW / 2; h++) {
+      const int k = p / 2 + h;
+      if (k == 0) {
+        o[h] = make_float2(a[0].x + a[0].y, a[0].x - a[0].y);
+      } else {
+        const float2 z = a[bitrev(k, LOGNC)], c = cconj(a[bitrev(NC - k, LOGNC)]);
+        const float2 E = cscale(cadd(z, c), 0.5f);
+        const float2 Dd = csub(z, c);
+        const float2 Od = make_float2(0.5f * Dd.y, -0.5f * Dd.x);
+        o[h] = cadd(E, cmul(c_fir_tw[k * (64 / O)], Od));
+      }
+    }
+    float* dst = wb + (int64_t)(p / GW) * P * GW;
+    if constexpr (GW == 8) st_global_v8(dst, o[0].x, o[0].y, o[1].x, o[1].y, o[2].x, o[2].y, o[3].x, o[3].y);
+    else *reinterpret_cast<float4*>(dst) = make_float4(o[0].x, o[0].y, o[1].x, o[1].y);
+  }
+}
+
+// The last segment keeps the chunk's last 4*O rows as the next chunk's tail.
+template <int O>
+__device__ __forceinline__ void fold_tail_state(const float* ys, int phi, const FirItem& it, int P, int acclen,
+                                                float* __restrict__ state_out, int tid) {
+  float* st = state_out + ((int64_t)it.in * P + it.n) * (4 * O);
+  for (int i = tid; i < 4 * O; i += kFirThreads) st[i] = ys[yidx<O>(4 * O - it.s0 + (acclen - 4 * O + i), phi)];
+}
+
+// All of an item's fine blocks, one per thread, then its tail state.
+template <int O>
+__device__ __forceinline__ void fold_item_blocks(const float* ys, int phi, const float4* wt, const FirItem& it,
+                                                 const FoldArgs& fa, int P, int S, int acclen,
+                                                 float* __restrict__ state_out, int tid) {
+  int b0, b1;
+  fold_block_range<O>(it, fa, S, &b0, &b1);
+  for (int b = b0 + tid; b < b1; b += kFirThreads) fold_one_block<O>(ys, phi, wt, it, fa, P, b);
+  if (it.last) fold_tail_state<O>(ys, phi, it, P, acclen, state_out, tid);
 }
 
 // y rows that do not come from the filter: the previous chunk's tail (first
@@ -695,7 +716,8 @@ __global__ void __launch_bounds__(kFirThreads, J <= 32 ? 2 : 1)
     const FirItem it = fir_item(item, nseg, P, S, acclen, O);
     const int yoff = it.ylo - it.s0 + 4 * O;  // y row of computed row ylo
     const int phi = y_phase<O>(it, fa);
-    y_edges<O>(ys, phi, stage + Lay::XS + Lay::TAPS, it, yoff, tid);
+    float* ysb = ys + (phi & 1);  // blocks start on 8-byte boundaries (yidx)
+    y_edges<O>(ysb, phi, stage + Lay::XS + Lay::TAPS, it, yoff, tid);
     // y[ylo + i] = sum_j h[j + J] x[cut + ylo + i - j] = sum_k h[k] xs[i + 2J - k]
     if (tid * U < it.nrows) {
       float h[K];
@@ -717,10 +739,10 @@ __global__ void __launch_bounds__(kFirThreads, J <= 32 ? 2 : 1)
       const int t0 = yoff + tid * U;
       const int nv = it.nrows - tid * U;
 #pragma unroll
-      for (int g = 0; g < U; g++) ys[g < nv ? yidx<O>(t0 + g, phi) : Lay::YS - 1] = acc[g];  // spare slot past nrows
+      for (int g = 0; g < U; g++) ysb[g < nv ? yidx<O>(t0 + g, phi) : Lay::YS - 2] = acc[g];  // spare slot past nrows
     }
     __syncthreads();
-    fold_item_blocks<O>(ys, phi, reinterpret_cast<const float4*>(stage + Lay::XS + Lay::TAPS + Lay::ST), it, fa, P,
+    fold_item_blocks<O>(ysb, phi, reinterpret_cast<const float4*>(stage + Lay::XS + Lay::TAPS + Lay::ST), it, fa, P,
                         S, acclen, state_out, tid);
     __syncthreads();  // ys and this staging buffer are reused next
   }
@@ -778,8 +800,12 @@ __device__ __forceinline__ Iir3 iir_incoming(const float* z, int k, int dir, int
   return s;
 }
 
+// CTAs per SM: two for the 21- and 41-row tiles, one for the 67-row tile
+// (its two staging buffers take 150-210 KB of shared memory).
+__host__ __device__ constexpr int iir_ctas_per_sm(int U) { return U > kIirU32 ? 1 : 2; }
+
 template <int U, int G, int D>
-__global__ void __launch_bounds__(kFirThreads, 2)
+__global__ void __launch_bounds__(kFirThreads, iir_ctas_per_sm(U))
     iir_fold_kernel(const float* __restrict__ data, int64_t ld, int P, int nslice, int cut, int acclen, int S,
                     int nseg, int nitems, const float* __restrict__ coef, FoldArgs fa,
                     const float* __restrict__ state_in, float* __restrict__ state_out) {
@@ -820,7 +846,7 @@ __global__ void __launch_bounds__(kFirThreads, 2)
     const float* cf = stage + Lay::XS;
     const float w0 = cf[0], w1 = cf[1], w2 = cf[2], w3 = cf[3];
     const float a1 = cf[4], a2 = cf[5], a3 = cf[6];
-    const float* hh = cf + (U == kIirU32 ? 8 : 16);
+    const float* hh = cf + iir_hh_offset(U);
     float u[U];
     Iir3 s = {0.f, 0.f, 0.f};
     if (tid < nthr) {
@@ -848,9 +874,9 @@ __global__ void __launch_bounds__(kFirThreads, 2)
     zf[2 * kFirThreads + tid] = s.p3;
     __syncthreads();
     // the x window is dead: y rows go over it
-    float* ys = stage;
     const int yoff = it.ylo - it.s0 + 4 * O;  // y row of computed row ylo
     const int phi = y_phase<O>(it, fa);
+    float* ys = stage + (phi & 1);  // blocks start on 8-byte boundaries (yidx)
     y_edges<O>(ys, phi, stage + Lay::XS + Lay::TAPS, it, yoff, tid);
     Iir3 q = {0.f, 0.f, 0.f};
     if (tid < nthr) {
@@ -933,7 +959,7 @@ static int launch_iir_t(const FirArgs& a, const FoldArgs& fa, cudaStream_t s) {
   AB_CHECK_ARG(nitems < (1LL << 31), "IIR time stage: too many work items");
   const size_t smem = Lay::bytes();
   AB_CUDA(cudaFuncSetAttribute(iir_fold_kernel<U, G, D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  const int64_t grid = std::min<int64_t>(nitems, 2 * (int64_t)std::max(a.num_sms, 1));
+  const int64_t grid = std::min<int64_t>(nitems, iir_ctas_per_sm(U) * (int64_t)std::max(a.num_sms, 1));
   iir_fold_kernel<U, G, D><<<(unsigned)grid, kFirThreads, smem, s>>>(a.data, a.ld, a.P, a.nslice, a.cut, a.acclen, S,
                                                                      nseg, (int)nitems, a.taps, fa, a.state_in,
                                                                      a.state_out);
@@ -972,22 +998,26 @@ static int launch_iir_o(const FirArgs& a, const FoldArgs& fa, cudaStream_t s) {
 int launch_fir_fold(const FirArgs& a, const FoldArgs& fa, cudaStream_t s) {
   AB_CHECK_ARG(fa.ntap == 4, "FIR time stage: needs ntap = 4");
   AB_CHECK_ARG(a.P <= 65535 && a.ninputs <= 65535, "FIR time stage: grid too large");
-  AB_CHECK_ARG(a.row_tile == 16 || a.row_tile == 32, "FIR time stage: row tile must be 16 or 32");
+  AB_CHECK_ARG(a.row_tile == 16 || a.row_tile == 32 || a.row_tile == 64,
+               "FIR time stage: row tile must be 16, 32 or 64");
   AB_CHECK_ARG(a.num_sms > 0, "FIR time stage: SM count unknown");
   AB_CHECK_ARG(a.row_tile * kFirThreads > 4 * fa.O, "FIR time stage: row tile too small for osamp %d", fa.O);
   AB_CHECK_ARG(((uintptr_t)fa.W & 31) == 0 && (a.P % 4) == 0, "FIR time stage: W must be 32-byte aligned");
   // odd rows per thread keep the shared loads of lanes U rows apart
   // conflict-free without padding.  IIR: D = ceil(IW / U) exchanged states.
   if (a.iir_w > 0) {
-    const int U = a.row_tile == 32 ? kIirU32 : kIirU16;
+    const int U = a.row_tile == 64 ? kIirU64 : a.row_tile == 32 ? kIirU32 : kIirU16;
     const int D = (a.iir_w + U - 1) / U;
+    if (U == kIirU64 && D == 1) return launch_iir_o<kIirU64, 1>(a, fa, s);
+    if (U == kIirU64 && D == 2) return launch_iir_o<kIirU64, 2>(a, fa, s);
     if (U == kIirU32 && D == 1) return launch_iir_o<kIirU32, 1>(a, fa, s);
     if (U == kIirU32 && D == 2) return launch_iir_o<kIirU32, 2>(a, fa, s);
     if (U == kIirU16 && D == 2) return launch_iir_o<kIirU16, 2>(a, fa, s);
     if (U == kIirU16 && D == 4) return launch_iir_o<kIirU16, 4>(a, fa, s);
   } else {
-    if (a.J == 32) return a.row_tile == 32 ? launch_fir_o<32, 33>(a, fa, s) : launch_fir_o<32, 17>(a, fa, s);
-    if (a.J == 64) return a.row_tile == 32 ? launch_fir_o<64, 33>(a, fa, s) : launch_fir_o<64, 17>(a, fa, s);
+    // the FIR form has two row tiles; 64 takes the larger
+    if (a.J == 32) return a.row_tile >= 32 ? launch_fir_o<32, 33>(a, fa, s) : launch_fir_o<32, 17>(a, fa, s);
+    if (a.J == 64) return a.row_tile >= 32 ? launch_fir_o<64, 33>(a, fa, s) : launch_fir_o<64, 17>(a, fa, s);
   }
   set_error("FIR time stage: J = %d / IW = %d not supported", a.J, a.iir_w);
   return AB_ERR_UNSUPPORTED;

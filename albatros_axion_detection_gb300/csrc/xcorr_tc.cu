@@ -139,6 +139,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   constexpr int WPT = BPT / 4;          // 32-bit words per (antenna, sample)
   constexpr int ROWS = 128 / CPT;       // tile rows per channel
   constexpr int NA = ROWS / 4;          // antennas a channel's rows can hold
+  constexpr int IPT = NA * 8 / kTcGroup;  // (antenna, 8-sample group) items per producer thread
+  static_assert(IPT * kTcGroup == NA * 8, "items must divide evenly over a producer group");
   extern __shared__ uint8_t smem_raw[];
   // 1024-byte aligned stage ring (the swizzle atoms), then the barriers
   const uint32_t raw_s = smem_u32(smem_raw);
@@ -201,40 +203,36 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 #pragma unroll
       for (int j = 1; j < CPC; j++) vec = vec && channels[c0 + j] == ch0 + j;
     }
-    bool ok = true;
-    for (int s = g; s < nst && ok; s += 2) {
-      const int slot = s % kTcStages, use = s / kTcStages;
-      if (use > 0 && !mbar_wait(empty_bar(slot), (uint32_t)((use - 1) & 1))) {
-        atomicExch(fault, 1);
-        ok = false;
-        break;
-      }
-      uint8_t* stage = stages + slot * kTcStageBytes;
+    // The packet words of one stage for this thread's IPT items (antenna,
+    // 8-sample group): 8 samples x WPT words each, zero past the slice end
+    // and for absent antennas.  A stage's words are loaded before the
+    // previous stage of the group is decoded, so the loads stay in flight
+    // while the thread decodes.
+    auto load_stage = [&](int s, uint32_t (&w)[IPT][8][WPT]) {
       const int64_t kt = k_begin + (int64_t)s * kTcKt;
-      for (int item = pt; item < NA * 8; item += kTcGroup) {
-        const int ant = item >> 3, kc = item & 7;
-        if (ant >= nant) continue;  // its rows stay zero
-        uint32_t w[8][WPT];
+#pragma unroll
+      for (int it = 0; it < IPT; it++) {
+        const int item = pt + it * kTcGroup, ant = item >> 3, kc = item & 7;
 #pragma unroll
         for (int i = 0; i < 8; i++) {
-          const int64_t k = kt + 8 * kc + i;
 #pragma unroll
-          for (int q = 0; q < WPT; q++) w[i][q] = 0u;
-          if (k < k_end) {
+          for (int q = 0; q < WPT; q++) w[it][i][q] = 0u;
+          const int64_t k = kt + 8 * kc + i;
+          if (ant < nant && s < nst && k < k_end) {
             const int64_t r = rows ? (int64_t)rows[(int64_t)ant * nrows + k] : rowstart + k;
             const uint8_t* src = raw + (int64_t)ant * ant_stride + r * row_bytes;
             if (vec) {
               const uint8_t* p = src + 2 * channels[c0];
               if constexpr (WPT == 4) {
                 const uint4 v = __ldg(reinterpret_cast<const uint4*>(p));
-                w[i][0] = v.x;
-                w[i][1] = v.y;
-                w[i][2] = v.z;
-                w[i][3] = v.w;
+                w[it][i][0] = v.x;
+                w[it][i][1] = v.y;
+                w[it][i][2] = v.z;
+                w[it][i][3] = v.w;
               } else {
                 const uint2 v = __ldg(reinterpret_cast<const uint2*>(p));
-                w[i][0] = v.x;
-                w[i][1] = v.y;
+                w[it][i][0] = v.x;
+                w[it][i][1] = v.y;
               }
             } else {
 #pragma unroll
@@ -244,13 +242,34 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                   const uint8_t* p = src + 2 * channels[c0 + j];
                   b2 = (uint32_t)__ldg(p) | ((uint32_t)__ldg(p + 1) << 8);
                 }
-                w[i][j >> 1] |= b2 << (16 * (j & 1));
+                w[it][i][j >> 1] |= b2 << (16 * (j & 1));
               }
             }
           }
-#pragma unroll
-          for (int q = 0; q < WPT; q++) w[i][q] = nib_plus7(w[i][q]);
         }
+      }
+    };
+    uint32_t w[IPT][8][WPT];
+    load_stage(g, w);
+    bool ok = true;
+    for (int s = g; s < nst && ok; s += 2) {
+      const int slot = s % kTcStages, use = s / kTcStages;
+      uint32_t wn[IPT][8][WPT];
+      load_stage(s + 2, wn);  // nothing past the last stage
+      if (use > 0 && !mbar_wait(empty_bar(slot), (uint32_t)((use - 1) & 1))) {
+        atomicExch(fault, 1);
+        ok = false;
+        break;
+      }
+      uint8_t* stage = stages + slot * kTcStageBytes;
+#pragma unroll
+      for (int it = 0; it < IPT; it++) {
+        const int item = pt + it * kTcGroup, ant = item >> 3, kc = item & 7;
+        if (ant >= nant) continue;  // its rows stay zero
+#pragma unroll
+        for (int i = 0; i < 8; i++)
+#pragma unroll
+          for (int q = 0; q < WPT; q++) w[it][i][q] = nib_plus7(w[it][i][q]);
         // byte b = 2 j + pol of channel j: high nibble -> row (.., re), low -> (.., im)
 #pragma unroll
         for (int b = 0; b < BPT; b++) {
@@ -261,7 +280,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
           uint32_t re[4], im[4];
 #pragma unroll
           for (int m = 0; m < 4; m++) {
-            const uint32_t p = __byte_perm(w[2 * m][b >> 2], w[2 * m + 1][b >> 2], sel);
+            const uint32_t p = __byte_perm(w[it][2 * m][b >> 2], w[it][2 * m + 1][b >> 2], sel);
             im[m] = nib_to_h2(p);
             re[m] = nib_to_h2(p >> 4);
           }
@@ -272,6 +291,12 @@ __global__ void __launch_bounds__(kTcThreads, 1)
       }
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       if (!(withhold && s == 0)) mbar_arrive(full_bar(slot));  // withhold: failure-path test, the MMA wait runs out
+#pragma unroll
+      for (int it = 0; it < IPT; it++)
+#pragma unroll
+        for (int i = 0; i < 8; i++)
+#pragma unroll
+          for (int q = 0; q < WPT; q++) w[it][i][q] = wn[it][i][q];
     }
   } else if (lane == 0) {
     // ---------------- MMA issuer ----------------

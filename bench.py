@@ -701,7 +701,7 @@ def main():
     ap.add_argument("--lanes", type=int, default=4, help="uneven-batch: concurrent CUDA streams")
     ap.add_argument("--time-filter", default="default", choices=["default", "iir", "fir", "fft"],
                     help="stream: IPFB time stage form (default: the library's choice)")
-    ap.add_argument("--row-tile", type=int, default=0, help="stream: IIR / FIR row tile (16 or 32)")
+    ap.add_argument("--row-tile", type=int, default=0, help="stream: IIR / FIR row tile (16, 32 or 64)")
     ap.add_argument("--row-ffts", type=int, default=0, help="stream: spectra per row-stage CTA (8, 4 or 2)")
     ap.add_argument("--pfb-tma", type=int, default=-1,
                     help="stream: PFB band DFT tile fetch: 0 plain loads (default), 1 TMA into the FFT buffers, "

@@ -63,7 +63,8 @@ int ab_ctx_set_fft_plan(ab_ctx *ctx, int64_t n, const int32_t *radices, int64_t 
  * nslice.  mode 0 (default): IIR, else FIR, else FFT; mode 1: FFT only;
  * mode 2: FFT where it runs, else IIR/FIR; mode 3: FIR, else FFT.
  * row_tile: rows-per-thread class of the IIR / FIR stages (16, the default:
- * 21 / 17 rows a thread; 32: 41 / 33; 0 keeps the current value), taken by
+ * 21 / 17 rows a thread; 32: 41 / 33; 64: 67 rows a thread for the IIR form,
+ * one CTA per SM, 33 for the FIR form; 0 keeps the current value), taken by
  * streams created after the call.  No reference counterpart: the reference
  * always filters with cuFFT (albatros_analysis/src/utils/pfb_gpu_utils.py:56-91). */
 int ab_ctx_set_time_filter(ab_ctx *ctx, int32_t mode, int32_t row_tile);

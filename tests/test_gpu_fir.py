@@ -55,17 +55,20 @@ def test_fir_chosen_and_matches_fft_and_oracle():
 
 @pytest.mark.parametrize("mode", [FIR, IIR])
 def test_row_tiles_agree(mode):
-    """Row tiles 33 and 17: the FIR sums are identical term by term (bitwise);
-    the IIR threads' ranges (41 or 21 rows) differ, so equal to rounding."""
+    """Row tiles 33 and 17 (FIR; tile class 64 runs 33 as well): the FIR sums
+    are identical term by term (bitwise); the IIR threads' ranges (67, 41 or
+    21 rows) differ, so equal to rounding."""
     raw = gen.raw_4bit(seed=22, nspec=3 * 1024, nchan=8, nant=1)
     ch = np.arange(100, 108)
     cfg = dict(CFG, osamp=64, nblock=16)
     a, _ = stream_vis(raw, ch, mode=mode, row_tile=32, **cfg)
     b, _ = stream_vis(raw, ch, mode=mode, row_tile=16, **cfg)
+    c, _ = stream_vis(raw, ch, mode=mode, row_tile=64, **cfg)
     if mode == FIR:
-        assert np.array_equal(a, b)
+        assert np.array_equal(a, b) and np.array_equal(a, c)
     else:
         assert np.linalg.norm(a - b) / np.linalg.norm(a) < 1e-6
+        assert np.linalg.norm(a - c) / np.linalg.norm(a) < 1e-6
 
 
 @pytest.mark.parametrize("mode", [FIR, IIR])
@@ -125,7 +128,7 @@ def test_time_stage_tuner(tmp_path, monkeypatch):
 
 
 @pytest.mark.parametrize("mode", [FIR, IIR])
-@pytest.mark.parametrize("osamp,row_tile", [(64, 16), (64, 32), (4, 16)])
+@pytest.mark.parametrize("osamp,row_tile", [(64, 16), (64, 32), (4, 16), (64, 64)])
 def test_multi_segment_columns(osamp, row_tile, mode):
     """acclen 8192 spans 2-3 segments per column (a segment holds
     row_tile*256 - 4*osamp new rows): blocks across segment edges and the
@@ -138,5 +141,22 @@ def test_multi_segment_columns(osamp, row_tile, mode):
     ref, _ = po.repfb_xcorr_avg(raw, ch, **kw)
     v, tf = stream_vis(raw, ch, mode=mode, row_tile=row_tile, **kw)
     assert tf[0] == ("fir" if mode == FIR else "iir")
+    check(v, ref)
+
+
+@pytest.mark.parametrize("osamp,cut,thresh", [(64, 10, 0.45), (4, 64, 0.45), (64, 80, 0.2)])
+def test_iir_large_tile_segments(osamp, cut, thresh):
+    """The 67-row IIR tile (one CTA per SM) holds 16384 new rows per segment:
+    acclen 2^15 spans two segments per column, so blocks across the segment
+    edge, the tail state between chunks and (threshold 0.2, 80-row carry)
+    the two-neighbour state exchange are all exercised against the oracle."""
+    acclen, nchunks = 32768, 2
+    raw = gen.raw_4bit(seed=osamp + cut, nspec=nchunks * acclen, nchan=2, nant=1)
+    ch = np.arange(1000, 1002)
+    kw = dict(acclen=acclen, nchunks=nchunks, nblock=acclen // osamp // 4, chanstart=0, chanend=2, osamp=osamp,
+              cut=cut)
+    ref, _ = po.repfb_xcorr_avg(raw, ch, filt_thresh=thresh, **kw)
+    v, tf = stream_vis(raw, ch, mode=IIR, row_tile=64, thresh=thresh, **kw)
+    assert tf == ("iir", 40 if thresh == 0.45 else 80)
     check(v, ref)
 

@@ -124,7 +124,7 @@ def schedule_error(U, D, n):
     return np.linalg.norm(y - ye) / np.linalg.norm(ye)
 
 
-@pytest.mark.parametrize("U,D", [(21, 2), (41, 1), (21, 4), (41, 2)])  # D*U >= 40: the tiles the library runs
+@pytest.mark.parametrize("U,D", [(21, 2), (41, 1), (21, 4), (41, 2), (67, 1), (67, 2)])  # D*U >= 40: the tiles the library runs
 @pytest.mark.parametrize("n", [0, 1, 1000, 2048, 2112, 4095])  # 2112: 1/A decays slowest (37 rows)
 def test_iir_schedule_matches_exact_filter(U, D, n):
     assert schedule_error(U, D, n) < 1e-6
