@@ -143,6 +143,7 @@ OPT_COARSE_ENGINE = 6
 OPT_COARSE_TC_SLICE = 7
 OPT_PFB_TMA = 9
 OPT_FAULT_TEST = 10
+OPT_COARSE_TC_TMA = 11
 DEFAULT_ROW_PREFETCH = 2
 
 
@@ -163,6 +164,12 @@ def set_coarse_tc_slice(samples: int, device: Optional[int] = None) -> None:
     """Time samples one CTA of the tcgen05 coarse correlator sums (0: chosen
     per call; else a multiple of 64 up to 131072)."""
     _lib.call("ab_ctx_set_option", _lib.ctx(device), OPT_COARSE_TC_SLICE, int(samples))
+
+
+def set_coarse_tc_tma(on: int, device: Optional[int] = None) -> None:
+    """tcgen05 coarse correlator: packet bytes staged by TMA into a ring in
+    shared memory (1, default) or loaded into registers (0); both exact."""
+    _lib.call("ab_ctx_set_option", _lib.ctx(device), OPT_COARSE_TC_TMA, int(on))
 
 
 def set_pfb_tma(on: int, device: Optional[int] = None) -> None:

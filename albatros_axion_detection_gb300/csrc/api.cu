@@ -478,6 +478,10 @@ int ab_ctx_set_option(ab_ctx* ctx, int32_t option, int32_t value) {
       AB_CHECK_ARG(value == 0 || value == 1, "ab_ctx_set_option: fault test must be 0 or 1");
       ctx->test_withhold_stage = value;
       return AB_OK;
+    case AB_OPT_COARSE_TC_TMA:
+      AB_CHECK_ARG(value == 0 || value == 1, "ab_ctx_set_option: coarse TMA staging must be 0 or 1");
+      ctx->coarse_tc_tma = value;
+      return AB_OK;
     case AB_OPT_COARSE_TC_SLICE:
       AB_CHECK_ARG(value >= 0 && value % 64 == 0 && value <= (1 << 17),
                    "ab_ctx_set_option: tensor-core slice must be 0 (auto) or a multiple of 64 up to 131072");

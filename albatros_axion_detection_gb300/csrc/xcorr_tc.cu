@@ -127,6 +127,34 @@ __device__ __forceinline__ uint32_t sw128_offset(int row, int c) {
   return (uint32_t)(row * 128 + (((c ^ row) & 7) << 4));
 }
 
+// Decode one (antenna, 8-sample group kc) item of a stage: w[i] holds the
+// packet words of the group's i-th sample (every selected channel's two pols,
+// nib_plus7 already applied); each byte b = 2 j + pol of channel j gives the
+// rows (.., re) from its high nibbles and (.., im) from its low ones, 8
+// samples = one 16-byte chunk of a 128-byte swizzled row.
+template <int CPT>
+__device__ __forceinline__ void tc_store_item(const uint32_t (&w)[8][CPT == 2 ? 4 : 2], int ant, int kc,
+                                              uint8_t* stage) {
+  constexpr int CPC = kTcTiles * CPT, BPT = 2 * CPC, ROWS = 128 / CPT;
+#pragma unroll
+  for (int b = 0; b < BPT; b++) {
+    const int j = b >> 1, pol = b & 1;
+    const int tile = j / CPT, h = j % CPT;
+    const int row_re = h * ROWS + 4 * ant + 2 * pol;
+    const uint32_t sel = (uint32_t)(b & 3) * 0x1111u + 0x4400u;  // byte b%4 of each word -> bytes 0|1 and 2|3
+    uint32_t re[4], im[4];
+#pragma unroll
+    for (int m = 0; m < 4; m++) {
+      const uint32_t p = __byte_perm(w[2 * m][b >> 2], w[2 * m + 1][b >> 2], sel);
+      im[m] = nib_to_h2(p);
+      re[m] = nib_to_h2(p >> 4);
+    }
+    uint8_t* tb = stage + tile * kTcTileBytes;
+    *reinterpret_cast<uint4*>(tb + sw128_offset(row_re, kc)) = make_uint4(re[0], re[1], re[2], re[3]);
+    *reinterpret_cast<uint4*>(tb + sw128_offset(row_re + 1, kc)) = make_uint4(im[0], im[1], im[2], im[3]);
+  }
+}
+
 template <int CPT>  // channels per 128-row tile: 2 (nant <= 16) or 1 (nant <= 32)
 __global__ void __launch_bounds__(kTcThreads, 1)
     coarse_xcorr_tc_kernel(const uint8_t* __restrict__ raw, int64_t ant_stride, int64_t row_bytes, int nant,
@@ -270,24 +298,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         for (int i = 0; i < 8; i++)
 #pragma unroll
           for (int q = 0; q < WPT; q++) w[it][i][q] = nib_plus7(w[it][i][q]);
-        // byte b = 2 j + pol of channel j: high nibble -> row (.., re), low -> (.., im)
-#pragma unroll
-        for (int b = 0; b < BPT; b++) {
-          const int j = b >> 1, pol = b & 1;
-          const int tile = j / CPT, h = j % CPT;
-          const int row_re = h * ROWS + 4 * ant + 2 * pol;
-          const uint32_t sel = (uint32_t)(b & 3) * 0x1111u + 0x4400u;  // byte b%4 of each word -> bytes 0|1 and 2|3
-          uint32_t re[4], im[4];
-#pragma unroll
-          for (int m = 0; m < 4; m++) {
-            const uint32_t p = __byte_perm(w[it][2 * m][b >> 2], w[it][2 * m + 1][b >> 2], sel);
-            im[m] = nib_to_h2(p);
-            re[m] = nib_to_h2(p >> 4);
-          }
-          uint8_t* tb = stage + tile * kTcTileBytes;
-          *reinterpret_cast<uint4*>(tb + sw128_offset(row_re, kc)) = make_uint4(re[0], re[1], re[2], re[3]);
-          *reinterpret_cast<uint4*>(tb + sw128_offset(row_re + 1, kc)) = make_uint4(im[0], im[1], im[2], im[3]);
-        }
+        tc_store_item<CPT>(w[it], ant, kc, stage);
       }
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       if (!(withhold && s == 0)) mbar_arrive(full_bar(slot));  // withhold: failure-path test, the MMA wait runs out
@@ -356,6 +367,235 @@ __global__ void __launch_bounds__(kTcThreads, 1)
   }
 }
 
+// TMA form (CPT = 2: up to 16 antennas, 8 channels a CTA; contiguous channel
+// groups on 16-byte boundaries, no row lists).  A stage's packet bytes, 16
+// bytes (8 channels x 2 pols) of 64 samples of each of 16 antennas, arrive as
+// one cp.async.bulk.tensor box in a 4-slot ring of 16 KB slots (antennas past
+// nant and rows past the array read as zero), issued by warp 9 up to four
+// stages ahead; the decoders then read them from shared memory instead of
+// issuing 16-byte global loads of rows 512 bytes apart, whose scattered
+// lines kept the L1 data pipe busy.  Thread (antenna, kc) takes the samples
+// kc + 8 i (i < 8): the 16-byte reads of a quarter-warp fall on 8
+// consecutive 16-byte slots (no bank conflicts), and its 8 samples fill the
+// chunk kc of the operand rows.  That permutes the stage's 64 samples in the
+// same way for every row, which leaves the Gram sums unchanged.  Two operand
+// stages (each decoder group always fills the same one), 128 KB, plus the
+// 64 KB ring.  Waits are bounded as in the form above; before exiting, warp
+// 9 waits (bounded) for every box it issued, so no copy lands after the CTA
+// ends.
+constexpr int kTmaRing = 4;                 // packet slots
+constexpr int kTmaSlotBytes = 16 * kTcKt * 16;  // 16 ant x 64 samples x 16 bytes
+constexpr int kTcOpStagesT = 2;
+constexpr int kTcThreadsT = kTcProducers + 64;  // + the MMA warp + the TMA warp
+constexpr size_t kTcSmemBytesT =
+    (size_t)kTcOpStagesT * kTcStageBytes + (size_t)kTmaRing * kTmaSlotBytes + 1024 /* alignment */ + 256 /* barriers */;
+
+__global__ void __launch_bounds__(kTcThreadsT, 1)
+    coarse_xcorr_tc_tma_kernel(const __grid_constant__ CUtensorMap tmap, const uint8_t* __restrict__ raw,
+                               int64_t ant_stride, int64_t row_bytes, int nant, int64_t rowstart, int64_t nrows,
+                               const int64_t* __restrict__ channels, int ncols, int64_t chunk_rows, int64_t slice,
+                               int64_t slices_per_chunk, int Rp, long long* __restrict__ G, int* __restrict__ fault,
+                               int withhold) {
+  constexpr int CPT = 2, CPC = kTcTiles * CPT, ROWS = 128 / CPT, WPT = 4;
+  extern __shared__ uint8_t smem_raw[];
+  const uint32_t raw_s = smem_u32(smem_raw);
+  const uint32_t pad = (1024u - (raw_s & 1023u)) & 1023u;
+  uint8_t* stages = smem_raw + pad;
+  const uint32_t stages_s = raw_s + pad;
+  uint8_t* ring = stages + kTcOpStagesT * kTcStageBytes;
+  const uint32_t ring_s = stages_s + kTcOpStagesT * kTcStageBytes;
+  const uint32_t bar_s = ring_s + kTmaRing * kTmaSlotBytes;
+  auto op_full = [&](int i) { return bar_s + 8u * (uint32_t)i; };
+  auto op_empty = [&](int i) { return bar_s + 8u * (uint32_t)(kTcOpStagesT + i); };
+  auto rg_full = [&](int i) { return bar_s + 8u * (uint32_t)(2 * kTcOpStagesT + i); };
+  auto rg_empty = [&](int i) { return bar_s + 8u * (uint32_t)(2 * kTcOpStagesT + kTmaRing + i); };
+  const uint32_t done_bar = bar_s + 8u * (2 * kTcOpStagesT + 2 * kTmaRing);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(ring + kTmaRing * kTmaSlotBytes + 8 * (2 * kTcOpStagesT + 2 * kTmaRing + 1));
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int c0 = blockIdx.x * CPC;
+  const int64_t chunk = blockIdx.y / slices_per_chunk;
+  const int64_t sl = blockIdx.y % slices_per_chunk;
+  const int64_t k_begin = chunk * chunk_rows + sl * slice;
+  const int64_t chunk_end = min((chunk + 1) * chunk_rows, nrows);
+  const int64_t k_end = min(k_begin + slice, chunk_end);
+  const int nst = k_end > k_begin ? (int)((k_end - k_begin + kTcKt - 1) / kTcKt) : 0;
+
+  __shared__ int skip;
+  if (tid == 0) skip = *reinterpret_cast<volatile int*>(fault);
+  __syncthreads();
+  if (skip) return;
+  // this CTA's channels: contiguous and 16-byte aligned -> TMA; else
+  // (a ragged last group, scattered channels) 16-byte or byte loads
+  bool tma = c0 + CPC <= ncols;
+  if (tma) {
+    const int64_t ch0 = channels[c0];
+    tma = (2 * ch0) % 16 == 0;
+#pragma unroll
+    for (int j = 1; j < CPC; j++) tma = tma && channels[c0 + j] == ch0 + j;
+  }
+
+  for (int i = tid; i < kTcOpStagesT * kTcStageBytes / 16; i += kTcThreadsT)
+    reinterpret_cast<uint4*>(stages)[i] = make_uint4(0u, 0u, 0u, 0u);
+  if (tid == 0) {
+    for (int i = 0; i < kTcOpStagesT; i++) {
+      mbar_init(op_full(i), kTcGroup);
+      mbar_init(op_empty(i), 1);
+    }
+    for (int i = 0; i < kTmaRing; i++) {
+      mbar_init(rg_full(i), 1);
+      mbar_init(rg_empty(i), kTcGroup);
+    }
+    mbar_init(done_bar, 1);
+    mbar_init_fence();
+  }
+  if (warp == kTcProducers / 32) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(kTcTiles * 128));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp < kTcProducers / 32) {
+    // ---------------- decoders: group g takes stages g, g + 2, ... ----------------
+    const int g = tid / kTcGroup, pt = tid % kTcGroup;
+    const int ant = pt >> 3, kc = pt & 7;  // one item a thread (16 antennas x 8 groups)
+    for (int s = g; s < nst; s += 2) {
+      const int oslot = s % kTcOpStagesT, ouse = s / kTcOpStagesT;
+      const int64_t kt = k_begin + (int64_t)s * kTcKt;
+      uint32_t w[8][WPT];
+      if (tma) {
+        const int r = s % kTmaRing;
+        if (!mbar_wait(rg_full(r), (uint32_t)((s / kTmaRing) & 1))) {
+          atomicExch(fault, 1);
+          break;
+        }
+        const uint8_t* slot = ring + r * kTmaSlotBytes + ant * (kTcKt * 16);
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+          const int smp = kc + 8 * i;
+          const uint4 v = *reinterpret_cast<const uint4*>(slot + smp * 16);
+          const bool in = kt + smp < k_end;  // rows of the box past the slice read as zero
+          w[i][0] = in ? v.x : 0u;
+          w[i][1] = in ? v.y : 0u;
+          w[i][2] = in ? v.z : 0u;
+          w[i][3] = in ? v.w : 0u;
+        }
+        mbar_arrive(rg_empty(r));
+      } else {
+#pragma unroll
+        for (int i = 0; i < 8; i++) {
+          const int64_t k = kt + 8 * kc + i;
+#pragma unroll
+          for (int q = 0; q < WPT; q++) w[i][q] = 0u;
+          if (ant < nant && k < k_end) {
+            const uint8_t* src = raw + (int64_t)ant * ant_stride + (rowstart + k) * row_bytes;
+#pragma unroll
+            for (int j = 0; j < CPC; j++) {
+              uint32_t b2 = 0u;
+              if (c0 + j < ncols) {
+                const uint8_t* p = src + 2 * channels[c0 + j];
+                b2 = (uint32_t)__ldg(p) | ((uint32_t)__ldg(p + 1) << 8);
+              }
+              w[i][j >> 1] |= b2 << (16 * (j & 1));
+            }
+          }
+        }
+      }
+      if (ouse > 0 && !mbar_wait(op_empty(oslot), (uint32_t)((ouse - 1) & 1))) {
+        atomicExch(fault, 1);
+        break;
+      }
+      if (ant < nant) {
+#pragma unroll
+        for (int i = 0; i < 8; i++)
+#pragma unroll
+          for (int q = 0; q < WPT; q++) w[i][q] = nib_plus7(w[i][q]);
+        tc_store_item<CPT>(w, ant, kc, stages + oslot * kTcStageBytes);
+      }
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      if (!(withhold && s == 0)) mbar_arrive(op_full(oslot));
+    }
+  } else if (warp == kTcProducers / 32) {
+    if (lane == 0) {
+      // ---------------- MMA issuer ----------------
+      for (int s = 0; s < nst; s++) {
+        const int slot = s % kTcOpStagesT, use = s / kTcOpStagesT;
+        if (!mbar_wait(op_full(slot), (uint32_t)(use & 1))) {
+          atomicExch(fault, 1);
+          break;
+        }
+        tc_fence_after();
+        const uint32_t st = stages_s + slot * kTcStageBytes;
+#pragma unroll
+        for (int t = 0; t < kTcTiles; t++) {
+#pragma unroll
+          for (int kk = 0; kk < kTcKt / 16; kk++) {
+            const uint64_t d = sw128_kmajor_desc(st + t * kTcTileBytes + kk * 32);
+            tc_mma(tmem + 128u * t, d, d, (s > 0 || kk > 0) ? 1u : 0u);
+          }
+        }
+        tc_commit(op_empty(slot));
+      }
+      tc_commit(done_bar);
+    }
+  } else if (lane == 0 && tma) {
+    // ---------------- TMA issuer ----------------
+    const int x = (int)(2 * channels[c0]);
+    int issued = 0;
+    for (int s = 0; s < nst; s++) {
+      const int r = s % kTmaRing, use = s / kTmaRing;
+      if (use > 0 && !mbar_wait(rg_empty(r), (uint32_t)((use - 1) & 1))) {
+        atomicExch(fault, 1);
+        break;
+      }
+      mbar_arrive_expect_tx(rg_full(r), (uint32_t)kTmaSlotBytes);
+      tma_load_3d(ring_s + r * kTmaSlotBytes, &tmap, x, (int)(rowstart + k_begin + (int64_t)s * kTcKt), 0, rg_full(r));
+      issued = s + 1;
+    }
+    // every box issued has landed before the CTA may end
+    for (int s = max(0, issued - kTmaRing); s < issued; s++)
+      if (!mbar_wait(rg_full(s % kTmaRing), (uint32_t)((s / kTmaRing) & 1))) atomicExch(fault, 1);
+  }
+
+  // ---------------- epilogue: warps 0-3 read lanes 32w .. 32w+31 ----------------
+  if (warp < 4) {
+    const bool done = nst > 0 && mbar_wait(done_bar, 0u);
+    if (nst > 0 && !done) atomicExch(fault, 1);
+    tc_fence_after();
+    if (done) {
+      const int row = 32 * warp + lane;
+      const int h = row / ROWS, rr = row % ROWS;
+      const int R = 4 * nant;
+#pragma unroll 1
+      for (int t = 0; t < kTcTiles; t++) {
+        const int ch = c0 + t * CPT + h;
+#pragma unroll 1
+        for (int cb = 0; cb < ROWS; cb += 32) {
+          float v[32];
+          tc_ld32(tmem + ((uint32_t)(32 * warp) << 16) + 128u * t + (uint32_t)(h * ROWS + cb), v);
+          if (ch < ncols && rr < R) {
+            long long* Gr = G + (((int64_t)chunk * ncols + ch) * Rp + rr) * Rp;
+#pragma unroll
+            for (int c = 0; c < 32; c++)
+              if (cb + c < R) atomicAdd((unsigned long long*)&Gr[cb + c], (unsigned long long)__float2ll_rn(v[c]));
+          }
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == kTcProducers / 32) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcTiles * 128));
+  }
+}
+
 // Launch the tensor-core form for 1 <= nant <= 32 into G (zeroed by the
 // caller, stride Rp >= 4*nant); *fault must be zero before the launch.
 int launch_coarse_tc(ab_ctx* ctx, const uint8_t* raw, int64_t ant_stride, int64_t nant, int64_t nchan,
@@ -384,6 +624,25 @@ int launch_coarse_tc(ab_ctx* ctx, const uint8_t* raw, int64_t ant_stride, int64_
     std::lock_guard<std::mutex> lk(ctx->mu);
     withhold = ctx->test_withhold_stage;
     ctx->test_withhold_stage = 0;  // one call only
+  }
+  // TMA staging: 16 antennas at most, no row lists, 16-byte aligned rows
+  const int64_t row_bytes = 2 * nchan;
+  if (cpt == 2 && ctx->coarse_tc_tma && !rows && (uintptr_t)raw % 16 == 0 && ant_stride % 16 == 0 &&
+      row_bytes % 16 == 0 && rowstart + nrows + kTcKt < (1LL << 31) && kTcSmemBytesT <= ctx->smem_optin) {
+    CUtensorMap tmap;
+    const uint64_t dims[3] = {(uint64_t)row_bytes, (uint64_t)(rowstart + nrows), (uint64_t)nant};
+    const uint64_t strides[2] = {(uint64_t)row_bytes, (uint64_t)ant_stride};
+    const uint32_t box[3] = {16, (uint32_t)kTcKt, 16};
+    if (encode_tmap(&tmap, CU_TENSOR_MAP_DATA_TYPE_UINT8, 3, raw, dims, strides, box) == AB_OK) {
+      AB_CUDA(cudaFuncSetAttribute(coarse_xcorr_tc_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)kTcSmemBytesT));
+      coarse_xcorr_tc_tma_kernel<<<grid, kTcThreadsT, kTcSmemBytesT, s>>>(
+          tmap, raw, ant_stride, row_bytes, (int)nant, rowstart, nrows, channels, (int)ncols, chunk_rows, slice, spc,
+          Rp, G, fault, withhold);
+      AB_LAUNCH_CHECK();
+      return AB_OK;
+    }
+    set_error("");  // the map was refused: the register-load form below
   }
   if (cpt == 2) {
     AB_CUDA(cudaFuncSetAttribute(coarse_xcorr_tc_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,

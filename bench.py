@@ -570,6 +570,9 @@ def run_coarse(args, nant, nchan, nspec, chunk, workload):
     if args.mma_bits:
         from albatros_axion_detection_gb300 import autotune
         autotune.set_coarse_mma_bits(args.mma_bits)
+    if args.coarse_tma >= 0:
+        from albatros_axion_detection_gb300 import autotune
+        autotune.set_coarse_tc_tma(args.coarse_tma)
     fn = lambda: correlations.xcorr_coarse_4bit(raw, 0, nspec, channels, nchan, chunk=chunk, average=False)
     ms, clk = _timed(torch, fn, args.steps, args.warmup, local)
     host = torch.empty(raw.shape, dtype=torch.uint8, pin_memory=True)
@@ -595,7 +598,9 @@ def run_coarse(args, nant, nchan, nspec, chunk, workload):
                    "h2d_bytes_per_step": int(bytes_in), "d2h_bytes_per_step": int(out_re.numel() * 16)},
            "roofline": {"bound": "hbm",
                         "kernel": ("coarse_xcorr_kernel (int8 mma.sync)" if args.mma_bits == 8 else
-                                   "coarse_xcorr_tc_kernel (tcgen05)" if 9 <= nant <= 32 else
+                                   ("coarse_xcorr_tc_tma_kernel (tcgen05, TMA-staged packets)"
+                                    if nant <= 16 and args.coarse_tma != 0 and (2 * nchan) % 16 == 0 else
+                                    "coarse_xcorr_tc_kernel (tcgen05)") if 9 <= nant <= 32 else
                                    "coarse_xcorr_f16_kernel (fp16 mma.sync)"),
                         "achieved": achieved, "peak": peak,
                         "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
@@ -710,6 +715,8 @@ def main():
                     help="stream: row stage 0 = one CTA per tile, 1 = persistent prefetching, "
                          "2 (default) = + shared twiddles")
     ap.add_argument("--check", action="store_true", help="uneven-batch: job-0 error of every file vs the FP64 oracle")
+    ap.add_argument("--coarse-tma", type=int, default=-1,
+                    help="coarse workloads: tcgen05 packet staging, 1 TMA (library default), 0 register loads")
     ap.add_argument("--mma-bits", type=int, default=0, help="coarse workloads: tensor-core operand bits (16 or 8)")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -108,6 +108,12 @@ int ab_ctx_set_time_filter(ab_ctx *ctx, int32_t mode, int32_t row_tile);
  * call's outputs are all INT64_MIN, and the tensor memory is freed.  The
  * setting applies to one call. */
 #define AB_OPT_FAULT_TEST 10
+/* AB_OPT_COARSE_TC_TMA: how the tcgen05 coarse correlator (up to 16
+ * antennas, contiguous 16-byte-aligned channel groups, no row lists) fetches
+ * its packet bytes: 1 (default) TMA tensor copies (cp.async.bulk.tensor, a
+ * box of 16 bytes x 64 samples x 16 antennas per stage) into a 4-slot ring
+ * in shared memory; 0 plain 16-byte loads into registers.  Both are exact. */
+#define AB_OPT_COARSE_TC_TMA 11
 int ab_ctx_set_option(ab_ctx *ctx, int32_t option, int32_t value);
 
 /* ---- unpacking ----------------------------------------------------------

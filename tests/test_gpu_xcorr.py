@@ -127,6 +127,7 @@ def tc_engine():
     yield
     autotune.set_coarse_engine(0)
     autotune.set_coarse_tc_slice(0)
+    autotune.set_coarse_tc_tma(1)
 
 
 @pytest.mark.parametrize("nant,nspec,nchan,chunk,ch", [
@@ -148,6 +149,36 @@ def test_coarse_xcorr_tcgen05_bit_exact(tc_engine, nant, nspec, nchan, chunk, ch
         er, ei = io.xcorr_all_ant_4bit(raw, r0, r1, chans, nchan, nthreads=8)
         np.testing.assert_array_equal(re[k], er)
         np.testing.assert_array_equal(im[k], ei)
+
+
+@pytest.mark.parametrize("nant,nspec,nchan,rowstart,chunk,chans", [
+    (16, 5000, 64, 0, 1000, "all"),       # chunks of 15 stages + 40 samples: boxes cross chunk and slice ends
+    (7, 3001, 40, 17, None, "from8"),     # 7 antennas (box rows 7-15 read as zero), rows from 17, channels
+                                          # 8..34: three TMA groups and a ragged one on 16-byte loads
+    (16, 2 ** 16, 256, 64, 2 ** 14, "all"),  # full boxes, 4 chunks
+    (4, 2000, 32, 0, None, "step2"),      # scattered channels: no group takes TMA inside the TMA kernel
+])
+def test_coarse_xcorr_tcgen05_tma_exact(tc_engine, nant, nspec, nchan, rowstart, chunk, chans):
+    """The TMA-staged form (packet bytes in a ring of 16 B x 64 samples x 16
+    antennas boxes, samples taken in a permuted order) is bit-exact against
+    the int64 oracle and equal to the register-load form."""
+    from albatros_axion_detection_gb300 import autotune
+    from albatros_axion_detection_gb300.correlations import xcorr_coarse_4bit
+    raw = gen.raw_4bit_uniform(seed=nant * 31 + nspec, nspec=rowstart + nspec, nchan=nchan, nant=nant)
+    ch = {"all": np.arange(nchan), "from8": np.arange(8, 35), "step2": np.arange(0, nchan, 2)}[chans]
+    got = {}
+    for tma in (1, 0):
+        autotune.set_coarse_tc_tma(tma)
+        re, im = xcorr_coarse_4bit(cu(raw), rowstart, rowstart + nspec, ch, nchan, chunk=chunk, average=False)
+        got[tma] = (re.cpu().numpy(), im.cpu().numpy())
+    np.testing.assert_array_equal(got[1][0], got[0][0])
+    np.testing.assert_array_equal(got[1][1], got[0][1])
+    c = nspec if chunk is None else chunk
+    for k in range(got[1][0].shape[0]):
+        r0, r1 = rowstart + k * c, rowstart + min((k + 1) * c, nspec)
+        er, ei = io.xcorr_all_ant_4bit(raw, r0, r1, ch, nchan, nthreads=8)
+        np.testing.assert_array_equal(got[1][0][k], er)
+        np.testing.assert_array_equal(got[1][1][k], ei)
 
 
 def test_coarse_xcorr_tcgen05_longest_slice_exact(tc_engine):
