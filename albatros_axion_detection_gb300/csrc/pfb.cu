@@ -615,6 +615,9 @@ __global__ void __launch_bounds__(kBtThreads, 1)
       bufB[pidx(n)] = cmul(cmul(make_float2(v.z, v.w), bB), qtw[16 + q]);
       wv[qq] = v.y;
     }
+    // the next tile's boxes are written by the asynchronous proxy: every
+    // thread orders its generic reads of the landing tile before them
+    fence_proxy_async();
     __syncthreads();  // the landing tile is consumed: fetch the next tile into it
     if (tid == 0 && t + gridDim.x < ntile) issue(t + gridDim.x);
     float2* buf = half ? bufB : bufA;

@@ -370,47 +370,114 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 // TMA form (CPT = 2: up to 16 antennas, 8 channels a CTA; contiguous channel
 // groups on 16-byte boundaries, no row lists).  A stage's packet bytes, 16
 // bytes (8 channels x 2 pols) of 64 samples of each of 16 antennas, arrive as
-// one cp.async.bulk.tensor box in a 4-slot ring of 16 KB slots (antennas past
-// nant and rows past the array read as zero), issued by warp 9 up to four
-// stages ahead; the decoders then read them from shared memory instead of
-// issuing 16-byte global loads of rows 512 bytes apart, whose scattered
-// lines kept the L1 data pipe busy.  Thread (antenna, kc) takes the samples
-// kc + 8 i (i < 8): the 16-byte reads of a quarter-warp fall on 8
-// consecutive 16-byte slots (no bank conflicts), and its 8 samples fill the
-// chunk kc of the operand rows.  That permutes the stage's 64 samples in the
-// same way for every row, which leaves the Gram sums unchanged.  Two operand
-// stages (each decoder group always fills the same one), 128 KB, plus the
-// 64 KB ring.  Waits are bounded as in the form above; before exiting, warp
-// 9 waits (bounded) for every box it issued, so no copy lands after the CTA
-// ends.
-constexpr int kTmaRing = 4;                 // packet slots
+// one cp.async.bulk.tensor box in a ring of 16 KB slots (antennas past nant
+// and rows past the array read as zero), issued by warp 17 ahead of the
+// decoders; the decoders read them from shared memory instead of issuing
+// 16-byte global loads of rows 512 bytes apart, whose scattered lines kept
+// the L1 data pipe busy.  A decoder orders its reads of a slot before the
+// slot's next box with fence.proxy.async before it releases the slot: the
+// box is written by the asynchronous proxy, and without the fence a box
+// could land before the reads were done (measured: wrong sums in up to 40 %
+// of the outputs).
+//
+// Decoders: 16 warps in two groups of 8 taking alternate stages.  Thread
+// (antenna, half, kc) takes half of the sample record (4 channels x 2 pols,
+// 8 bytes) of the samples kc + 8 i (i < 8): the 8-byte reads of a half-warp
+// cover 128 consecutive bytes and the 16-byte stores of a quarter-warp one
+// 128-byte row (no bank conflicts), and the 8 samples fill the chunk kc of
+// the operand rows.  That permutes the stage's 64 samples in the same way
+// for every row, which leaves the Gram sums unchanged.
+//
+// Levels are stored as 16 x (n - 7) (n = (v + 7) mod 16 of the raw nibble
+// v): a low nibble n in the mantissa of 0x7400 is the fp16 value 16384 +
+// 16 n, a high nibble in place (n << 4) under 0x6400 is 1024 + 16 n, so one
+// subtraction each gives 16 (n - 7) with no shift.  Every product is then a
+// multiple of 256 and every partial sum a multiple of 256 below 2^31 (64 x
+// 256 x kTcMaxSlice), exact in fp32; the epilogue divides by 256 (exact).
+//
+// Waits are bounded as in the form above; before exiting, warp 17 waits
+// (bounded) for every box it issued, so no copy lands after the CTA ends.
 constexpr int kTmaSlotBytes = 16 * kTcKt * 16;  // 16 ant x 64 samples x 16 bytes
-constexpr int kTcOpStagesT = 2;
-constexpr int kTcThreadsT = kTcProducers + 64;  // + the MMA warp + the TMA warp
-constexpr size_t kTcSmemBytesT =
-    (size_t)kTcOpStagesT * kTcStageBytes + (size_t)kTmaRing * kTmaSlotBytes + 1024 /* alignment */ + 256 /* barriers */;
+constexpr int kTcProducersT = 512;                 // warps 0-15
+constexpr int kTcGroupT = kTcProducersT / 2;       // decoder threads per stage
+constexpr int kTcThreadsT = kTcProducersT + 64;    // + the MMA warp (16) + the TMA warp (17)
+// NOP operand stages, NRG packet slots
+__host__ __device__ constexpr size_t tc_tma_smem(int nop, int nrg) {
+  return (size_t)nop * kTcStageBytes + (size_t)nrg * kTmaSlotBytes + 1024 /* alignment */ + 256 /* barriers */;
+}
+// Two operand stages and four packet slots (measured on 16 antennas x 256
+// channels x 2^18 spectra: 0.89 ms; three operand stages with two slots, the
+// most that fit: 0.90 ms)
+constexpr int kTcOpStagesTma = 2, kTcRingTma = 4;
+constexpr size_t kTcSmemBytesTma = tc_tma_smem(kTcOpStagesTma, kTcRingTma);
 
+// fp16 pairs 16 (n - 7) from the low nibbles (lo) and high nibbles (hi) of
+// bytes 0 and 2 of p.
+__device__ __forceinline__ uint32_t nib_lo_h2x16(uint32_t p) {
+  uint32_t r;
+  asm("sub.rn.f16x2 %0, %1, %2;" : "=r"(r) : "r"((p & 0x000F000Fu) | 0x74007400u), "r"(0x74077407u));
+  return r;
+}
+__device__ __forceinline__ uint32_t nib_hi_h2x16(uint32_t p) {
+  uint32_t r;
+  asm("sub.rn.f16x2 %0, %1, %2;" : "=r"(r) : "r"((p & 0x00F000F0u) | 0x64006400u), "r"(0x64706470u));
+  return r;
+}
+
+// Half an item: bytes 8 half + b (b < 8) of the 8 samples in w[i] (2 words
+// each, nib_plus7 applied) into the operand rows, 16 x the levels.
+__device__ __forceinline__ void tc_store_half(const uint32_t (&w)[8][2], int ant, int kc, int half, uint8_t* stage) {
+  constexpr int ROWS = 64;  // CPT = 2
+#pragma unroll
+  for (int b = 0; b < 8; b++) {
+    const int j = 4 * half + (b >> 1), pol = b & 1;  // channel j of the CTA's 8
+    const int tile = j >> 1, h = j & 1;
+    const int row_re = h * ROWS + 4 * ant + 2 * pol;
+    const uint32_t sel = (uint32_t)(b & 3) * 0x1111u + 0x4400u;
+    uint32_t re[4], im[4];
+#pragma unroll
+    for (int m = 0; m < 4; m++) {
+      const uint32_t p = __byte_perm(w[2 * m][b >> 2], w[2 * m + 1][b >> 2], sel);
+      im[m] = nib_lo_h2x16(p);
+      re[m] = nib_hi_h2x16(p);
+    }
+    uint8_t* tb = stage + tile * kTcTileBytes;
+    *reinterpret_cast<uint4*>(tb + sw128_offset(row_re, kc)) = make_uint4(re[0], re[1], re[2], re[3]);
+    *reinterpret_cast<uint4*>(tb + sw128_offset(row_re + 1, kc)) = make_uint4(im[0], im[1], im[2], im[3]);
+  }
+}
+
+template <int kTcOpStagesT, int kTmaRing>
 __global__ void __launch_bounds__(kTcThreadsT, 1)
     coarse_xcorr_tc_tma_kernel(const __grid_constant__ CUtensorMap tmap, const uint8_t* __restrict__ raw,
                                int64_t ant_stride, int64_t row_bytes, int nant, int64_t rowstart, int64_t nrows,
                                const int64_t* __restrict__ channels, int ncols, int64_t chunk_rows, int64_t slice,
                                int64_t slices_per_chunk, int Rp, long long* __restrict__ G, int* __restrict__ fault,
                                int withhold) {
-  constexpr int CPT = 2, CPC = kTcTiles * CPT, ROWS = 128 / CPT, WPT = 4;
+  constexpr int CPT = 2, CPC = kTcTiles * CPT, ROWS = 128 / CPT;
+  constexpr int MMA_WARP = kTcProducersT / 32, TMA_WARP = MMA_WARP + 1;
+  // Layout: barriers and the tensor-memory address (256 bytes), then from
+  // the next 1024-byte boundary the packet ring, then the operand stages
+  // (1024-byte aligned for the swizzle atoms).
   extern __shared__ uint8_t smem_raw[];
   const uint32_t raw_s = smem_u32(smem_raw);
-  const uint32_t pad = (1024u - (raw_s & 1023u)) & 1023u;
-  uint8_t* stages = smem_raw + pad;
-  const uint32_t stages_s = raw_s + pad;
-  uint8_t* ring = stages + kTcOpStagesT * kTcStageBytes;
-  const uint32_t ring_s = stages_s + kTcOpStagesT * kTcStageBytes;
-  const uint32_t bar_s = ring_s + kTmaRing * kTmaSlotBytes;
-  auto op_full = [&](int i) { return bar_s + 8u * (uint32_t)i; };
-  auto op_empty = [&](int i) { return bar_s + 8u * (uint32_t)(kTcOpStagesT + i); };
-  auto rg_full = [&](int i) { return bar_s + 8u * (uint32_t)(2 * kTcOpStagesT + i); };
-  auto rg_empty = [&](int i) { return bar_s + 8u * (uint32_t)(2 * kTcOpStagesT + kTmaRing + i); };
-  const uint32_t done_bar = bar_s + 8u * (2 * kTcOpStagesT + 2 * kTmaRing);
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(ring + kTmaRing * kTmaSlotBytes + 8 * (2 * kTcOpStagesT + 2 * kTmaRing + 1));
+  const uint32_t bar_s = raw_s;
+  const uint32_t pad = (1024u - ((raw_s + 256u) & 1023u)) & 1023u;
+  uint8_t* ring = smem_raw + 256 + pad;
+  const uint32_t ring_s = raw_s + 256u + pad;
+  uint8_t* stages = ring + kTmaRing * kTmaSlotBytes;
+  const uint32_t stages_s = ring_s + kTmaRing * kTmaSlotBytes;
+  // Operand barriers per virtual slot v = s mod NV (NV = lcm(2, stages)):
+  // each is waited on, phase after phase, by one decoder group or by the MMA
+  // thread alone, so no parity wait can pass a phase early.
+  constexpr int NV = kTcOpStagesT % 2 ? 2 * kTcOpStagesT : kTcOpStagesT;
+  auto op_full = [&](int v) { return bar_s + 8u * (uint32_t)v; };
+  auto op_empty = [&](int v) { return bar_s + 8u * (uint32_t)(NV + v); };
+  auto rg_full = [&](int i) { return bar_s + 8u * (uint32_t)(2 * NV + i); };
+  auto rg_empty = [&](int i) { return bar_s + 8u * (uint32_t)(2 * NV + kTmaRing + i); };
+  const uint32_t done_bar = bar_s + 8u * (2 * NV + 2 * kTmaRing);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem_raw + 8 * (2 * NV + 2 * kTmaRing + 1));
+  static_assert(8 * (2 * NV + 2 * kTmaRing + 1) + 4 <= 256, "barrier space");
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int c0 = blockIdx.x * CPC;
@@ -426,7 +493,7 @@ __global__ void __launch_bounds__(kTcThreadsT, 1)
   __syncthreads();
   if (skip) return;
   // this CTA's channels: contiguous and 16-byte aligned -> TMA; else
-  // (a ragged last group, scattered channels) 16-byte or byte loads
+  // (a ragged last group, scattered channels) byte loads
   bool tma = c0 + CPC <= ncols;
   if (tma) {
     const int64_t ch0 = channels[c0];
@@ -438,18 +505,18 @@ __global__ void __launch_bounds__(kTcThreadsT, 1)
   for (int i = tid; i < kTcOpStagesT * kTcStageBytes / 16; i += kTcThreadsT)
     reinterpret_cast<uint4*>(stages)[i] = make_uint4(0u, 0u, 0u, 0u);
   if (tid == 0) {
-    for (int i = 0; i < kTcOpStagesT; i++) {
-      mbar_init(op_full(i), kTcGroup);
-      mbar_init(op_empty(i), 1);
+    for (int v = 0; v < NV; v++) {
+      mbar_init(op_full(v), kTcGroupT);
+      mbar_init(op_empty(v), 1);
     }
     for (int i = 0; i < kTmaRing; i++) {
       mbar_init(rg_full(i), 1);
-      mbar_init(rg_empty(i), kTcGroup);
+      mbar_init(rg_empty(i), kTcGroupT);
     }
     mbar_init(done_bar, 1);
     mbar_init_fence();
   }
-  if (warp == kTcProducers / 32) {
+  if (warp == MMA_WARP) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
                  "r"(kTcTiles * 128));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
@@ -460,72 +527,78 @@ __global__ void __launch_bounds__(kTcThreadsT, 1)
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
 
-  if (warp < kTcProducers / 32) {
+  if (warp < MMA_WARP) {
     // ---------------- decoders: group g takes stages g, g + 2, ... ----------------
-    const int g = tid / kTcGroup, pt = tid % kTcGroup;
-    const int ant = pt >> 3, kc = pt & 7;  // one item a thread (16 antennas x 8 groups)
+    const int g = tid / kTcGroupT, pt = tid % kTcGroupT;
+    // kc fastest: a quarter-warp's 16-byte stores fill one 128-byte row
+    const int ant = pt >> 4, half = (pt >> 3) & 1, kc = pt & 7;
     for (int s = g; s < nst; s += 2) {
-      const int oslot = s % kTcOpStagesT, ouse = s / kTcOpStagesT;
+      const int oslot = s % kTcOpStagesT;
       const int64_t kt = k_begin + (int64_t)s * kTcKt;
-      uint32_t w[8][WPT];
+      uint32_t w[8][2];
       if (tma) {
         const int r = s % kTmaRing;
         if (!mbar_wait(rg_full(r), (uint32_t)((s / kTmaRing) & 1))) {
           atomicExch(fault, 1);
           break;
         }
-        const uint8_t* slot = ring + r * kTmaSlotBytes + ant * (kTcKt * 16);
+        const uint8_t* slot = ring + r * kTmaSlotBytes + ant * (kTcKt * 16) + 8 * half;
 #pragma unroll
         for (int i = 0; i < 8; i++) {
           const int smp = kc + 8 * i;
-          const uint4 v = *reinterpret_cast<const uint4*>(slot + smp * 16);
+          const uint2 v = *reinterpret_cast<const uint2*>(slot + smp * 16);
           const bool in = kt + smp < k_end;  // rows of the box past the slice read as zero
           w[i][0] = in ? v.x : 0u;
           w[i][1] = in ? v.y : 0u;
-          w[i][2] = in ? v.z : 0u;
-          w[i][3] = in ? v.w : 0u;
         }
+        // the slot's next box is written by the asynchronous proxy: order
+        // these generic reads before it, then release the slot
+        fence_proxy_async();
         mbar_arrive(rg_empty(r));
       } else {
 #pragma unroll
         for (int i = 0; i < 8; i++) {
-          const int64_t k = kt + 8 * kc + i;
-#pragma unroll
-          for (int q = 0; q < WPT; q++) w[i][q] = 0u;
+          const int64_t k = kt + kc + 8 * i;
+          w[i][0] = 0u;
+          w[i][1] = 0u;
           if (ant < nant && k < k_end) {
             const uint8_t* src = raw + (int64_t)ant * ant_stride + (rowstart + k) * row_bytes;
 #pragma unroll
-            for (int j = 0; j < CPC; j++) {
+            for (int jj = 0; jj < 4; jj++) {
+              const int j = 4 * half + jj;
               uint32_t b2 = 0u;
               if (c0 + j < ncols) {
                 const uint8_t* p = src + 2 * channels[c0 + j];
                 b2 = (uint32_t)__ldg(p) | ((uint32_t)__ldg(p + 1) << 8);
               }
-              w[i][j >> 1] |= b2 << (16 * (j & 1));
+              w[i][jj >> 1] |= b2 << (16 * (jj & 1));
             }
           }
         }
       }
-      if (ouse > 0 && !mbar_wait(op_empty(oslot), (uint32_t)((ouse - 1) & 1))) {
+      // the slot's previous stage, s - kTcOpStagesT, has left the tensor cores
+      const int sp = s - kTcOpStagesT;
+      if (sp >= 0 && !mbar_wait(op_empty(sp % NV), (uint32_t)((sp / NV) & 1))) {
         atomicExch(fault, 1);
         break;
       }
       if (ant < nant) {
 #pragma unroll
-        for (int i = 0; i < 8; i++)
-#pragma unroll
-          for (int q = 0; q < WPT; q++) w[i][q] = nib_plus7(w[i][q]);
-        tc_store_item<CPT>(w, ant, kc, stages + oslot * kTcStageBytes);
+        for (int i = 0; i < 8; i++) {
+          w[i][0] = nib_plus7(w[i][0]);
+          w[i][1] = nib_plus7(w[i][1]);
+        }
+        tc_store_half(w, ant, kc, half, stages + oslot * kTcStageBytes);
       }
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      if (!(withhold && s == 0)) mbar_arrive(op_full(oslot));
+      if (!(withhold && s == 0)) mbar_arrive(op_full(s % NV));
     }
-  } else if (warp == kTcProducers / 32) {
+  } else if (warp == MMA_WARP) {
     if (lane == 0) {
       // ---------------- MMA issuer ----------------
       for (int s = 0; s < nst; s++) {
-        const int slot = s % kTcOpStagesT, use = s / kTcOpStagesT;
-        if (!mbar_wait(op_full(slot), (uint32_t)(use & 1))) {
+        const int slot = s % kTcOpStagesT;
+        if (!mbar_wait(op_full(s % NV), (uint32_t)((s / NV) & 1))) {
           atomicExch(fault, 1);
           break;
         }
@@ -539,11 +612,11 @@ __global__ void __launch_bounds__(kTcThreadsT, 1)
             tc_mma(tmem + 128u * t, d, d, (s > 0 || kk > 0) ? 1u : 0u);
           }
         }
-        tc_commit(op_empty(slot));
+        tc_commit(op_empty(s % NV));
       }
       tc_commit(done_bar);
     }
-  } else if (lane == 0 && tma) {
+  } else if (warp == TMA_WARP && lane == 0 && tma) {
     // ---------------- TMA issuer ----------------
     const int x = (int)(2 * channels[c0]);
     int issued = 0;
@@ -581,8 +654,9 @@ __global__ void __launch_bounds__(kTcThreadsT, 1)
           if (ch < ncols && rr < R) {
             long long* Gr = G + (((int64_t)chunk * ncols + ch) * Rp + rr) * Rp;
 #pragma unroll
-            for (int c = 0; c < 32; c++)
-              if (cb + c < R) atomicAdd((unsigned long long*)&Gr[cb + c], (unsigned long long)__float2ll_rn(v[c]));
+            for (int c = 0; c < 32; c++)  // sums of 256 x the level products (exact)
+              if (cb + c < R)
+                atomicAdd((unsigned long long*)&Gr[cb + c], (unsigned long long)__float2ll_rn(v[c] * (1.0f / 256.0f)));
           }
         }
       }
@@ -590,7 +664,7 @@ __global__ void __launch_bounds__(kTcThreadsT, 1)
   }
   tc_fence_before();
   __syncthreads();
-  if (warp == kTcProducers / 32) {
+  if (warp == MMA_WARP) {
     tc_fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTcTiles * 128));
   }
@@ -628,15 +702,15 @@ int launch_coarse_tc(ab_ctx* ctx, const uint8_t* raw, int64_t ant_stride, int64_
   // TMA staging: 16 antennas at most, no row lists, 16-byte aligned rows
   const int64_t row_bytes = 2 * nchan;
   if (cpt == 2 && ctx->coarse_tc_tma && !rows && (uintptr_t)raw % 16 == 0 && ant_stride % 16 == 0 &&
-      row_bytes % 16 == 0 && rowstart + nrows + kTcKt < (1LL << 31) && kTcSmemBytesT <= ctx->smem_optin) {
+      row_bytes % 16 == 0 && rowstart + nrows + kTcKt < (1LL << 31) && kTcSmemBytesTma <= ctx->smem_optin) {
     CUtensorMap tmap;
     const uint64_t dims[3] = {(uint64_t)row_bytes, (uint64_t)(rowstart + nrows), (uint64_t)nant};
     const uint64_t strides[2] = {(uint64_t)row_bytes, (uint64_t)ant_stride};
     const uint32_t box[3] = {16, (uint32_t)kTcKt, 16};
     if (encode_tmap(&tmap, CU_TENSOR_MAP_DATA_TYPE_UINT8, 3, raw, dims, strides, box) == AB_OK) {
-      AB_CUDA(cudaFuncSetAttribute(coarse_xcorr_tc_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)kTcSmemBytesT));
-      coarse_xcorr_tc_tma_kernel<<<grid, kTcThreadsT, kTcSmemBytesT, s>>>(
+      AB_CUDA(cudaFuncSetAttribute(coarse_xcorr_tc_tma_kernel<kTcOpStagesTma, kTcRingTma>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTcSmemBytesTma));
+      coarse_xcorr_tc_tma_kernel<kTcOpStagesTma, kTcRingTma><<<grid, kTcThreadsT, kTcSmemBytesTma, s>>>(
           tmap, raw, ant_stride, row_bytes, (int)nant, rowstart, nrows, channels, (int)ncols, chunk_rows, slice, spc,
           Rp, G, fault, withhold);
       AB_LAUNCH_CHECK();

@@ -140,3 +140,138 @@ def test_slices_cover_each_chunk_once():
                 if hi > lo:
                     cover[lo - c * chunk:hi - c * chunk] += 1
             assert np.all(cover == 1)
+
+
+# ---------------------------------------------------------------------------
+# The TMA form (coarse_xcorr_tc_tma_kernel): scaled decode and barrier protocol.
+
+def scaled_pair(p, hi):
+    """16 (n - 7) for the nibbles of bytes 0 and 2 of p: low nibbles under
+    0x7400 (16384 + 16 n), high nibbles in place under 0x6400 (1024 + 16 n)."""
+    if hi:
+        x, c = (int(p) & 0x00F000F0) | 0x64006400, 0x6470
+    else:
+        x, c = (int(p) & 0x000F000F) | 0x74007400, 0x7407
+    cf = np.frombuffer(np.uint16(c).tobytes(), np.float16)[0]
+    out = []
+    for half in (x & 0xFFFF, x >> 16):
+        v = np.frombuffer(np.uint16(half).tobytes(), np.float16)[0]
+        out.append(float(np.float16(v - cf)))
+    return out
+
+
+def test_scaled_decode_is_16_times_the_level():
+    """Every byte value: both scaled fp16 conversions give exactly 16 x the
+    oracle's level (0x8 -> +8), and the largest product sums of a CTA slice
+    (2^17 samples of 128 x 128) stay multiples of 256 below 2^32 (exact in
+    fp32, whose 24-bit significand then spans 2^8 .. 2^32)."""
+    lv_re, lv_im = po.decode_4bit(np.arange(256, dtype=np.uint8))
+    for v in range(256):
+        w = nib_plus7(v | (v << 16))
+        assert scaled_pair(w, True) == [16.0 * float(lv_re[v])] * 2
+        assert scaled_pair(w, False) == [16.0 * float(lv_im[v])] * 2
+    assert (1 << 17) * 128 * 128 <= 2 ** 31 < 2 ** 32
+
+
+class _Bar:
+    """mbarrier: arrival count, phase counter, parity wait."""
+
+    def __init__(self, count):
+        self.count, self.pending, self.phase = count, count, 0
+
+    def arrive(self):
+        self.pending -= 1
+        if self.pending == 0:
+            self.phase, self.pending = self.phase + 1, self.count
+
+    def passed(self, parity):  # the phase with this parity has completed
+        return (self.phase & 1) != parity
+
+
+def _run_protocol(nop, nrg, nst, seed, per_slot=False, fence=True):
+    """One CTA of the TMA form under a random interleaving: two decoder groups
+    (stages g, g + 2, ...), the MMA thread, the TMA thread; MMAs complete in
+    order, their completion arrivals reach the barriers after independent
+    random delays, and a box may land before its slot's reads unless the
+    readers fence.  Returns the first violation, or None."""
+    rnd = np.random.default_rng(seed)
+    nv = nop if (nop % 2 == 0 or per_slot) else 2 * nop
+    G = 3  # threads a group (model)
+    full, empty = [_Bar(G) for _ in range(nv)], [_Bar(1) for _ in range(nv)]
+    rfull, rempty = [_Bar(1) for _ in range(nrg)], [_Bar(G) for _ in range(nrg)]
+    held = [None] * nop          # stage whose operands a physical slot holds
+    ring = [None] * nrg          # stage whose box a packet slot holds
+    unread = {}                  # packet slot -> readers that released it without a fence
+    done, arrivals, queue = set(), [], []
+    dec = {(g, t): [g, 0] for g in range(2) for t in range(G)}
+    mma_s = tma_s = 0
+    for _ in range(100000):
+        acts = [("dec", k) for k, (s, _) in dec.items() if s < nst]
+        acts += [("mma",)] * (mma_s < nst) + [("tma",)] * (tma_s < nst)
+        acts += [("complete",)] * bool(queue) + [("deliver",)] * bool(arrivals)
+        if not acts:
+            return None
+        a = acts[rnd.integers(len(acts))]
+        if a[0] == "deliver":
+            arrivals.pop(rnd.integers(len(arrivals))).arrive()
+        elif a[0] == "complete":
+            s = queue.pop(0)
+            done.add(s)
+            arrivals.append(empty[s % nv])
+        elif a[0] == "tma":
+            s, r = tma_s, tma_s % nrg
+            if s >= nrg and not rempty[r].passed(((s // nrg) - 1) & 1):
+                continue
+            if unread.get(r):
+                return "box landed before a read"
+            ring[r] = s
+            rfull[r].arrive()
+            tma_s += 1
+        elif a[0] == "mma":
+            s = mma_s
+            if not full[s % nv].passed((s // nv) & 1):
+                continue
+            if held[s % nop] != s:
+                return "MMA read another stage's operands"
+            queue.append(s)
+            mma_s += 1
+        else:
+            k = a[1]
+            s, st = dec[k]
+            r = s % nrg
+            if st == 0:  # read the box, release the slot
+                if not rfull[r].passed((s // nrg) & 1):
+                    continue
+                if ring[r] != s:
+                    return "read another stage's box"
+                if not fence:
+                    unread[r] = unread.get(r, 0) + 1  # the read may still be in flight
+                rempty[r].arrive()
+                dec[k][1] = 1
+            else:  # write the operand slot
+                if not fence:
+                    unread[r] -= 1
+                sp = s - nop
+                v, ph = (s % nop, s // nop - 1) if per_slot else (sp % nv, sp // nv)
+                if sp >= 0 and not empty[v].passed(ph & 1):
+                    continue
+                if sp >= 0 and sp not in done:
+                    return "operands overwritten before their MMA completed"
+                held[s % nop] = s
+                full[s % nv].arrive()
+                dec[k] = [s + 2, 0]
+    return "stalled"
+
+
+def test_tma_form_barrier_protocol():
+    """The kernel's protocol (operand barriers per stage mod lcm(2, stages),
+    one packet slot per box, fence before releasing a slot) is correct in
+    every interleaving tried, for the shipped two operand stages with four
+    packet slots and for three stages with two; per-physical-slot operand
+    barriers with three stages, or releasing packet slots without the fence,
+    are not."""
+    for nop, nrg in ((2, 4), (3, 2), (2, 2)):
+        for seed in range(60):
+            assert _run_protocol(nop, nrg, 24, seed) is None, (nop, nrg, seed)
+    assert any(_run_protocol(3, 2, 24, seed, per_slot=True) for seed in range(60))
+    assert any(_run_protocol(2, 4, 24, seed, fence=False) for seed in range(60))

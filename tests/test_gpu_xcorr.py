@@ -192,6 +192,14 @@ def test_coarse_xcorr_tcgen05_longest_slice_exact(tc_engine):
     raw = np.full((2, nspec, 8), 0x88, np.uint8)
     re, im = xcorr_coarse_4bit(cu(raw), 0, nspec, np.arange(4), 4, average=False)
     assert np.all(re.cpu().numpy() == nspec * 128) and np.all(im.cpu().numpy() == 0)
+    # the TMA form (8 contiguous channels, 16-byte rows) stores 16 x the
+    # levels: its partial sums reach 256 * 2^23 = 2^31, still exact in fp32
+    raw = np.full((2, nspec, 16), 0x88, np.uint8)
+    re, im = xcorr_coarse_4bit(cu(raw), 0, nspec, np.arange(8), 8, average=False)
+    assert np.all(re.cpu().numpy() == nspec * 128) and np.all(im.cpu().numpy() == 0)
+    raw = np.full((2, nspec, 16), 0x99, np.uint8)  # -7 everywhere: the largest negative products
+    re, im = xcorr_coarse_4bit(cu(raw), 0, nspec, np.arange(8), 8, average=False)
+    assert np.all(re.cpu().numpy() == nspec * 98) and np.all(im.cpu().numpy() == 0)
     # a mixed pattern at the same length: bit-exact against the int64 oracle
     raw = gen.raw_4bit_uniform(seed=17, nspec=nspec, nchan=4, nant=2)
     re, im = xcorr_coarse_4bit(cu(raw), 0, nspec, np.arange(4), 4, average=False)
