@@ -144,6 +144,7 @@ OPT_COARSE_TC_SLICE = 7
 OPT_PFB_TMA = 9
 OPT_FAULT_TEST = 10
 OPT_COARSE_TC_TMA = 11
+OPT_ROW_TC = 12
 DEFAULT_ROW_PREFETCH = 2
 
 
@@ -170,6 +171,13 @@ def set_coarse_tc_tma(on: int, device: Optional[int] = None) -> None:
     """tcgen05 coarse correlator: packet bytes staged by TMA into a ring in
     shared memory (1, default) or loaded into registers (0); both exact."""
     _lib.call("ab_ctx_set_option", _lib.ctx(device), OPT_COARSE_TC_TMA, int(on))
+
+
+def set_row_tc(on: int, device: Optional[int] = None) -> None:
+    """Streaming row stage (inverse real FFT of every spectrum) of streams
+    created from now on: a matrix product on the tcgen05 tensor cores (1,
+    default; 4-bit packets, at most 64 channels) or the FFT (0)."""
+    _lib.call("ab_ctx_set_option", _lib.ctx(device), OPT_ROW_TC, int(on))
 
 
 def set_pfb_tma(on: int, device: Optional[int] = None) -> None:

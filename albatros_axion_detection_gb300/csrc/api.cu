@@ -482,6 +482,10 @@ int ab_ctx_set_option(ab_ctx* ctx, int32_t option, int32_t value) {
       AB_CHECK_ARG(value == 0 || value == 1, "ab_ctx_set_option: coarse TMA staging must be 0 or 1");
       ctx->coarse_tc_tma = value;
       return AB_OK;
+    case AB_OPT_ROW_TC:
+      AB_CHECK_ARG(value == 0 || value == 1, "ab_ctx_set_option: tensor-core row stage must be 0 or 1");
+      ctx->row_tc = value;
+      return AB_OK;
     case AB_OPT_COARSE_TC_SLICE:
       AB_CHECK_ARG(value >= 0 && value % 64 == 0 && value <= (1 << 17),
                    "ab_ctx_set_option: tensor-core slice must be 0 (auto) or a multiple of 64 up to 131072");
@@ -504,6 +508,7 @@ int ab_ctx_destroy(ab_ctx* ctx) {
     cudaFree(const_cast<float2*>(kv.second.filt));
   }
   for (auto& kv : ctx->fir_taps) cudaFree((void*)kv.second.second);
+  for (auto& kv : ctx->row_bases) cudaFree(kv.second);
   for (auto& kv : ctx->scratch)
     if (kv.second.first) cudaFree(kv.second.first);
   delete ctx;

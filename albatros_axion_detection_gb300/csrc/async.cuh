@@ -69,6 +69,15 @@ __device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map
       : "memory");
 }
 
+// Untiled bulk copy of `bytes` (a multiple of 16; both addresses 16-byte
+// aligned) from global memory into shared memory at dst, completing on the
+// mbarrier bar.
+__device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+               "l"(reinterpret_cast<uint64_t>(src)), "r"(bytes), "r"(bar)
+               : "memory");
+}
+
 // Host: encode a tiled tensor map of `rank` (2 or 3) dimensions over
 // `base`: dims[0] innermost (contiguous), strides[i] the byte stride of
 // dimension i+1, box[] the tile, no swizzle, no interleave, 128-byte L2

@@ -61,6 +61,8 @@ struct ab_stream {
   float2* Y = nullptr;
   float2* vis = nullptr;
   int* d_fault = nullptr;    // set by a stage whose asynchronous copies did not arrive; vis is then NaN
+  const uint16_t* row_basis = nullptr;  // tensor-core row stage: basis image of the channel set (context cache)
+  int row_kb = 0;                       // its K-blocks (64 fp16 each)
   bool owns_scratch = true;  // interm[0], W, Y allocated here (not a shared workspace)
   int64_t nb_max = 0;
   int64_t chunks_done = 0;  // next chunk expected
@@ -258,6 +260,12 @@ extern "C" int ab_stream_create(ab_ctx* ctx, int64_t nant, int64_t nchan_raw, in
     delete st;
     return AB_ERR_CUDA;
   }
+  // the row stage as a tensor-core matrix product where it applies (else the FFT)
+  if (ctx->row_tc && bits == 4 && nsel <= 64 && P % 256 == 0 &&
+      get_row_tc_basis(ctx, P, ha, &st->row_basis, &st->row_kb) != AB_OK) {
+    st->row_basis = nullptr;
+    set_error("");
+  }
   *out = st;
   return AB_OK;
 }
@@ -415,7 +423,11 @@ static int stream_push(ab_stream* st, const uint8_t* raw, int64_t ant_stride, co
                  st->d_cols, st->d_abs, (int)st->nsel, st->bits};
   {
     StageTimer t(st, s, 0);
-    AB_TRY(launch_row_stage_packed4(st->ctx, src, st->nant, (int)nslice, P, st->planP, st->twP, cur, ld, s));
+    if (st->row_basis && ld % 8 == 0 && ((uintptr_t)cur & 31) == 0)
+      AB_TRY(launch_row_stage_tc(st->ctx, src, st->nant, (int)nslice, P, st->row_basis, st->row_kb, cur, ld,
+                                 st->d_fault, s));
+    else
+      AB_TRY(launch_row_stage_packed4(st->ctx, src, st->nant, (int)nslice, P, st->planP, st->twP, cur, ld, s));
     t.done(1);
   }
   // 2. time stage (with the PFB fold fused in when osamp >= 4)

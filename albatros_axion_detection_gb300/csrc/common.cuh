@@ -88,6 +88,7 @@ struct ab_ctx {
   std::map<std::vector<int>, float2*> streams;
   std::map<std::vector<int>, int2*> pair_tables;
   std::map<int, ab::BluesteinPass> bluestein;  // keyed by the prime radix
+  std::map<std::vector<int>, uint16_t*> row_bases;  // tensor-core row stage: basis image per (P, channel bins)
   // FFT plans chosen by the autotuner: length -> radix order (forces the
   // runtime-plan kernels for that length)
   std::map<int, std::vector<int>> plan_override;
@@ -103,6 +104,7 @@ struct ab_ctx {
   int coarse_engine = 0;     // fp16 coarse correlator: 0 = tcgen05 from 9 antennas up, 1 = warp-level mma.sync, 2 = tcgen05
   int coarse_tc_slice = 0;   // samples per CTA of the tcgen05 form (0: chosen per call)
   int coarse_tc_tma = 1;     // tcgen05 form: packet bytes staged by TMA (1) or loaded into registers (0)
+  int row_tc = 1;            // streaming row stage on the tensor cores where it applies (1) or the FFT (0)
   int test_withhold_stage = 0;  // failure-path test: the next tcgen05 correlator call withholds its first stage
   int pfb_tma = 0;           // streaming PFB band DFT: plain loads (0), TMA into the FFT buffers (1), persistent TMA (2)
   int row_ffts_per_cta = 8;  // row stage: 8 = time-paired spectra of one input per CTA;

@@ -31,6 +31,15 @@ struct Packed4Src {
 int launch_row_stage_packed4(ab_ctx* ctx, const Packed4Src& src, int nant, int nrows, int P, const FftPlan& plan,
                              const float2* twP, float* out, int64_t ld, cudaStream_t s);
 
+// Row stage on the tensor cores (row_tc.cu): 4-bit packets, 1 <= nsel <= 64,
+// P a multiple of 256, ld % 8 == 0 and a 32-byte aligned out.  The basis of
+// the channel set (absolute bins kabs) comes from get_row_tc_basis (cached in
+// the context; kb = K-blocks of 64 fp16).  *fault is set when a bounded wait
+// runs out.
+int get_row_tc_basis(ab_ctx* ctx, int P, const std::vector<int32_t>& kabs, const uint16_t** out, int* kb);
+int launch_row_stage_tc(ab_ctx* ctx, const Packed4Src& src, int nant, int nrows, int P, const uint16_t* basis, int kb,
+                        float* out, int64_t ld, int* fault, cudaStream_t s);
+
 // Row stage for dense c64 rows (nslice, P/2+1): out (P, ld) for one input.
 int launch_row_stage_c64(ab_ctx* ctx, const float2* dat, int64_t nslice, int P, const FftPlan& plan,
                          const float2* twP, float* out, int64_t ld, cudaStream_t s);

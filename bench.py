@@ -203,6 +203,9 @@ def run_ours(args):
     if args.row_prefetch >= 0:
         from albatros_axion_detection_gb300 import autotune
         autotune.set_row_prefetch(args.row_prefetch)
+    if args.row_tc >= 0:
+        from albatros_axion_detection_gb300 import autotune
+        autotune.set_row_tc(args.row_tc)
     if args.pfb_tma >= 0:
         from albatros_axion_detection_gb300 import autotune
         autotune.set_pfb_tma(args.pfb_tma)
@@ -715,6 +718,8 @@ def main():
                     help="stream: row stage 0 = one CTA per tile, 1 = persistent prefetching, "
                          "2 (default) = + shared twiddles")
     ap.add_argument("--check", action="store_true", help="uneven-batch: job-0 error of every file vs the FP64 oracle")
+    ap.add_argument("--row-tc", type=int, default=-1,
+                    help="stream: row stage on the tensor cores (1, library default) or the FFT (0)")
     ap.add_argument("--coarse-tma", type=int, default=-1,
                     help="coarse workloads: tcgen05 packet staging, 1 TMA (library default), 0 register loads")
     ap.add_argument("--mma-bits", type=int, default=0, help="coarse workloads: tensor-core operand bits (16 or 8)")
