@@ -130,10 +130,12 @@ def test_stream_row_stage_shapes(per_cta, nrows_extra):
     spec_map = np.where(present, np.arange(3 * acclen)[None, :], -1).astype(np.int32)
     ref, _ = po.repfb_xcorr_avg(raw, channels, spec_present=present, **kw)
     autotune.set_row_ffts_per_cta(per_cta)
+    autotune.set_row_tc(0)  # the FFT row stage's shapes
     try:
         vis, _ = run(raw, channels, spec_map=spec_map, **kw)
     finally:
         autotune.set_row_ffts_per_cta(8)
+        autotune.set_row_tc(1)
     check(vis, ref)
 
 
@@ -153,15 +155,49 @@ def test_row_prefetch_equals_one_cta_per_tile(bits, nrows_extra):
     present[0, 90:133] = False
     present[1, 600:611] = False
     spec_map = np.where(present, np.arange(3 * acclen)[None, :], -1).astype(np.int32)
-    a, _ = run(raw, channels, spec_map=spec_map, **kw)  # default: twiddles in shared memory
+    autotune.set_row_tc(0)  # the FFT row stage's forms
     try:
+        a, _ = run(raw, channels, spec_map=spec_map, **kw)  # default: twiddles in shared memory
         autotune.set_row_prefetch(0)
         b, _ = run(raw, channels, spec_map=spec_map, **kw)
         autotune.set_row_prefetch(1)  # twiddles from global memory
         c, _ = run(raw, channels, spec_map=spec_map, **kw)
     finally:
         autotune.set_row_prefetch(autotune.DEFAULT_ROW_PREFETCH)
+        autotune.set_row_tc(1)
     assert np.array_equal(a, b) and np.array_equal(a, c)
+    ref, _ = po.repfb_xcorr_avg(raw, channels, spec_present=present, **kw)
+    check(a, ref)
+
+
+@pytest.mark.parametrize("channels,chs,nrows_extra", [
+    (np.arange(0, 8), (0, 8), 0),                    # the DC bin (weight 1/P, no sine term)
+    (np.arange(2040, 2048), (0, 8), 3),              # the top channels a band may hold, ragged last spectrum tile
+    (np.arange(900, 905), (0, 5), 1),                # 5 channels: a partial channel quad
+    (np.arange(1000, 1033), (0, 33), 0),             # 33 channels: two K-blocks, the second partial
+    (np.arange(300, 364), (10, 50), 2),              # a 40-channel band of 64 raw channels
+])
+def test_row_stage_tensor_cores_vs_fft_and_oracle(channels, chs, nrows_extra):
+    """The row stage as a tensor-core product (the default for 4-bit packets
+    with at most 64 channels) against the FFT row stage and the FP64 oracle,
+    with missing spectra: the DC and Nyquist bins, partial channel quads and
+    K-blocks, spectrum tiles cut by the window's end."""
+    from albatros_axion_detection_gb300 import autotune
+    nchan = len(channels)
+    acclen, cut = 512 + nrows_extra, 32
+    raw = gen.raw_4bit(seed=int(channels[0]) + nrows_extra, nspec=3 * acclen, nchan=nchan, nant=2)
+    kw = dict(acclen=acclen, nchunks=3, nblock=24, chanstart=chs[0], chanend=chs[1], osamp=16, cut=cut)
+    present = np.ones((2, 3 * acclen), bool)
+    present[0, 200:260] = False
+    present[1, 1000:1003] = False
+    spec_map = np.where(present, np.arange(3 * acclen)[None, :], -1).astype(np.int32)
+    a, _ = run(raw, channels, spec_map=spec_map, **kw)
+    autotune.set_row_tc(0)
+    try:
+        b, _ = run(raw, channels, spec_map=spec_map, **kw)
+    finally:
+        autotune.set_row_tc(1)
+    assert np.linalg.norm(a - b) / np.linalg.norm(b) < 2e-6
     ref, _ = po.repfb_xcorr_avg(raw, channels, spec_present=present, **kw)
     check(a, ref)
 
