@@ -25,7 +25,7 @@ static PFN_cuTensorMapEncodeTiled_v12000 tmap_encoder() {
 }
 
 int encode_tmap(CUtensorMap* map, CUtensorMapDataType dtype, int rank, const void* base, const uint64_t* dims,
-                const uint64_t* strides, const uint32_t* box) {
+                const uint64_t* strides, const uint32_t* box, CUtensorMapSwizzle swizzle) {
   auto fn = tmap_encoder();
   if (!fn) {
     set_error("tensor map: the driver's cuTensorMapEncodeTiled is not available");
@@ -39,7 +39,7 @@ int encode_tmap(CUtensorMap* map, CUtensorMapDataType dtype, int rank, const voi
   }
   for (int i = 0; i + 1 < rank; i++) gs[i] = strides[i];
   CUresult r = fn(map, dtype, (cuuint32_t)rank, const_cast<void*>(base), gd, gs, bx, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                  CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+                  swizzle, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) {
     set_error("tensor map: cuTensorMapEncodeTiled failed (%d)", (int)r);
     return AB_ERR_ARG;

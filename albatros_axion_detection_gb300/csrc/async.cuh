@@ -78,13 +78,30 @@ __device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_
                : "memory");
 }
 
+// Store of a 2-D box from shared memory at src (laid out as the tensor map's
+// swizzle mode says) to the tensor at (x, y); x * element size must be a
+// multiple of 16 bytes and neither coordinate negative.  Elements outside the
+// tensor are not written.  Completion is tracked per thread by bulk groups.
+__device__ __forceinline__ void tma_store_2d(const CUtensorMap* map, int x, int y, uint32_t src) {
+  asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.tile.bulk_group [%0, {%1, %2}], [%3];" ::"l"(
+                   reinterpret_cast<uint64_t>(map)),
+               "r"(x), "r"(y), "r"(src)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+// all of this thread's bulk stores have read their shared-memory source
+__device__ __forceinline__ void bulk_wait_read_all() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+// all of this thread's bulk stores are complete
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+
 // Host: encode a tiled tensor map of `rank` (2 or 3) dimensions over
 // `base`: dims[0] innermost (contiguous), strides[i] the byte stride of
-// dimension i+1, box[] the tile, no swizzle, no interleave, 128-byte L2
-// promotion, zero fill outside the tensor.  The driver's encoder is reached
-// through the runtime (no link against the driver library).  Returns an
-// AB_* status.
+// dimension i+1, box[] the tile, the given swizzle (none by default), no
+// interleave, 128-byte L2 promotion, zero fill outside the tensor.  The
+// driver's encoder is reached through the runtime (no link against the
+// driver library).  Returns an AB_* status.
 int encode_tmap(CUtensorMap* map, CUtensorMapDataType dtype, int rank, const void* base, const uint64_t* dims,
-                const uint64_t* strides, const uint32_t* box);
+                const uint64_t* strides, const uint32_t* box,
+                CUtensorMapSwizzle swizzle = CU_TENSOR_MAP_SWIZZLE_NONE);
 
 }  // namespace ab

@@ -32,8 +32,9 @@
 //     fp16, K-major in the 128-byte swizzled layout) from the packets (rows
 //     through the spectrum map; missing rows and rows past the window are
 //     zero), then run the epilogue of every phase tile: tcgen05.ld of their
-//     32 tensor-memory lanes (phases) x 128 columns (spectra) and 32-byte
-//     stores of 128 consecutive rows of one column of the (n, t) output;
+//     32 tensor-memory lanes (phases) x 32 columns (spectra) at a time,
+//     staged in shared memory and written by a TMA tensor store (32 rows of
+//     128 bytes of the (n, t) output per store);
 //   * warp 9 streams the basis tiles (A_hi and A_lo of 128 phases, one bulk
 //     copy of the pre-swizzled image, 2 x KB x 16 KB) into a 2-slot ring;
 //   * warp 8 issues per phase tile 2 pols x 2 parts x 4 KB MMAs into one of
@@ -63,10 +64,12 @@ constexpr int kRtSplit = 2;                 // phase ranges per (spectrum tile, 
 constexpr double kRtScale = 2048.0;         // basis scale 2^11
 constexpr int kRtKbBytes = kRtTile * 128;   // one K-block of a 128-row operand: 64 fp16 a row
 
+constexpr int kRtStageBytes = 32 * 32 * 4;  // a worker warp's output staging tile: 32 phases x 32 spectra
+
 // shared memory: barriers (256 B), alignment, A ring (2 slots x 2 parts x KB
-// K-blocks), B (2 pols x KB K-blocks)
+// K-blocks), B (2 pols x KB K-blocks), 8 output staging tiles
 __host__ __device__ constexpr size_t row_tc_smem(int kb) {
-  return 256 + 1024 + (size_t)2 * 2 * kb * kRtKbBytes + (size_t)2 * kb * kRtKbBytes;
+  return 256 + 1024 + (size_t)2 * 2 * kb * kRtKbBytes + (size_t)2 * kb * kRtKbBytes + (size_t)8 * kRtStageBytes;
 }
 
 // fp16 bits of x (|x| <= 2), rounded to nearest even, subnormals included.
@@ -162,8 +165,9 @@ __device__ __forceinline__ uint32_t byte_to_h2(uint32_t b) {
 
 template <int KB>
 __global__ void __launch_bounds__(kRtThreads, 1)
-    row_stage_tc_kernel(Packed4Src src, int nrows, int P, int nant, const uint16_t* __restrict__ basis,
-                        float* __restrict__ out, int64_t ld, int nitems, int* __restrict__ fault) {
+    row_stage_tc_kernel(const __grid_constant__ CUtensorMap omap, Packed4Src src, int nrows, int P, int nant,
+                        const uint16_t* __restrict__ basis, float* __restrict__ out, int64_t ld, int nitems,
+                        int* __restrict__ fault) {
   constexpr int SLOT = 2 * KB * kRtKbBytes;  // one basis tile (hi, lo)
   constexpr int BPOL = KB * kRtKbBytes;      // one pol's B tile
   const int TPI = P / kRtTile / kRtSplit;    // phase tiles per item
@@ -175,6 +179,8 @@ __global__ void __launch_bounds__(kRtThreads, 1)
   const uint32_t abuf_s = raw_s + 256u + pad;
   uint8_t* bbuf = abuf + 2 * SLOT;
   const uint32_t bbuf_s = abuf_s + 2 * SLOT;
+  uint8_t* obuf = bbuf + 2 * BPOL;  // 8 staging tiles, 1024-byte aligned (128-byte swizzle)
+  const uint32_t obuf_s = bbuf_s + 2 * BPOL;
   auto a_full = [&](int i) { return bar_s + 8u * (uint32_t)i; };
   auto a_empty = [&](int i) { return bar_s + 8u * (uint32_t)(2 + i); };
   auto d_full = [&](int i) { return bar_s + 8u * (uint32_t)(4 + i); };
@@ -266,28 +272,37 @@ __global__ void __launch_bounds__(kRtThreads, 1)
           break;
         }
         tc_fence_after();
-        const int n = (ph * TPI + j) * kRtTile + 32 * q + lane;
-        float* dst = out + ((int64_t)(2 * a + pol_e) * P + n) * ld + t0;
+        // this warp's 32 phases (rows of the output) and the 128 spectra of
+        // the item, in four 32 x 32 blocks: each staged in shared memory in
+        // the 128-byte swizzled layout (row = phase, 16-byte chunk c at
+        // c ^ (row mod 8): the 8 lanes of a store phase hit distinct banks)
+        // and written by one TMA tensor store; the TMA engine skips rows of
+        // the output past nrows.
+        const int row0 = (2 * a + pol_e) * P + (ph * TPI + j) * kRtTile + 32 * q;
+        uint8_t* st = obuf + warp * kRtStageBytes;
+        const uint32_t st_s = obuf_s + warp * kRtStageBytes;
 #pragma unroll 1
         for (int c = 0; c < kRtTile / 32; c++) {
           float v[32];
           tc_ld32(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(slot * 256 + pol_e * 128 + 32 * c), v);
-          const int tb = t0 + 32 * c;
-          if (tb + 32 <= nrows) {
+          if (lane == 0) bulk_wait_read_all();  // the previous block has left the staging tile
+          __syncwarp();
 #pragma unroll
-            for (int i = 0; i < 32; i += 8)
-              st_global_v8(dst + 32 * c + i, v[i] * inv, v[i + 1] * inv, v[i + 2] * inv, v[i + 3] * inv,
-                           v[i + 4] * inv, v[i + 5] * inv, v[i + 6] * inv, v[i + 7] * inv);
-          } else {
-#pragma unroll
-            for (int i = 0; i < 32; i++)
-              if (tb + i < nrows) dst[32 * c + i] = v[i] * inv;
+          for (int i = 0; i < 8; i++)
+            *reinterpret_cast<float4*>(st + lane * 128 + ((i ^ (lane & 7)) << 4)) =
+                make_float4(v[4 * i] * inv, v[4 * i + 1] * inv, v[4 * i + 2] * inv, v[4 * i + 3] * inv);
+          fence_proxy_async();
+          __syncwarp();
+          if (lane == 0 && t0 + 32 * c < nrows) {
+            tma_store_2d(&omap, t0 + 32 * c, row0, st_s);
+            bulk_commit();
           }
         }
         tc_fence_before();
         mbar_arrive(d_empty(slot));
       }
     }
+    if (lane == 0) bulk_wait_all();  // every output block written before the CTA ends
   } else if (warp == 8) {
     if (lane == 0) {
       // ---------------- MMA issuer ----------------
@@ -366,12 +381,20 @@ int launch_row_stage_tc(ab_ctx* ctx, const Packed4Src& src, int nant, int nrows,
   const int64_t nitems = (int64_t)((nrows + kRtTile - 1) / kRtTile) * nant * kRtSplit;
   AB_CHECK_ARG(nitems < (1LL << 31), "row stage (tensor cores): too many work items");
   const int grid = (int)std::min<int64_t>(nitems, ctx->num_sms);
+  // output tensor: rows (input, phase) of nrows floats, ld apart; 32 x 32 boxes, 128-byte swizzle
+  CUtensorMap omap;
+  const uint64_t dims[2] = {(uint64_t)nrows, (uint64_t)2 * nant * P};
+  const uint64_t strides[1] = {(uint64_t)ld * sizeof(float)};
+  const uint32_t box[2] = {32, 32};
+  AB_TRY(encode_tmap(&omap, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, out, dims, strides, box, CU_TENSOR_MAP_SWIZZLE_128B));
   if (kb == 1) {
     AB_CUDA(cudaFuncSetAttribute(row_stage_tc_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    row_stage_tc_kernel<1><<<grid, kRtThreads, smem, s>>>(src, nrows, P, nant, basis, out, ld, (int)nitems, fault);
+    row_stage_tc_kernel<1><<<grid, kRtThreads, smem, s>>>(omap, src, nrows, P, nant, basis, out, ld, (int)nitems,
+                                                           fault);
   } else {
     AB_CUDA(cudaFuncSetAttribute(row_stage_tc_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    row_stage_tc_kernel<2><<<grid, kRtThreads, smem, s>>>(src, nrows, P, nant, basis, out, ld, (int)nitems, fault);
+    row_stage_tc_kernel<2><<<grid, kRtThreads, smem, s>>>(omap, src, nrows, P, nant, basis, out, ld, (int)nitems,
+                                                           fault);
   }
   AB_LAUNCH_CHECK();
   return AB_OK;
