@@ -487,12 +487,25 @@ struct FirItem {
   bool first, last;
 };
 
-__device__ __forceinline__ FirItem fir_item(int item, int nseg, int P, int S, int acclen, int O) {
+// Work item -> (input, segment, column): item = (in * nseg + seg) * P + n, so
+// that CTAs working side by side take neighbouring columns (whose 32-byte W
+// groups share lines).  P is a power of two (pshift = log2 P); r / nseg is
+// taken as a 64-bit product with mseg = ceil(2^32 / nseg), exact for
+// r < 2^32 / nseg (r = in * nseg + seg is far below that).
+struct ItemDecode {
+  int nseg, pshift;
+  uint64_t mseg;
+};
+__device__ __forceinline__ ItemDecode item_decode(int nseg, int P) {
+  return ItemDecode{nseg, __ffs(P) - 1, ((1ull << 32) + (uint64_t)nseg - 1) / (uint64_t)nseg};
+}
+__device__ __forceinline__ FirItem fir_item(int item, const ItemDecode& dc, int S, int acclen, int O) {
   FirItem it;
-  it.seg = item % nseg;
-  const int r = item / nseg;
-  it.n = r % P;
-  it.in = r / P;
+  const uint32_t r = (uint32_t)item >> dc.pshift;
+  const uint32_t q = (uint32_t)(((uint64_t)r * dc.mseg) >> 32);
+  it.n = item & ((1 << dc.pshift) - 1);
+  it.in = (int)q;
+  it.seg = (int)(r - q * (uint32_t)dc.nseg);
   it.s0 = it.seg * S;
   it.s1 = min(it.s0 + S, acclen);
   it.first = it.seg == 0;
@@ -564,8 +577,8 @@ __device__ __forceinline__ void prefetch_item_extras(float* st_taps, int K, int 
 // taking half the FFT, removed the fold's idle threads but met 2-way
 // conflicts on every y load and cost more than it saved.)
 template <int O>
-__device__ __forceinline__ int yidx(int q, int phi) {
-  return q + kYPad * ((q - phi + O) / O);
+__device__ __forceinline__ int yidx(int q, int phi) {  // q >= 0, 0 <= phi < O
+  return q + kYPad * (int)((unsigned)(q - phi + O) / (unsigned)O);
 }
 template <int O>
 __device__ __forceinline__ int y_phase(const FirItem& it, const FoldArgs& fa) {
@@ -689,9 +702,10 @@ __global__ void __launch_bounds__(kFirThreads, J <= 32 ? 2 : 1)
   float* stage0 = reinterpret_cast<float*>(smem4);
   float* ys = stage0 + 2 * Lay::STAGE;
   const int tid = threadIdx.x;
+  const ItemDecode dc = item_decode(nseg, P);
 
   auto prefetch = [&](int item, float* stage) {
-    const FirItem it = fir_item(item, nseg, P, S, acclen, O);
+    const FirItem it = fir_item(item, dc, S, acclen, O);
     const float* col = data + ((int64_t)it.in * P + it.n) * ld;
     // x window: stage[e] = x[(cut + ylo - J + e) mod nslice], e < nrows + 2J
     const int xbase = cut + it.ylo - J, nx = it.nrows + 2 * J;
@@ -713,7 +727,7 @@ __global__ void __launch_bounds__(kFirThreads, J <= 32 ? 2 : 1)
       cp_async_wait<0>();
     }
     __syncthreads();
-    const FirItem it = fir_item(item, nseg, P, S, acclen, O);
+    const FirItem it = fir_item(item, dc, S, acclen, O);
     const int yoff = it.ylo - it.s0 + 4 * O;  // y row of computed row ylo
     const int phi = y_phase<O>(it, fa);
     float* ysb = ys + (phi & 1);  // blocks start on 8-byte boundaries (yidx)
@@ -817,11 +831,12 @@ __global__ void __launch_bounds__(kFirThreads, iir_ctas_per_sm(U))
   float* zf = stage0 + 2 * Lay::STAGE;  // [3][kFirThreads] forward end states
   float* zb = zf + 3 * kFirThreads;     // [3][kFirThreads] backward end states
   const int tid = threadIdx.x;
+  const ItemDecode dc = item_decode(nseg, P);
   // threads that run: up to D past the one holding the last computed row
   auto threads_of = [](const FirItem& it) { return min(kFirThreads, (D * U + it.nrows - 1) / U + D + 1); };
 
   auto prefetch = [&](int item, float* stage) {
-    const FirItem it = fir_item(item, nseg, P, S, acclen, O);
+    const FirItem it = fir_item(item, dc, S, acclen, O);
     const float* col = data + ((int64_t)it.in * P + it.n) * ld;
     const int xbase = cut + it.ylo - D * U - 3, nx = threads_of(it) * U + 3;
     prefetch_window(stage, col, xbase, nx, nslice, window_shift(col, xbase, nx, nslice), tid);
@@ -841,7 +856,7 @@ __global__ void __launch_bounds__(kFirThreads, iir_ctas_per_sm(U))
       cp_async_wait<0>();
     }
     __syncthreads();
-    const FirItem it = fir_item(item, nseg, P, S, acclen, O);
+    const FirItem it = fir_item(item, dc, S, acclen, O);
     const int nthr = threads_of(it);
     const float* cf = stage + Lay::XS;
     const float w0 = cf[0], w1 = cf[1], w2 = cf[2], w3 = cf[3];
@@ -998,6 +1013,7 @@ static int launch_iir_o(const FirArgs& a, const FoldArgs& fa, cudaStream_t s) {
 int launch_fir_fold(const FirArgs& a, const FoldArgs& fa, cudaStream_t s) {
   AB_CHECK_ARG(fa.ntap == 4, "FIR time stage: needs ntap = 4");
   AB_CHECK_ARG(a.P <= 65535 && a.ninputs <= 65535, "FIR time stage: grid too large");
+  AB_CHECK_ARG(a.P > 0 && (a.P & (a.P - 1)) == 0, "FIR time stage: P = %d must be a power of two", a.P);
   AB_CHECK_ARG(a.row_tile == 16 || a.row_tile == 32 || a.row_tile == 64,
                "FIR time stage: row tile must be 16, 32 or 64");
   AB_CHECK_ARG(a.num_sms > 0, "FIR time stage: SM count unknown");
