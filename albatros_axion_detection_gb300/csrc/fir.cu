@@ -844,18 +844,18 @@ __global__ void __launch_bounds__(kFirThreads, iir_ctas_per_sm(U))
     cp_async_commit();
   };
 
+  // The next item's inputs are fetched into the other staging buffer right
+  // after this item's opening barrier: every thread has then finished the
+  // previous item, whose buffer that is, so no barrier is needed at the end
+  // of an item.
   int item = blockIdx.x, buf = 0;
   if (item < nitems) prefetch(item, stage0);
   for (; item < nitems; item += gridDim.x, buf ^= 1) {
     float* stage = stage0 + buf * Lay::STAGE;
     const int next = item + gridDim.x;
-    if (next < nitems) {
-      prefetch(next, stage0 + (buf ^ 1) * Lay::STAGE);
-      cp_async_wait<1>();
-    } else {
-      cp_async_wait<0>();
-    }
+    cp_async_wait<0>();  // this item's inputs: the only copies in flight
     __syncthreads();
+    if (next < nitems) prefetch(next, stage0 + (buf ^ 1) * Lay::STAGE);
     const FirItem it = fir_item(item, dc, S, acclen, O);
     const int nthr = threads_of(it);
     const float* cf = stage + Lay::XS;
@@ -931,7 +931,6 @@ __global__ void __launch_bounds__(kFirThreads, iir_ctas_per_sm(U))
     __syncthreads();
     fold_item_blocks<O>(ys, phi, reinterpret_cast<const float4*>(stage + Lay::XS + Lay::TAPS + 4 * O), it, fa, P, S,
                         acclen, state_out, tid);
-    __syncthreads();  // this staging buffer is refilled next
   }
 }
 
