@@ -11,8 +11,8 @@
 // Exactness.  The decoded nibbles are integers in [-7, 8] (0x8 decodes to +8,
 // as in albatros_analysis/src/correlations/unpacking.c:187-202), exact in
 // fp16; products are at most 64, and a CTA sums at most kTcMaxSlice = 2^17
-// samples, so every partial sum is an integer below 2^23 and the fp32
-// accumulation in tensor memory is exact in any order.  The partials are
+// samples, so every partial sum is an integer of magnitude at most 2^23 and
+// the fp32 accumulation in tensor memory is exact in any order.  The partials are
 // converted to int64 exactly and added into the per-chunk sums with int64
 // atomics (order-independent, bit-reproducible).
 //
@@ -323,8 +323,9 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 // v): a low nibble n in the mantissa of 0x7400 is the fp16 value 16384 +
 // 16 n, a high nibble in place (n << 4) under 0x6400 is 1024 + 16 n, so one
 // subtraction each gives 16 (n - 7) with no shift.  Every product is then a
-// multiple of 256 and every partial sum a multiple of 256 below 2^31 (64 x
-// 256 x kTcMaxSlice), exact in fp32; the epilogue divides by 256 (exact).
+// multiple of 256 and every partial sum a multiple of 256 of magnitude at
+// most 2^31 (64 x 256 x kTcMaxSlice), exact in fp32; the epilogue divides by
+// 256 (exact).
 //
 // Waits are bounded as in the form above; before exiting, warp 17 waits
 // (bounded) for every box it issued, so no copy lands after the CTA ends.
