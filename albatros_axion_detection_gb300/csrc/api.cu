@@ -475,7 +475,7 @@ int ab_ctx_set_option(ab_ctx* ctx, int32_t option, int32_t value) {
       ctx->pfb_tma = value;
       return AB_OK;
     case AB_OPT_FAULT_TEST:
-      AB_CHECK_ARG(value == 0 || value == 1, "ab_ctx_set_option: fault test must be 0 or 1");
+      AB_CHECK_ARG(value >= 0 && value <= 2, "ab_ctx_set_option: fault test must be 0, 1 or 2");
       ctx->test_withhold_stage = value;
       return AB_OK;
     case AB_OPT_COARSE_TC_TMA:

@@ -105,7 +105,8 @@ struct ab_ctx {
   int coarse_tc_slice = 0;   // samples per CTA of the tcgen05 form (0: chosen per call)
   int coarse_tc_tma = 1;     // tcgen05 form: packet bytes staged by TMA (1) or loaded into registers (0)
   int row_tc = 1;            // streaming row stage on the tensor cores where it applies (1) or the FFT (0)
-  int test_withhold_stage = 0;  // failure-path test: the next tcgen05 correlator call withholds its first stage
+  int test_withhold_stage = 0;  // failure-path test: 1 the next tcgen05 correlator call, 2 the next tensor-core
+                                // row-stage launch, withholds its first stage
   int pfb_tma = 0;           // streaming PFB band DFT: plain loads (0), TMA into the FFT buffers (1), persistent TMA (2)
   int row_ffts_per_cta = 8;  // row stage: 8 = time-paired spectra of one input per CTA;
                              // 4 or 2 = pol-paired spectra of one antenna per CTA

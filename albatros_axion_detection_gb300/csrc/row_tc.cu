@@ -44,7 +44,9 @@
 // Every barrier is waited on by one role only, phase after phase.  Waits are
 // bounded (about 2 s); one that runs out sets the stream's fault word (its
 // visibilities become NaN), and the copy warp waits for its copies in flight
-// before the CTA ends.
+// before the CTA ends.  For a test of that path without any fault, withhold
+// makes the workers keep back their first item's "B full" arrival: the MMA
+// thread's wait runs out, and with it the workers' and the copy warp's.
 #include <math.h>
 
 #include <vector>
@@ -167,7 +169,7 @@ template <int KB>
 __global__ void __launch_bounds__(kRtThreads, 1)
     row_stage_tc_kernel(const __grid_constant__ CUtensorMap omap, Packed4Src src, int nrows, int P, int nant,
                         const uint16_t* __restrict__ basis, float* __restrict__ out, int64_t ld, int nitems,
-                        int* __restrict__ fault) {
+                        int* __restrict__ fault, int withhold) {
   constexpr int SLOT = 2 * KB * kRtKbBytes;  // one basis tile (hi, lo)
   constexpr int BPOL = KB * kRtKbBytes;      // one pol's B tile
   const int TPI = P / kRtTile / kRtSplit;    // phase tiles per item
@@ -262,7 +264,7 @@ __global__ void __launch_bounds__(kRtThreads, 1)
         }
       }
       fence_proxy_async();
-      mbar_arrive(b_full);
+      if (!(withhold && li == 0)) mbar_arrive(b_full);
       const float inv = (float)(1.0 / kRtScale);
       for (int j = 0; j < TPI; j++, T++) {
         const int slot = T & 1;
@@ -387,14 +389,22 @@ int launch_row_stage_tc(ab_ctx* ctx, const Packed4Src& src, int nant, int nrows,
   const uint64_t strides[1] = {(uint64_t)ld * sizeof(float)};
   const uint32_t box[2] = {32, 32};
   AB_TRY(encode_tmap(&omap, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, out, dims, strides, box, CU_TENSOR_MAP_SWIZZLE_128B));
+  int withhold = 0;
+  {
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    if (ctx->test_withhold_stage == 2) {  // one launch only
+      withhold = 1;
+      ctx->test_withhold_stage = 0;
+    }
+  }
   if (kb == 1) {
     AB_CUDA(cudaFuncSetAttribute(row_stage_tc_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     row_stage_tc_kernel<1><<<grid, kRtThreads, smem, s>>>(omap, src, nrows, P, nant, basis, out, ld, (int)nitems,
-                                                           fault);
+                                                           fault, withhold);
   } else {
     AB_CUDA(cudaFuncSetAttribute(row_stage_tc_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     row_stage_tc_kernel<2><<<grid, kRtThreads, smem, s>>>(omap, src, nrows, P, nant, basis, out, ld, (int)nitems,
-                                                           fault);
+                                                           fault, withhold);
   }
   AB_LAUNCH_CHECK();
   return AB_OK;

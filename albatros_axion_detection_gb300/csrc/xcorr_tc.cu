@@ -12,9 +12,9 @@
 // as in albatros_analysis/src/correlations/unpacking.c:187-202), exact in
 // fp16; products are at most 64, and a CTA sums at most kTcMaxSlice = 2^17
 // samples, so every partial sum is an integer of magnitude at most 2^23 and
-// the fp32 accumulation in tensor memory is exact in any order.  The partials are
-// converted to int64 exactly and added into the per-chunk sums with int64
-// atomics (order-independent, bit-reproducible).
+// the fp32 accumulation in tensor memory is exact in any order.  The
+// partials are converted to int64 exactly and added into the per-chunk sums
+// with int64 atomics (order-independent, bit-reproducible).
 //
 // Tiles.  A 128-row operand tile holds CPT channels' rows (CPT = 2 with 64
 // rows a channel for up to 16 antennas, CPT = 1 with 128 rows for up to 32);
@@ -41,7 +41,7 @@
 // runs out sets the call's fault word, stops issuing work and drains, the
 // tensor memory is freed on every path, CTAs starting after it do nothing,
 // and the finalize kernel then writes INT64_MIN to every output of the call
-// (so a fault cannot pass for data).  AB_OPT_FAULT_TEST makes the next call's
+// (so a fault cannot pass for data).  AB_OPT_FAULT_TEST 1 makes the next call's
 // producers withhold their first stage, so that path can be tested without
 // a fault.
 #include <cuda_fp16.h>
@@ -628,8 +628,10 @@ int launch_coarse_tc(ab_ctx* ctx, const uint8_t* raw, int64_t ant_stride, int64_
   int withhold = 0;
   {
     std::lock_guard<std::mutex> lk(ctx->mu);
-    withhold = ctx->test_withhold_stage;
-    ctx->test_withhold_stage = 0;  // one call only
+    if (ctx->test_withhold_stage == 1) {  // one call only
+      withhold = 1;
+      ctx->test_withhold_stage = 0;
+    }
   }
   // TMA staging: 16 antennas at most, no row lists, 16-byte aligned rows
   const int64_t row_bytes = 2 * nchan;

@@ -105,8 +105,12 @@ int ab_ctx_set_time_filter(ab_ctx *ctx, int32_t mode, int32_t row_tile);
 /* AB_OPT_FAULT_TEST: 1 makes the next call of the tcgen05 coarse correlator
  * test its failure path without any fault: its producers withhold their
  * first stage, so the MMA thread's bounded wait (about 2 s) runs out, the
- * call's outputs are all INT64_MIN, and the tensor memory is freed.  The
- * setting applies to one call. */
+ * call's outputs are all INT64_MIN, and the tensor memory is freed.  2 does
+ * the same for the next launch of the streaming chain's tensor-core row
+ * stage: its workers withhold their first item's decoded tiles, every role's
+ * bounded wait runs out, the stream's fault word is set (its visibilities
+ * are NaN until ab_stream_reset), and the tensor memory is freed.  The
+ * setting applies to one call or launch. */
 #define AB_OPT_FAULT_TEST 10
 /* AB_OPT_COARSE_TC_TMA: how the tcgen05 coarse correlator (up to 16
  * antennas, contiguous 16-byte-aligned channel groups, no row lists) fetches

@@ -202,6 +202,41 @@ def test_row_stage_tensor_cores_vs_fft_and_oracle(channels, chs, nrows_extra):
     check(a, ref)
 
 
+def test_row_stage_tensor_cores_wait_timeout_reports_fault():
+    """Failure path of the tensor-core row stage's bounded waits, without a
+    GPU fault: its workers withhold their first item's decoded tiles (nothing
+    else signals them), the MMA thread's wait runs out after about 2 s and
+    with it the other roles', the stream's fault word turns the visibilities
+    NaN, and the tensor memory was freed: after a reset the same stream gives
+    the visibilities of a fresh one."""
+    import time
+    from albatros_axion_detection_gb300 import _lib, autotune, stream
+    acclen, nchunks, nchan = 512, 3, 8
+    raw = torch.from_numpy(gen.raw_4bit(seed=57, nspec=nchunks * acclen, nchan=nchan, nant=2)).cuda()
+    mk = lambda: stream.StreamCorrelator(2, np.arange(40, 48), 0, nchan, acclen, nchunks, 16, 16, 32, nchan_raw=nchan)
+    a, b = mk(), mk()
+    try:
+        for j in range(nchunks):
+            a.push(raw, j, final=(j == nchunks - 1))
+        good = a.vis_device().clone()
+        _lib.call("ab_ctx_set_option", _lib.ctx(), autotune.OPT_FAULT_TEST, 2)
+        t0 = time.time()
+        for j in range(nchunks):
+            b.push(raw, j, final=(j == nchunks - 1))
+        torch.cuda.synchronize()
+        assert time.time() - t0 < 30
+        assert torch.isnan(b.vis_device()).all()
+        b.reset()
+        for j in range(nchunks):
+            b.push(raw, j, final=(j == nchunks - 1))
+        torch.cuda.synchronize()
+        assert torch.isfinite(good).all() and torch.equal(b.vis_device(), good)
+    finally:
+        _lib.call("ab_ctx_set_option", _lib.ctx(), autotune.OPT_FAULT_TEST, 0)
+        a.close()
+        b.close()
+
+
 def test_run_from_host_overlapped_copies_equal_device_run():
     """Per-chunk host->device copies on a side stream, each push waiting on
     its own chunk's copy, give the visibilities of a run on device packets."""
