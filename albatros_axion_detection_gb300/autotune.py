@@ -176,7 +176,7 @@ def set_coarse_tc_tma(on: int, device: Optional[int] = None) -> None:
 def set_row_tc(on: int, device: Optional[int] = None) -> None:
     """Streaming row stage (inverse real FFT of every spectrum) of streams
     created from now on: a matrix product on the tcgen05 tensor cores (1,
-    default; 4-bit packets, at most 64 channels) or the FFT (0)."""
+    default; 4-bit or 1-bit packets, at most 64 channels) or the FFT (0)."""
     _lib.call("ab_ctx_set_option", _lib.ctx(device), OPT_ROW_TC, int(on))
 
 

@@ -261,7 +261,7 @@ extern "C" int ab_stream_create(ab_ctx* ctx, int64_t nant, int64_t nchan_raw, in
     return AB_ERR_CUDA;
   }
   // the row stage as a tensor-core matrix product where it applies (else the FFT)
-  if (ctx->row_tc && bits == 4 && nsel <= 64 && P % 256 == 0 &&
+  if (ctx->row_tc && nsel <= 64 && P % 256 == 0 &&
       get_row_tc_basis(ctx, P, ha, &st->row_basis, &st->row_kb) != AB_OK) {
     st->row_basis = nullptr;
     set_error("");

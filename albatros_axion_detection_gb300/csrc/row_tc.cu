@@ -1,6 +1,6 @@
 // row_tc.cu -- the IPFB row stage (inverse real FFT of every spectrum) on the
-// fifth-generation tensor cores, for packed 4-bit spectra with at most 64
-// selected channels.
+// fifth-generation tensor cores, for packed 4-bit or 1-bit spectra with at
+// most 64 selected channels.
 //
 // Reference: cupy_ipfb (albatros_analysis/src/utils/pfb_gpu_utils.py:56-91)
 // starts with an irfft of every (nslice, 2049) spectrum row to 4096 samples;
@@ -13,7 +13,8 @@
 // the sum running over the selected channels only.  For a tile of spectra
 // that is a matrix product D[n][t] = sum_j A[n][j] B[t][j] with
 // j = 2 k' + (0: Re, 1: Im) over the nsel selected channels k':
-//   * B holds the decoded 4-bit levels (integers in [-7, 8], exact in fp16);
+//   * B holds the decoded levels (4-bit: integers in [-7, 8]; 1-bit: signs
+//     +-1), exact in fp16;
 //   * A is the basis, scaled by 2^11 so that its entries lie in [-1, 1], and
 //     split as A = A_hi + A_lo with both parts fp16 (A_hi the rounding of A,
 //     A_lo of the remainder), computed once per channel set in FP64 on the
@@ -165,6 +166,13 @@ __device__ __forceinline__ uint32_t byte_to_h2(uint32_t b) {
   return nib_to_h2(nib_plus7((b >> 4) | ((b & 15u) << 16)));
 }
 
+// fp16 pair (re, im) = (+1 if bit 1 of v is set, else -1; the same for bit
+// 0): one pol of a 1-bit channel, whose nibble holds r0 i0 r1 i1 from the
+// top bit down (albatros_analysis/src/correlations/unpacking.c:207-246).
+__device__ __forceinline__ uint32_t bits_to_h2(uint32_t v) {
+  return 0x3C003C00u | ((~v & 2u) << 14) | ((~v & 1u) << 31);
+}
+
 template <int KB>
 __global__ void __launch_bounds__(kRtThreads, 1)
     row_stage_tc_kernel(const __grid_constant__ CUtensorMap omap, Packed4Src src, int nrows, int P, int nant,
@@ -250,12 +258,22 @@ __global__ void __launch_bounds__(kRtThreads, 1)
           uint32_t w0[4] = {0u, 0u, 0u, 0u}, w1[4] = {0u, 0u, 0u, 0u};
           if (row >= 0) {
             const uint8_t* prow = src.raw + (int64_t)a * src.ant_stride + (int64_t)row * src.row_bytes;
+            if (src.bits == 4) {  // bytes 2c (pol 0) and 2c + 1 (pol 1)
 #pragma unroll
-            for (int j = 0; j < 4; j++) {
-              if (cols[j] < 0) continue;
-              const uint32_t pb = __ldg(reinterpret_cast<const unsigned short*>(prow + 2 * cols[j]));
-              w0[j] = byte_to_h2(pb & 0xffu);
-              w1[j] = byte_to_h2(pb >> 8);
+              for (int j = 0; j < 4; j++) {
+                if (cols[j] < 0) continue;
+                const uint32_t pb = __ldg(reinterpret_cast<const unsigned short*>(prow + 2 * cols[j]));
+                w0[j] = byte_to_h2(pb & 0xffu);
+                w1[j] = byte_to_h2(pb >> 8);
+              }
+            } else {  // 1-bit: the high nibble of byte c/2 for even c, the low one for odd c
+#pragma unroll
+              for (int j = 0; j < 4; j++) {
+                if (cols[j] < 0) continue;
+                const uint32_t q = ((uint32_t)__ldg(prow + (cols[j] >> 1)) >> ((cols[j] & 1) ? 0 : 4)) & 15u;
+                w0[j] = bits_to_h2(q >> 2);
+                w1[j] = bits_to_h2(q);
+              }
             }
           }
           const uint32_t off = (uint32_t)(c4 / 8) * kRtKbBytes + sw128_offset(r, c4 % 8);
@@ -375,7 +393,7 @@ __global__ void __launch_bounds__(kRtThreads, 1)
 
 int launch_row_stage_tc(ab_ctx* ctx, const Packed4Src& src, int nant, int nrows, int P, const uint16_t* basis, int kb,
                         float* out, int64_t ld, int* fault, cudaStream_t s) {
-  AB_CHECK_ARG(src.bits == 4 && src.nsel >= 1 && src.nsel <= 64 && kb >= 1 && kb <= 2 && P % (kRtTile * kRtSplit) == 0 &&
+  AB_CHECK_ARG((src.bits == 4 || src.bits == 1) && src.nsel >= 1 && src.nsel <= 64 && kb >= 1 && kb <= 2 && P % (kRtTile * kRtSplit) == 0 &&
                    ld % 8 == 0 && ((uintptr_t)out & 31) == 0 && nrows >= 1,
                "row stage (tensor cores): unsupported shape");
   const size_t smem = row_tc_smem(kb);

@@ -119,7 +119,7 @@ int ab_ctx_set_time_filter(ab_ctx *ctx, int32_t mode, int32_t row_tile);
  * in shared memory; 0 plain 16-byte loads into registers.  Both are exact. */
 #define AB_OPT_COARSE_TC_TMA 11
 /* AB_OPT_ROW_TC: the streaming chain's IPFB row stage (inverse real FFT of
- * every spectrum) for 4-bit packets with at most 64 selected channels:
+ * every spectrum) for 4-bit or 1-bit packets with at most 64 selected channels:
  * 1 (default) as a matrix product on the tcgen05 tensor cores (the decoded
  * levels, exact in fp16, times an FP64-built cos/sin basis split into two
  * fp16 parts, fp32 accumulation); 0 the FFT.  Taken by streams created after

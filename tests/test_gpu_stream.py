@@ -178,15 +178,31 @@ def test_row_prefetch_equals_one_cta_per_tile(bits, nrows_extra):
     (np.arange(300, 364), (10, 50), 2),              # a 40-channel band of 64 raw channels
 ])
 def test_row_stage_tensor_cores_vs_fft_and_oracle(channels, chs, nrows_extra):
-    """The row stage as a tensor-core product (the default for 4-bit packets
-    with at most 64 channels) against the FFT row stage and the FP64 oracle,
-    with missing spectra: the DC and Nyquist bins, partial channel quads and
-    K-blocks, spectrum tiles cut by the window's end."""
+    """The row stage as a tensor-core product (the default for 4-bit and
+    1-bit packets with at most 64 channels) against the FFT row stage and the
+    FP64 oracle, with missing spectra: the DC and Nyquist bins, partial
+    channel quads and K-blocks, spectrum tiles cut by the window's end."""
+    acclen = 512 + nrows_extra
+    raw = gen.raw_4bit(seed=int(channels[0]) + nrows_extra, nspec=3 * acclen, nchan=len(channels), nant=2)
+    _row_tc_vs_fft_and_oracle(raw, channels, chs, acclen, bits=4)
+
+
+@pytest.mark.parametrize("nchan,chs,nrows_extra", [
+    (32, (0, 32), 1),   # 32 channels: one K-block
+    (64, (3, 61), 0),   # 58 of 64 channels from an odd column: two K-blocks, a partial quad
+    (10, (1, 9), 2),    # 8 channels, every other one in a low nibble
+])
+def test_row_stage_tensor_cores_1bit_vs_fft_and_oracle(nchan, chs, nrows_extra):
+    """1-bit sign packets (r0 i0 r1 i1 per channel, two channels a byte)
+    through the tensor-core row stage: as the FFT row stage and the oracle."""
+    acclen = 512 + nrows_extra
+    raw = np.stack([gen.raw_1bit(seed=40 + nchan + a, nspec=3 * acclen, nchan=nchan) for a in range(2)])
+    _row_tc_vs_fft_and_oracle(raw, np.arange(1200, 1200 + nchan), chs, acclen, bits=1)
+
+
+def _row_tc_vs_fft_and_oracle(raw, channels, chs, acclen, bits):
     from albatros_axion_detection_gb300 import autotune
-    nchan = len(channels)
-    acclen, cut = 512 + nrows_extra, 32
-    raw = gen.raw_4bit(seed=int(channels[0]) + nrows_extra, nspec=3 * acclen, nchan=nchan, nant=2)
-    kw = dict(acclen=acclen, nchunks=3, nblock=24, chanstart=chs[0], chanend=chs[1], osamp=16, cut=cut)
+    kw = dict(acclen=acclen, nchunks=3, nblock=24, chanstart=chs[0], chanend=chs[1], osamp=16, cut=32, bits=bits)
     present = np.ones((2, 3 * acclen), bool)
     present[0, 200:260] = False
     present[1, 1000:1003] = False
